@@ -1,0 +1,222 @@
+/*
+ * tapkee_gb300.h -- C ABI of the GB300 local-neighborhood operator.
+ *
+ * This library computes, on one GB300 GPU (sm_103a), the stage that the
+ * reference (lisitsyn/tapkee 1.3.4) runs inside
+ *   tapkee::with((method=KernelLocallyLinearEmbedding | KernelLocalTangentSpaceAlignment,
+ *                 neighbors_method=Brute, num_neighbors=k, klle_shift=s)).embedUsing(X)
+ * before its eigensolver: brute-force kNN under the linear kernel, the
+ * connectivity check with its 2k retry, LLE reconstruction weights or LTSA
+ * tangent bases, and the sparse alignment matrix M in CSR form.
+ *
+ * Conventions
+ *   - X is points-major: point i occupies X[i*ldx .. i*ldx + D), which is the
+ *     memory layout of the reference's D x N column-major DenseMatrix
+ *     (defines/types.hpp:23). dtype is TK_F32 or TK_F64.
+ *   - Every buffer is caller-owned. Pointers may be host memory (pageable or
+ *     pinned) or device memory of the context's GPU; the library detects which.
+ *   - Indices are int32 (the reference's IndexType, defines/types.hpp:19);
+ *     CSR row pointers are int64, columns int32, values double.
+ *   - No C++ exception crosses this boundary: every call returns a tk_status.
+ *     tk_last_error() gives the message of the last failing call on a context.
+ *   - One tk_ctx owns one CUDA stream and its scratch memory. Calls on one
+ *     context are serialised by the caller; different contexts are independent.
+ */
+#ifndef TAPKEE_GB300_H
+#define TAPKEE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The C++ facade maps them onto the reference's exception types
+ * (exceptions.hpp:14-91). */
+typedef enum tk_status
+{
+    TK_OK = 0,
+    TK_ERR_INVALID_ARG = 1,      /* wrong_parameter_error                          */
+    TK_ERR_NO_DATA = 2,          /* no_data_error (N == 0)                         */
+    TK_ERR_OOM = 3,              /* not_enough_memory_error                        */
+    TK_ERR_CUDA = 4,             /* a CUDA runtime call failed                     */
+    TK_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up             */
+    TK_ERR_CANCELLED = 6,        /* cancelled_exception (cancel_function true)     */
+    TK_ERR_BUFFER_TOO_SMALL = 7, /* output capacity below the required size       */
+    TK_ERR_UNSUPPORTED = 8,      /* unsupported_method_error                       */
+    TK_ERR_NO_DEVICE = 9,        /* no usable sm_103a device                       */
+    TK_ERR_INTERNAL = 10         /* an internal consistency check failed           */
+} tk_status;
+
+typedef enum tk_dtype
+{
+    TK_F32 = 0,
+    TK_F64 = 1
+} tk_dtype;
+
+/* Method tags (defines/methods.hpp:74,82). */
+typedef enum tk_method
+{
+    TK_METHOD_KLLE = 0, /* KernelLocallyLinearEmbedding            */
+    TK_METHOD_KLTSA = 1 /* KernelLocalTangentSpaceAlignment         */
+} tk_method;
+
+/* Distance screening engine of the brute kNN. Both are followed by the same
+ * exact FP64 re-rank and certification, so they return identical neighbours. */
+typedef enum tk_screen
+{
+    TK_SCREEN_TENSOR = 0, /* tcgen05 tensor-core fp16 split GEMM (default) */
+    TK_SCREEN_FP32 = 1    /* plain FP32 CUDA-core GEMM                     */
+} tk_screen;
+
+/* Log levels, mirroring utils/logging.hpp:89-144. */
+typedef enum tk_log_level
+{
+    TK_LOG_INFO = 0,
+    TK_LOG_WARNING = 1,
+    TK_LOG_DEBUG = 2,
+    TK_LOG_ERROR = 3,
+    TK_LOG_BENCHMARK = 4
+} tk_log_level;
+
+typedef void (*tk_log_fn)(int level, const char* message, void* user);
+
+typedef struct tk_ctx tk_ctx;
+
+/* Parameters of the stage; the defaults are the reference keyword defaults
+ * (defines/keywords.hpp). */
+typedef struct tk_params
+{
+    int method;             /* tk_method; required                             keywords.hpp:35  */
+    int num_neighbors;      /* default 5, must lie in [3, N)                   keywords.hpp:112 */
+    int target_dimension;   /* default 2, must lie in [1, N)                   keywords.hpp:125 */
+    double klle_shift;      /* default 1e-3                                    keywords.hpp:248 */
+    double nullspace_shift; /* default 1e-9                                    keywords.hpp:235 */
+    int check_connectivity; /* default 1                                       keywords.hpp:272 */
+    int screen;             /* tk_screen, default TK_SCREEN_TENSOR                              */
+    int (*cancel_function)(void); /* polled between stages; NULL = never cancel              */
+} tk_params;
+
+/* Statistics of one brute kNN call. */
+typedef struct tk_knn_stats
+{
+    int64_t rows_uncertified; /* rows whose screened candidate list could not be
+                                 certified and were recomputed exactly          */
+    int32_t candidates;       /* candidates kept per row by the screen          */
+    int32_t screen;           /* engine used                                    */
+} tk_knn_stats;
+
+/* Summary of the operator held by a context after tk_local_operator(). */
+typedef struct tk_operator_info
+{
+    int64_t n;                /* number of points                                   */
+    int32_t k;                /* neighbours per point actually used (after the
+                                 clamp to N-1 and any connectivity doublings)       */
+    int32_t method;           /* tk_method                                          */
+    int32_t target_dimension; /* td (LTSA basis width)                              */
+    int32_t connectivity_retries; /* how many times k was doubled                   */
+    int64_t nnz;              /* non-zeros of M                                     */
+    int64_t rows_uncertified; /* see tk_knn_stats                                   */
+    float stage_ms[6];        /* device time per stage: knn, connectivity, weights,
+                                 assembly, total, reserved                           */
+} tk_operator_info;
+
+/* ---- context -------------------------------------------------------------- */
+
+/* Fills p with the reference defaults (method = TK_METHOD_KLLE). */
+void tk_params_default(tk_params* p);
+
+/* Creates a context on `device`. `stream` is a cudaStream_t to run on, or NULL
+ * for a context-owned non-blocking stream. Fails with TK_ERR_NO_DEVICE unless the
+ * device is compute capability 10.3. */
+int tk_ctx_create(int device, void* stream, tk_ctx** out);
+int tk_ctx_destroy(tk_ctx* ctx);
+
+/* Message of the last failing call on ctx (never NULL). */
+const char* tk_last_error(const tk_ctx* ctx);
+const char* tk_status_string(int status);
+
+/* Installs a log sink (utils/logging.hpp:119-137, set_logger_impl); NULL restores
+ * the default (warnings and errors to stderr). */
+int tk_set_log_callback(tk_ctx* ctx, tk_log_fn fn, void* user);
+
+/* Library version string ("major.minor.patch"). */
+const char* tk_version(void);
+
+/* ---- stage entry points ----------------------------------------------------- */
+
+/* Brute-force k nearest neighbours of every point under the kernel-trick
+ * distance sqrt(k(x,x) - 2 k(x,y) + k(y,y)) with the linear kernel.
+ * Replaces find_neighbors_bruteforce_impl (neighbors/neighbors.hpp:119-149) with
+ * KernelDistance (neighbors/neighbors.hpp:40-55) over eigen_kernel_callback
+ * (callbacks/eigen_callbacks.hpp:34-46).
+ * idx_out (N x k) receives, per row, the k nearest other points ordered by
+ * (distance, index); d2_out (N x k, optional) their FP64 squared distances.
+ * Requires 1 <= k <= N-1. */
+int tk_knn_brute(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, int k, int screen,
+                 int32_t* idx_out, double* d2_out, tk_knn_stats* stats);
+
+/* Reachability of every vertex from vertex 0 along kNN out-edges.
+ * Replaces is_connected (neighbors/connected.hpp:19-62). *connected = 1 or 0. */
+int tk_check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx, int* connected);
+
+/* LLE reconstruction weights: per point, C = Gram of (neighbours - x) plus
+ * klle_shift * trace(C) * I, w = C^{-1} 1 / sum. W_out is N x k, aligned with idx.
+ * Replaces the per-point solve of linear_weight_matrix
+ * (routines/locally_linear.hpp:107-131). */
+int tk_lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                   int k, double klle_shift, double* W_out);
+
+/* LTSA tangent basis: per point, the eigenvectors of the td largest eigenvalues
+ * of the double-centred neighbour Gram. V_out is N x k x td (sign of each vector
+ * is arbitrary); the alignment block is P = (1/k) 1 1^T + V V^T.
+ * Replaces the per-point part of tangent_weight_matrix
+ * (routines/locally_linear.hpp:45-63, with centerMatrix utils/matrix.hpp:12-19). */
+int tk_ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                  int k, int td, double* V_out);
+
+/* Sparse alignment matrix M in CSR (= CSC, M is symmetric), duplicates summed:
+ *   TK_METHOD_KLLE : M = (I - W)^T (I - W) + shift I   from weights = W (N x k)
+ *                    (triplets of routines/locally_linear.hpp:133-146)
+ *   TK_METHOD_KLTSA: M = shift I + sum_i S_i^T (I - P_i) S_i from weights = V
+ *                    (N x k x td) (triplets of routines/locally_linear.hpp:65-77)
+ * followed by sparse_matrix_from_triplets (utils/sparse.hpp:16-21).
+ * Columns are ascending within each row. Two-phase: with col_idx == NULL the
+ * call only writes row_ptr (if non-NULL) and *nnz_io = nnz; with buffers whose
+ * capacity *nnz_io is below nnz it returns TK_ERR_BUFFER_TOO_SMALL and sets
+ * *nnz_io = nnz. */
+int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, int64_t* nnz_io);
+
+/* The whole stage of KernelLocallyLinearEmbeddingImplementation::embed /
+ * KernelLocalTangentSpaceAlignmentImplementation::embed up to the eigensolver
+ * (methods/kernel_locally_linear_embedding.hpp:22-30,
+ *  methods/kernel_local_tangent_space_alignment.hpp:22-30): parameter checks of
+ * ImplementationBase (methods/base.hpp:31-49,82-88), find_neighbors with the k
+ * clamp and connectivity retry (neighbors/neighbors.hpp:173-213), weights, and M.
+ * The result stays on the device, owned by ctx, until the next call; read it
+ * with tk_operator_copy / tk_operator_device_views. info may be NULL. */
+int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int dtype, int64_t N, int D,
+                      int64_t ldx, tk_operator_info* info);
+
+/* Copies the operator held by ctx into caller buffers (host or device; any may
+ * be NULL): idx N x k, weights (N x k for KLLE, N x k x td for KLTSA),
+ * row_ptr N+1, col_idx nnz, vals nnz. */
+int tk_operator_copy(tk_ctx* ctx, int32_t* idx, double* weights, int64_t* row_ptr, int32_t* col_idx,
+                     double* vals);
+
+/* Device pointers of the operator held by ctx (valid until the next call on ctx). */
+int tk_operator_device_views(tk_ctx* ctx, const int32_t** idx, const double** weights, const int64_t** row_ptr,
+                             const int32_t** col_idx, const double** vals);
+
+/* Information about the operator held by ctx. */
+int tk_operator_get_info(const tk_ctx* ctx, tk_operator_info* info);
+
+/* Waits for all work queued on the context's stream. */
+int tk_ctx_synchronize(tk_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAPKEE_GB300_H */

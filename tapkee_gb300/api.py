@@ -1,0 +1,449 @@
+"""Host-side mirror of the reference's interface for the local-neighborhood stage.
+
+* ``Context`` -- one GPU context (CUDA stream + scratch) with one method per C ABI
+  stage: ``knn_brute``, ``check_connected``, ``lle_weights``, ``ltsa_basis``,
+  ``assemble`` and the whole stage ``local_operator``.
+* ``embed(data, method='lle', ...)`` -- the keyword signature of the reference's
+  Python module (src/python/nanobind_extension.cpp:28-96): ``data`` is
+  features x samples, the result samples x target_dimension.
+* ``with_(method=..., num_neighbors=...).embed_using(matrix)`` -- the chain of
+  ``tapkee::with((...)).embedUsing(matrix)`` (chain_interface.hpp:471-500).
+
+Errors map onto the reference's exception types (exceptions.hpp:14-91).
+Arrays may be numpy (host) or torch tensors (host or CUDA); outputs follow the
+input: numpy in, numpy out; CUDA tensor in, CUDA tensors out.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi as C
+
+# ---------------------------------------------------------------- exceptions
+
+
+class TapkeeError(Exception):
+    """Base class of the errors raised by this package."""
+
+
+class WrongParameterError(TapkeeError, ValueError):
+    """tapkee::wrong_parameter_error"""
+
+
+class NoDataError(TapkeeError, ValueError):
+    """tapkee::no_data_error"""
+
+
+class NotEnoughMemoryError(TapkeeError, MemoryError):
+    """tapkee::not_enough_memory_error"""
+
+
+class CancelledError(TapkeeError):
+    """tapkee::cancelled_exception"""
+
+
+class UnsupportedMethodError(TapkeeError):
+    """tapkee::unsupported_method_error"""
+
+
+class EigendecompositionError(TapkeeError):
+    """tapkee::eigendecomposition_error"""
+
+
+class MultipleParameterError(TapkeeError):
+    """tapkee::multiple_parameter_error"""
+
+
+class MissedParameterError(TapkeeError):
+    """tapkee::missed_parameter_error"""
+
+
+class DeviceError(TapkeeError, RuntimeError):
+    """A CUDA failure or a device-side check (including a bounded wait that expired)."""
+
+
+_STATUS_EXC = {
+    C.TK_ERR_INVALID_ARG: WrongParameterError,
+    C.TK_ERR_NO_DATA: NoDataError,
+    C.TK_ERR_OOM: NotEnoughMemoryError,
+    C.TK_ERR_CUDA: DeviceError,
+    C.TK_ERR_TIMEOUT: DeviceError,
+    C.TK_ERR_CANCELLED: CancelledError,
+    C.TK_ERR_BUFFER_TOO_SMALL: WrongParameterError,
+    C.TK_ERR_UNSUPPORTED: UnsupportedMethodError,
+    C.TK_ERR_NO_DEVICE: DeviceError,
+    C.TK_ERR_INTERNAL: DeviceError,
+}
+
+METHODS = {
+    "lle": C.TK_METHOD_KLLE,
+    "locally_linear_embedding": C.TK_METHOD_KLLE,
+    "klle": C.TK_METHOD_KLLE,
+    "ltsa": C.TK_METHOD_KLTSA,
+    "local_tangent_space_alignment": C.TK_METHOD_KLTSA,
+    "kltsa": C.TK_METHOD_KLTSA,
+}
+SCREENS = {"tensor": C.TK_SCREEN_TENSOR, "fp32": C.TK_SCREEN_FP32}
+
+
+def _raise(ctx_ptr, status, lib):
+    if status == C.TK_OK:
+        return
+    msg = lib.tk_last_error(ctx_ptr).decode() if ctx_ptr else lib.tk_status_string(status).decode()
+    raise _STATUS_EXC.get(status, DeviceError)(msg or lib.tk_status_string(status).decode())
+
+
+# ---------------------------------------------------------------- arrays
+
+
+def _torch():
+    try:
+        import torch  # noqa: F401
+        return torch
+    except Exception:  # pragma: no cover
+        return None
+
+
+def _is_torch(x):
+    t = _torch()
+    return t is not None and isinstance(x, t.Tensor)
+
+
+class _Buf:
+    """A contiguous array and its address, numpy or torch."""
+
+    def __init__(self, arr, kind):
+        self.arr = arr
+        self.kind = kind  # "np" | "torch"
+
+    @property
+    def ptr(self):
+        return self.arr.ctypes.data if self.kind == "np" else self.arr.data_ptr()
+
+
+def _as_points(X):
+    """Points-major (N x D) contiguous float32/float64 array."""
+    if _is_torch(X):
+        t = X.contiguous()
+        if t.dtype not in (_torch().float32, _torch().float64):
+            t = t.to(_torch().float64)
+        dt = C.TK_F64 if t.dtype == _torch().float64 else C.TK_F32
+        return _Buf(t, "torch"), dt
+    a = np.asarray(X)
+    if a.dtype not in (np.float32, np.float64):
+        a = a.astype(np.float64)
+    a = np.ascontiguousarray(a)
+    return _Buf(a, "np"), (C.TK_F64 if a.dtype == np.float64 else C.TK_F32)
+
+
+def _as_index(idx, like):
+    if _is_torch(idx):
+        return _Buf(idx.to(_torch().int32).contiguous(), "torch")
+    return _Buf(np.ascontiguousarray(np.asarray(idx, dtype=np.int32)), "np")
+
+
+def _as_f64(a):
+    if _is_torch(a):
+        return _Buf(a.to(_torch().float64).contiguous(), "torch")
+    return _Buf(np.ascontiguousarray(np.asarray(a, dtype=np.float64)), "np")
+
+
+def _empty(shape, dtype, like: _Buf):
+    if like.kind == "torch" and like.arr.is_cuda:
+        torch = _torch()
+        tdt = {np.int32: torch.int32, np.int64: torch.int64, np.float64: torch.float64}[dtype]
+        return _Buf(torch.empty(shape, dtype=tdt, device=like.arr.device), "torch")
+    return _Buf(np.empty(shape, dtype=dtype), "np")
+
+
+# ---------------------------------------------------------------- context
+
+
+@dataclass
+class LocalOperator:
+    """The operator of one stage run: neighbours, weights and M in CSR."""
+
+    idx: object
+    weights: object
+    row_ptr: object
+    col_idx: object
+    vals: object
+    k: int
+    method: int
+    target_dimension: int
+    connectivity_retries: int
+    rows_uncertified: int
+    stage_ms: dict = field(default_factory=dict)
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        n = len(self.row_ptr) - 1
+        rp, ci, v = (np.asarray(a.cpu()) if _is_torch(a) else np.asarray(a)
+                     for a in (self.row_ptr, self.col_idx, self.vals))
+        return sp.csr_matrix((v, ci, rp), shape=(n, n))
+
+
+class Context:
+    """One GPU context: a CUDA stream plus reusable device scratch memory."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self.lib = C.load()
+        self.ptr = ctypes.c_void_p()
+        st = ctypes.c_void_p(int(stream)) if stream is not None else None
+        rc = self.lib.tk_ctx_create(int(device), st, ctypes.byref(self.ptr))
+        if rc != C.TK_OK:
+            raise DeviceError(f"tk_ctx_create failed: {self.lib.tk_status_string(rc).decode()}")
+        self._log_cb = None
+
+    def close(self):
+        if self.ptr:
+            self.lib.tk_ctx_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        _raise(self.ptr, rc, self.lib)
+
+    def set_logger(self, fn):
+        """fn(level:int, message:str) receives the library's log messages."""
+        if fn is None:
+            self._log_cb = None
+            self._check(self.lib.tk_set_log_callback(self.ptr, C.LOG_FN(), None))
+            return
+        self._log_cb = C.LOG_FN(lambda lvl, msg, user: fn(lvl, msg.decode()))
+        self._check(self.lib.tk_set_log_callback(self.ptr, self._log_cb, None))
+
+    # -- stages ---------------------------------------------------------------
+    def knn_brute(self, X, k, screen="tensor", return_distances=False, return_stats=False):
+        """Brute-force k nearest neighbours (neighbors/neighbors.hpp:119-149).
+        Rows ordered by (FP64 squared distance, index)."""
+        xb, dt = _as_points(X)
+        N, D = xb.arr.shape
+        idx = _empty((N, k), np.int32, xb)
+        d2 = _empty((N, k), np.float64, xb) if return_distances else None
+        st = C.tk_knn_stats()
+        self._check(self.lib.tk_knn_brute(self.ptr, xb.ptr, dt, N, D, D, int(k), SCREENS[screen], idx.ptr,
+                                          d2.ptr if d2 else None, ctypes.byref(st)))
+        out = [idx.arr]
+        if return_distances:
+            out.append(d2.arr)
+        if return_stats:
+            out.append({"rows_uncertified": st.rows_uncertified, "candidates": st.candidates})
+        return out[0] if len(out) == 1 else tuple(out)
+
+    def check_connected(self, idx):
+        """Reachability of all vertices from vertex 0 (neighbors/connected.hpp:19-62)."""
+        ib = _as_index(idx, None)
+        N, k = ib.arr.shape
+        c = ctypes.c_int()
+        self._check(self.lib.tk_check_connected(self.ptr, N, k, ib.ptr, ctypes.byref(c)))
+        return bool(c.value)
+
+    def lle_weights(self, X, idx, klle_shift=1e-3):
+        """LLE reconstruction weights (routines/locally_linear.hpp:107-131)."""
+        xb, dt = _as_points(X)
+        ib = _as_index(idx, xb)
+        N, D = xb.arr.shape
+        k = ib.arr.shape[1]
+        W = _empty((N, k), np.float64, xb)
+        self._check(self.lib.tk_lle_weights(self.ptr, xb.ptr, dt, N, D, D, ib.ptr, k, float(klle_shift), W.ptr))
+        return W.arr
+
+    def ltsa_basis(self, X, idx, target_dimension=2):
+        """LTSA tangent bases V (N x k x td) (routines/locally_linear.hpp:45-63)."""
+        xb, dt = _as_points(X)
+        ib = _as_index(idx, xb)
+        N, D = xb.arr.shape
+        k = ib.arr.shape[1]
+        V = _empty((N, k, target_dimension), np.float64, xb)
+        self._check(self.lib.tk_ltsa_basis(self.ptr, xb.ptr, dt, N, D, D, ib.ptr, k, int(target_dimension), V.ptr))
+        return V.arr
+
+    def assemble(self, method, idx, weights, shift):
+        """M in CSR (routines/locally_linear.hpp:133-146 / :65-77 + utils/sparse.hpp:16-21)."""
+        m = METHODS[method] if isinstance(method, str) else int(method)
+        ib = _as_index(idx, None)
+        wb = _as_f64(weights)
+        N, k = ib.arr.shape
+        td = wb.arr.shape[2] if wb.arr.ndim == 3 else 0
+        rp = _empty((N + 1,), np.int64, wb)
+        nnz = ctypes.c_int64(0)
+        self._check(self.lib.tk_assemble(self.ptr, m, N, k, td, ib.ptr, wb.ptr, float(shift), rp.ptr, None, None,
+                                         ctypes.byref(nnz)))
+        col = _empty((nnz.value,), np.int32, wb)
+        val = _empty((nnz.value,), np.float64, wb)
+        self._check(self.lib.tk_assemble(self.ptr, m, N, k, td, ib.ptr, wb.ptr, float(shift), rp.ptr, col.ptr,
+                                         val.ptr, ctypes.byref(nnz)))
+        return rp.arr, col.arr, val.arr
+
+    def local_operator(self, X, method="lle", num_neighbors=5, target_dimension=2, klle_shift=1e-3,
+                       nullspace_shift=1e-9, check_connectivity=True, screen="tensor", cancel_function=None,
+                       copy_out=True):
+        """The whole stage of KLLE/KLTSA embed() up to the eigensolver."""
+        if method not in METHODS:
+            raise UnsupportedMethodError(f"method {method!r} is not provided by this library")
+        xb, dt = _as_points(X)
+        if xb.arr.ndim != 2:
+            raise WrongParameterError("X must be 2-D (points x features)")
+        N, D = xb.arr.shape
+        p = C.tk_params()
+        self.lib.tk_params_default(ctypes.byref(p))
+        p.method = METHODS[method]
+        p.num_neighbors = int(num_neighbors)
+        p.target_dimension = int(target_dimension)
+        p.klle_shift = float(klle_shift)
+        p.nullspace_shift = float(nullspace_shift)
+        p.check_connectivity = 1 if check_connectivity else 0
+        p.screen = SCREENS[screen]
+        if cancel_function is not None:
+            cb = C.CANCEL_FN(lambda: 1 if cancel_function() else 0)
+            p.cancel_function = cb
+        info = C.tk_operator_info()
+        self._check(self.lib.tk_local_operator(self.ptr, ctypes.byref(p), xb.ptr, dt, N, D, D, ctypes.byref(info)))
+        stage = dict(knn=info.stage_ms[0], connectivity=info.stage_ms[1], weights=info.stage_ms[2],
+                     assembly=info.stage_ms[3], total=info.stage_ms[4])
+        if not copy_out:
+            return info
+        k, td = info.k, info.target_dimension
+        wshape = (N, k) if info.method == C.TK_METHOD_KLLE else (N, k, td)
+        idx = _empty((N, k), np.int32, xb)
+        w = _empty(wshape, np.float64, xb)
+        rp = _empty((N + 1,), np.int64, xb)
+        col = _empty((info.nnz,), np.int32, xb)
+        val = _empty((info.nnz,), np.float64, xb)
+        self._check(self.lib.tk_operator_copy(self.ptr, idx.ptr, w.ptr, rp.ptr, col.ptr, val.ptr))
+        return LocalOperator(idx.arr, w.arr, rp.arr, col.arr, val.arr, k, info.method, td,
+                             info.connectivity_retries, info.rows_uncertified, stage)
+
+    def synchronize(self):
+        self._check(self.lib.tk_ctx_synchronize(self.ptr))
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+# ---------------------------------------------------------------- eigensolver
+
+
+def smallest_eigenvectors(op: LocalOperator, target_dimension: int, skip: int = 1, eigen_method: str = "dense"):
+    """Consumes the CSR of M unchanged: the eigenvectors of the target_dimension
+    smallest eigenvalues after skipping `skip` (routines/eigendecomposition.hpp:56-87,
+    dense path: symmetrise, self-adjoint solve, columns skip..skip+td). Runs on
+    the GPU in FP64."""
+    torch = _torch()
+    if eigen_method != "dense":
+        raise UnsupportedMethodError(f"eigen_method {eigen_method!r} is not provided (use 'dense')")
+    n = len(op.row_ptr) - 1
+    dev = "cuda"
+    rp = torch.as_tensor(np.asarray(op.row_ptr.cpu() if _is_torch(op.row_ptr) else op.row_ptr)).to(dev)
+    ci = torch.as_tensor(np.asarray(op.col_idx.cpu() if _is_torch(op.col_idx) else op.col_idx)).to(dev)
+    v = torch.as_tensor(np.asarray(op.vals.cpu() if _is_torch(op.vals) else op.vals)).to(dev)
+    M = torch.sparse_csr_tensor(rp, ci.to(torch.int64), v, size=(n, n)).to_dense()
+    M = (M + M.T) / 2
+    try:
+        w, V = torch.linalg.eigh(M)
+    except Exception as e:  # pragma: no cover
+        raise EigendecompositionError(str(e))
+    return V[:, skip:skip + target_dimension], w[skip:skip + target_dimension]
+
+
+# ---------------------------------------------------------------- reference-shaped entry points
+
+
+_KNOWN_KW = ("method", "neighbors_method", "eigen_method", "num_neighbors", "target_dimension",
+             "nullspace_shift", "klle_shift", "check_connectivity", "screen", "cancel_function")
+
+
+def embed(data, method="lle", neighbors_method=None, eigen_method=None, num_neighbors=None, target_dimension=None,
+          nullspace_shift=None, klle_shift=None, check_connectivity=None, screen="tensor", context=None,
+          **unsupported):
+    """Python signature of the reference module's ``embed`` for the methods this
+    library provides (KLLE, KLTSA with brute-force neighbours). ``data`` is
+    features x samples; returns samples x target_dimension (numpy)."""
+    for key, val in unsupported.items():
+        if val is not None:
+            raise UnsupportedMethodError(f"parameter {key!r} is not used by the local-neighborhood methods")
+    if method not in METHODS:
+        raise UnsupportedMethodError(f"method {method!r} is not provided by this library")
+    if neighbors_method not in (None, "brute"):
+        raise UnsupportedMethodError("only neighbors_method='brute' is provided")
+    X = data.T if not _is_torch(data) else data.t()
+    td = 2 if target_dimension is None else int(target_dimension)
+    ctx = context or default_context()
+    op = ctx.local_operator(X, method=method, num_neighbors=5 if num_neighbors is None else num_neighbors,
+                            target_dimension=td, klle_shift=1e-3 if klle_shift is None else klle_shift,
+                            nullspace_shift=1e-9 if nullspace_shift is None else nullspace_shift,
+                            check_connectivity=True if check_connectivity is None else bool(check_connectivity),
+                            screen=screen)
+    E, _ = smallest_eigenvectors(op, td, 1, eigen_method or "dense")
+    return E.cpu().numpy()
+
+
+@dataclass
+class TapkeeOutput:
+    embedding: np.ndarray
+    operator: LocalOperator | None = None
+
+
+class ParametersInitializedState:
+    """``tapkee::with(parameters)`` (chain_interface.hpp:497-500)."""
+
+    def __init__(self, params: dict):
+        self.params = dict(params)
+
+    def embed_using(self, matrix, context=None) -> TapkeeOutput:
+        """``embedUsing(const DenseMatrix&)`` (chain_interface.hpp:471-480): matrix is
+        features x samples (column = point)."""
+        p = self.params
+        if "method" not in p:
+            raise MissedParameterError("missed parameter: dimension reduction method")
+        ctx = context or default_context()
+        X = matrix.T if not _is_torch(matrix) else matrix.t()
+        td = p.get("target_dimension", 2)
+        op = ctx.local_operator(X, method=p["method"], num_neighbors=p.get("num_neighbors", 5),
+                                target_dimension=td, klle_shift=p.get("klle_shift", 1e-3),
+                                nullspace_shift=p.get("nullspace_shift", 1e-9),
+                                check_connectivity=p.get("check_connectivity", True),
+                                screen=p.get("screen", "tensor"), cancel_function=p.get("cancel_function"))
+        E, _ = smallest_eigenvectors(op, td, 1, p.get("eigen_method", "dense"))
+        return TapkeeOutput(E.cpu().numpy(), op)
+
+    embedUsing = embed_using
+
+
+def with_(*param_sets, **kwargs) -> ParametersInitializedState:
+    """Keyword-set form of ``tapkee::with((kw=value, ...))``. A keyword given
+    twice (across dicts and kwargs) raises MultipleParameterError, like
+    ParametersSet::check (stichwort/parameter.hpp:232-310)."""
+    merged = {}
+    for d in list(param_sets) + [kwargs]:
+        for key, val in d.items():
+            if key in merged:
+                raise MultipleParameterError(f"parameter {key!r} is set more than once")
+            if key not in _KNOWN_KW:
+                raise UnsupportedMethodError(f"parameter {key!r} is not used by the local-neighborhood methods")
+            merged[key] = val
+    if "neighbors_method" in merged and merged["neighbors_method"] != "brute":
+        raise UnsupportedMethodError("only neighbors_method='brute' is provided")
+    return ParametersInitializedState(merged)

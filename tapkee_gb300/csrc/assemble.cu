@@ -1,0 +1,466 @@
+// assemble.cu -- CSR assembly of the alignment matrix M (pull formulation).
+//
+// The reference emits per-point triplets (routines/locally_linear.hpp:133-146
+// for LLE, :65-77 for LTSA) and sums duplicates with setFromTriplets
+// (utils/sparse.hpp:16-21). Here every output row j gathers its own
+// contributions instead, so no atomics touch values and the result is
+// bit-reproducible:
+//   * reverse adjacency rev(j) = {(r, a) : idx[r][a] == j}, sorted by r;
+//   * row j visits its sources in ascending point order -- point j itself and
+//     every r in rev(j) -- exactly the order in which a serial run of the
+//     reference pushes the triplets that land in row j, and adds each
+//     contribution into a per-warp shared-memory hash table keyed by column.
+//     Contributions of one source to one row have distinct columns, so one
+//     source is one lane-parallel batch and every (row, col) sum is formed in
+//     the reference's serial triplet order;
+//   * the table is compacted, sorted by column (bitonic) and written.
+// Two passes: count (keys only) -> exclusive scan -> fill.
+//
+//   LLE  row j: source j  -> (j, 1+shift), (n_a, -w_ja)
+//               source r  -> (r, -w_ra), (n_b, w_ra w_rb)       [j = n_a of r]
+//   LTSA row j: source j  -> (j, shift)
+//               source r  -> (j, +1) then (n_b, -P_r[a][b])      [j = n_a of r]
+//               P_r = (1/k) 1 1^T + V_r V_r^T
+#include <cstdint>
+
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+constexpr int HC = 1024;        // hash slots per warp (normal rows)
+constexpr int HC_BIG = 8192;    // hash slots for rows with a large in-degree
+constexpr int ROW_WARPS = 4;
+
+__global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, int* cnt, unsigned* err)
+{
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int j = idx[e];
+        if (j < 0 || j >= N)
+        {
+            atomicOr(err, DEV_ERR_BOUNDS);
+            continue;
+        }
+        atomicAdd(&cnt[j], 1);
+    }
+}
+
+// exclusive scan of n int counters into int64 offsets (out has n+1 entries), one block
+__global__ void k_scan_i64(const int* in, int64_t n, int64_t* out)
+{
+    __shared__ int64_t part[1024];
+    const int t = threadIdx.x;
+    const int64_t per = (n + 1023) / 1024;
+    const int64_t b0 = t * per, b1 = min(n, b0 + per);
+    int64_t s = 0;
+    for (int64_t b = b0; b < b1; ++b)
+        s += in[b];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        const int64_t v = (t >= o) ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int64_t run = part[t] - s;
+    for (int64_t b = b0; b < b1; ++b)
+    {
+        out[b] = run;
+        run += in[b];
+    }
+    if (t == 1023)
+        out[n] = part[1023];
+}
+
+__global__ void k_fill_rev(const int32_t* __restrict__ idx, int64_t nk, const int64_t* rptr, int* fillc,
+                           int32_t* rev)
+{
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int j = idx[e];
+        const int pos = atomicAdd(&fillc[j], 1);
+        rev[rptr[j] + pos] = (int32_t)e;
+    }
+}
+
+// insertion sort of every reverse list (edge id = r*k + a, ascending = by r)
+__global__ void k_sort_rev(int64_t N, const int64_t* rptr, int32_t* rev)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t b = rptr[j], e = rptr[j + 1];
+        for (int64_t p = b + 1; p < e; ++p)
+        {
+            const int32_t v = rev[p];
+            int64_t q = p - 1;
+            while (q >= b && rev[q] > v)
+            {
+                rev[q + 1] = rev[q];
+                --q;
+            }
+            rev[q + 1] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned hash_col(int c) { return (unsigned)c * 2654435761u; }
+
+template <int CAP>
+struct RowTable
+{
+    int keys[CAP];
+    double vals[CAP];
+    unsigned long long sortk[CAP];
+};
+
+// insert-or-add; returns false if the table is full
+template <int CAP, bool VALUES>
+__device__ __forceinline__ bool table_add(RowTable<CAP>& T, int col, double v)
+{
+    unsigned h = hash_col(col) & (CAP - 1);
+    for (int probe = 0; probe < CAP; ++probe)
+    {
+        int key = T.keys[h];
+        if (key == -1)
+        {
+            key = atomicCAS(&T.keys[h], -1, col);
+            if (key == -1)
+                key = col;  // claimed
+        }
+        if (key == col)
+        {
+            if (VALUES)
+                T.vals[h] += v;  // distinct columns within a batch: no other lane owns this slot
+            return true;
+        }
+        h = (h + 1) & (CAP - 1);
+    }
+    return false;
+}
+
+// Upper bound of the number of distinct columns in row j.
+__device__ __forceinline__ int64_t row_bound(int method, int k, int64_t deg)
+{
+    return method == TK_METHOD_KLLE ? 1 + k + deg * (k + 1) : 1 + deg * k;
+}
+
+// Processes one row with one warp. Returns false on table overflow.
+template <int CAP, bool VALUES>
+__device__ bool process_row(RowTable<CAP>& T, int lane, int method, int64_t j, int k, int td,
+                            const int32_t* __restrict__ idx, const double* __restrict__ wts, double shift,
+                            const int64_t* __restrict__ rptr, const int32_t* __restrict__ rev)
+{
+    for (int h = lane; h < CAP; h += 32)
+    {
+        T.keys[h] = -1;
+        if (VALUES)
+            T.vals[h] = 0.0;
+    }
+    __syncwarp();
+    bool ok = true;
+    const int64_t b = rptr[j], e = rptr[j + 1];
+    bool self_done = false;
+    for (int64_t p = b; p <= e; ++p)
+    {
+        // next source in ascending point order: j itself is merged into rev(j)
+        int64_t src;
+        int slot = -1;
+        if (p < e)
+        {
+            const int32_t eid = rev[p];
+            src = eid / k;
+            slot = eid - (int32_t)src * k;
+            if (!self_done && j < src)
+            {
+                src = j;
+                slot = -1;
+                --p;  // revisit this edge next iteration
+            }
+        }
+        else
+        {
+            if (self_done)
+                break;
+            src = j;
+        }
+        if (src == j && slot < 0)
+            self_done = true;
+
+        if (method == TK_METHOD_KLLE)
+        {
+            if (slot < 0)
+            {
+                // source j: (j, 1+shift) and (n_a, -w_ja)
+                for (int t0 = 0; t0 < k + 1; t0 += 32)
+                {
+                    const int t = t0 + lane;
+                    if (t < k + 1)
+                    {
+                        const int col = (t == 0) ? (int)j : idx[j * k + t - 1];
+                        const double v = VALUES ? ((t == 0) ? 1.0 + shift : -wts[j * k + t - 1]) : 0.0;
+                        ok &= table_add<CAP, VALUES>(T, col, v);
+                    }
+                    __syncwarp();
+                }
+            }
+            else
+            {
+                // source r=src, j at slot a: (r, -w_ra), (n_b, w_ra w_rb)
+                const double wa = VALUES ? wts[src * k + slot] : 0.0;
+                for (int t0 = 0; t0 < k + 1; t0 += 32)
+                {
+                    const int t = t0 + lane;
+                    if (t < k + 1)
+                    {
+                        const int col = (t == 0) ? (int)src : idx[src * k + t - 1];
+                        const double v = VALUES ? ((t == 0) ? -wa : wa * wts[src * k + t - 1]) : 0.0;
+                        ok &= table_add<CAP, VALUES>(T, col, v);
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        else
+        {
+            if (slot < 0)
+            {
+                if (lane == 0)
+                    ok &= table_add<CAP, VALUES>(T, (int)j, shift);
+                __syncwarp();
+            }
+            else
+            {
+                if (lane == 0)
+                    ok &= table_add<CAP, VALUES>(T, (int)j, 1.0);
+                __syncwarp();
+                const double* Va = wts + (src * k + slot) * (int64_t)td;
+                for (int t0 = 0; t0 < k; t0 += 32)
+                {
+                    const int t = t0 + lane;
+                    if (t < k)
+                    {
+                        double v = 0.0;
+                        if (VALUES)
+                        {
+                            const double* Vb = wts + (src * k + t) * (int64_t)td;
+                            double pab = 1.0 / k;
+                            for (int q = 0; q < td; ++q)
+                                pab += Va[q] * Vb[q];
+                            v = -pab;
+                        }
+                        ok &= table_add<CAP, VALUES>(T, idx[src * k + t], v);
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+    }
+    return __all_sync(0xffffffffu, ok);
+}
+
+// number of occupied slots
+template <int CAP>
+__device__ int table_count(RowTable<CAP>& T, int lane)
+{
+    int c = 0;
+    for (int h = lane; h < CAP; h += 32)
+        c += (T.keys[h] != -1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    return c;
+}
+
+// compact, sort by column and write the row
+template <int CAP>
+__device__ void table_emit(RowTable<CAP>& T, int lane, int64_t base, int32_t* col_idx, double* vals)
+{
+    int n = 0;
+    for (int h0 = 0; h0 < CAP; h0 += 32)
+    {
+        const int h = h0 + lane;
+        const bool occ = T.keys[h] != -1;
+        const unsigned m = __ballot_sync(0xffffffffu, occ);
+        if (occ)
+        {
+            const int pos = n + __popc(m & ((1u << lane) - 1u));
+            T.sortk[pos] = ((unsigned long long)(unsigned)T.keys[h] << 20) | (unsigned)h;
+        }
+        n += __popc(m);
+    }
+    int P = 1;
+    while (P < n)
+        P <<= 1;
+    for (int t = n + lane; t < P; t += 32)
+        T.sortk[t] = ~0ull;
+    __syncwarp();
+    for (int size = 2; size <= P; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1)
+        {
+            for (int t = lane; t < P / 2; t += 32)
+            {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool asc = ((lo & size) == 0);
+                const unsigned long long a = T.sortk[lo], bb = T.sortk[hi];
+                if ((a > bb) == asc)
+                {
+                    T.sortk[lo] = bb;
+                    T.sortk[hi] = a;
+                }
+            }
+            __syncwarp();
+        }
+    for (int t = lane; t < n; t += 32)
+    {
+        const unsigned long long key = T.sortk[t];
+        col_idx[base + t] = (int32_t)(key >> 20);
+        vals[base + t] = T.vals[key & 0xfffffull];
+    }
+    __syncwarp();
+}
+
+template <bool VALUES>
+__global__ void __launch_bounds__(ROW_WARPS * 32)
+    k_rows(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx, const double* __restrict__ wts,
+           double shift, const int64_t* __restrict__ rptr, const int32_t* __restrict__ rev, int* row_nnz,
+           const int64_t* __restrict__ row_ptr, int32_t* col_idx, double* vals, int32_t* big_rows,
+           unsigned* nbig, unsigned* err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    RowTable<HC>& T = reinterpret_cast<RowTable<HC>*>(smem_raw)[wib];
+    const int64_t nw = (int64_t)gridDim.x * ROW_WARPS;
+    for (int64_t j = (int64_t)blockIdx.x * ROW_WARPS + wib; j < N; j += nw)
+    {
+        const int64_t deg = rptr[j + 1] - rptr[j];
+        if (row_bound(method, k, deg) > (HC * 3) / 4)
+        {
+            if (!VALUES && lane == 0)
+                big_rows[atomicAdd(nbig, 1u)] = (int32_t)j;
+            continue;
+        }
+        const bool ok = process_row<HC, VALUES>(T, lane, method, j, k, td, idx, wts, shift, rptr, rev);
+        if (!ok)
+        {
+            if (lane == 0)
+                atomicOr(err, DEV_ERR_OVERFLOW);
+            continue;
+        }
+        if (!VALUES)
+        {
+            const int c = table_count<HC>(T, lane);
+            if (lane == 0)
+                row_nnz[j] = c;
+        }
+        else
+            table_emit<HC>(T, lane, row_ptr[j], col_idx, vals);
+        __syncwarp();
+    }
+}
+
+// rows with a large in-degree: one warp per block, large table
+template <bool VALUES>
+__global__ void __launch_bounds__(32)
+    k_rows_big(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx,
+               const double* __restrict__ wts, double shift, const int64_t* __restrict__ rptr,
+               const int32_t* __restrict__ rev, int* row_nnz, const int64_t* __restrict__ row_ptr,
+               int32_t* col_idx, double* vals, const int32_t* big_rows, const unsigned* nbig, unsigned* err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    RowTable<HC_BIG>& T = *reinterpret_cast<RowTable<HC_BIG>*>(smem_raw);
+    const int lane = threadIdx.x & 31;
+    const unsigned nb = *nbig;
+    for (unsigned r = blockIdx.x; r < nb; r += gridDim.x)
+    {
+        const int64_t j = big_rows[r];
+        const int64_t deg = rptr[j + 1] - rptr[j];
+        if (row_bound(method, k, deg) > (int64_t)HC_BIG * 3 / 4)
+        {
+            // the bound is loose; try anyway and report overflow if it really fills
+        }
+        const bool ok = process_row<HC_BIG, VALUES>(T, lane, method, j, k, td, idx, wts, shift, rptr, rev);
+        if (!ok)
+        {
+            if (lane == 0)
+                atomicOr(err, DEV_ERR_OVERFLOW);
+            continue;
+        }
+        if (!VALUES)
+        {
+            const int c = table_count<HC_BIG>(T, lane);
+            if (lane == 0)
+                row_nnz[j] = c;
+        }
+        else
+            table_emit<HC_BIG>(T, lane, row_ptr[j], col_idx, vals);
+        __syncwarp();
+    }
+}
+
+} // namespace
+
+int64_t assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                 double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, bool count_only)
+{
+    cudaStream_t st = ctx->stream;
+    const int64_t nk = N * (int64_t)k;
+    if (nk >= (int64_t)1 << 31)
+        throw Error(TK_ERR_UNSUPPORTED, "assembly supports N*k < 2^31");
+    int* cnt = (int*)ctx->scratch.get("asm.cnt", sizeof(int) * (size_t)N * 2);
+    int* fillc = cnt + N;
+    int64_t* rptr = (int64_t*)ctx->scratch.get("asm.rptr", sizeof(int64_t) * (size_t)(N + 1));
+    int32_t* rev = (int32_t*)ctx->scratch.get("asm.rev", sizeof(int32_t) * (size_t)nk);
+    int* row_nnz = (int*)ctx->scratch.get("asm.rownnz", sizeof(int) * (size_t)N);
+    int32_t* big = (int32_t*)ctx->scratch.get("asm.big", sizeof(int32_t) * (size_t)N);
+    unsigned* nbig = (unsigned*)ctx->scratch.get("asm.nbig", 16);
+    int64_t* rp = row_ptr ? row_ptr : (int64_t*)ctx->scratch.get("asm.rowptr", sizeof(int64_t) * (size_t)(N + 1));
+    const int g = 4 * ctx->num_sms;
+
+    TK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)N * 2, st));
+    TK_CUDA(cudaMemsetAsync(nbig, 0, 16, st));
+    k_indeg<<<g, 256, 0, st>>>(idx, nk, N, cnt, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    k_scan_i64<<<1, 1024, 0, st>>>(cnt, N, rptr);
+    TK_CHECK_LAUNCH();
+    k_fill_rev<<<g, 256, 0, st>>>(idx, nk, rptr, fillc, rev);
+    TK_CHECK_LAUNCH();
+    k_sort_rev<<<g, 256, 0, st>>>(N, rptr, rev);
+    TK_CHECK_LAUNCH();
+
+    const size_t smem = sizeof(RowTable<HC>) * ROW_WARPS;
+    const size_t smem_big = sizeof(RowTable<HC_BIG>);
+    TK_CUDA(cudaFuncSetAttribute(k_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TK_CUDA(cudaFuncSetAttribute(k_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TK_CUDA(cudaFuncSetAttribute(k_rows_big<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
+    TK_CUDA(cudaFuncSetAttribute(k_rows_big<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
+    const int64_t want = (N + ROW_WARPS - 1) / ROW_WARPS;
+    const int grid = (int)std::min<int64_t>(want, (int64_t)ctx->num_sms * 8);
+
+    k_rows<false><<<grid, ROW_WARPS * 32, smem, st>>>(method, N, k, td, idx, weights, shift, rptr, rev, row_nnz,
+                                                       nullptr, nullptr, nullptr, big, nbig, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    k_rows_big<false><<<ctx->num_sms, 32, smem_big, st>>>(method, N, k, td, idx, weights, shift, rptr, rev,
+                                                           row_nnz, nullptr, nullptr, nullptr, big, nbig,
+                                                           ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    k_scan_i64<<<1, 1024, 0, st>>>(row_nnz, N, rp);
+    TK_CHECK_LAUNCH();
+    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, rp + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    TK_CUDA(cudaStreamSynchronize(st));
+    const int64_t nnz = ctx->host_i64[0];
+    if (count_only)
+        return nnz;
+    k_rows<true><<<grid, ROW_WARPS * 32, smem, st>>>(method, N, k, td, idx, weights, shift, rptr, rev, row_nnz, rp,
+                                                      col_idx, vals, big, nbig, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    k_rows_big<true><<<ctx->num_sms, 32, smem_big, st>>>(method, N, k, td, idx, weights, shift, rptr, rev, row_nnz,
+                                                          rp, col_idx, vals, big, nbig, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    return nnz;
+}
+
+} // namespace tk

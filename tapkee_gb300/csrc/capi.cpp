@@ -1,0 +1,670 @@
+// capi.cpp -- the extern "C" boundary: contexts, argument checks, host/device
+// buffer handling and the stage pipeline of tk_local_operator.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "tk_internal.h"
+
+#define TK_VERSION_STRING "0.1.0"
+
+namespace tk {
+
+void* Scratch::get(const std::string& name, size_t bytes)
+{
+    Buf& b = bufs[name];
+    if (b.bytes < bytes)
+    {
+        if (b.ptr)
+        {
+            // the old buffer may still be read by queued work
+            TK_CUDA(cudaDeviceSynchronize());
+            TK_CUDA(cudaFree(b.ptr));
+            b.ptr = nullptr;
+            b.bytes = 0;
+        }
+        size_t nb = std::max(bytes, (size_t)256);
+        nb = (nb + 255) & ~(size_t)255;
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, nb);
+        if (e != cudaSuccess)
+        {
+            cudaGetLastError();
+            throw Error(e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA,
+                        "device allocation of " + std::to_string(nb) + " bytes for '" + name + "' failed: " +
+                            cudaGetErrorString(e));
+        }
+        b.ptr = p;
+        b.bytes = nb;
+    }
+    return b.ptr;
+}
+
+void Scratch::release_all()
+{
+    for (auto& kv : bufs)
+        if (kv.second.ptr)
+            cudaFree(kv.second.ptr);
+    bufs.clear();
+}
+
+void log(tk_ctx* ctx, int level, const std::string& msg)
+{
+    if (ctx && ctx->log_fn)
+        ctx->log_fn(level, msg.c_str(), ctx->log_user);
+    else if (level == TK_LOG_WARNING || level == TK_LOG_ERROR)
+        std::fprintf(stderr, "[tapkee_gb300] %s\n", msg.c_str());
+}
+
+namespace {
+
+bool is_device_ptr(const void* p)
+{
+    if (!p)
+        return false;
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+size_t dtype_size(int dtype) { return dtype == TK_F64 ? 8 : 4; }
+
+void check_dtype(int dtype)
+{
+    if (dtype != TK_F32 && dtype != TK_F64)
+        throw Error(TK_ERR_INVALID_ARG, "dtype must be TK_F32 or TK_F64");
+}
+
+// Makes X device-resident (packed if it lives on the host); returns the device
+// pointer and its row stride.
+const void* device_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, int64_t* ldx_dev,
+                          const char* name)
+{
+    if (is_device_ptr(X))
+    {
+        *ldx_dev = ldx;
+        return X;
+    }
+    const size_t es = dtype_size(dtype);
+    void* d = ctx->scratch.get(name, es * (size_t)N * D);
+    TK_CUDA(cudaMemcpy2DAsync(d, es * D, X, es * ldx, es * D, (size_t)N, cudaMemcpyHostToDevice, ctx->stream));
+    *ldx_dev = D;
+    return d;
+}
+
+template <typename T>
+const T* device_array(tk_ctx* ctx, const T* p, size_t count, const char* name)
+{
+    if (is_device_ptr(p))
+        return p;
+    T* d = (T*)ctx->scratch.get(name, sizeof(T) * count);
+    TK_CUDA(cudaMemcpyAsync(d, p, sizeof(T) * count, cudaMemcpyHostToDevice, ctx->stream));
+    return d;
+}
+
+template <typename T>
+T* device_out(tk_ctx* ctx, T* p, size_t count, const char* name, bool* is_host)
+{
+    if (!p)
+    {
+        *is_host = false;
+        return nullptr;
+    }
+    if (is_device_ptr(p))
+    {
+        *is_host = false;
+        return p;
+    }
+    *is_host = true;
+    return (T*)ctx->scratch.get(name, sizeof(T) * count);
+}
+
+template <typename T>
+void copy_back(tk_ctx* ctx, T* host, const T* dev, size_t count)
+{
+    TK_CUDA(cudaMemcpyAsync(host, dev, sizeof(T) * count, cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+void check_device_errors(tk_ctx* ctx)
+{
+    TK_CUDA(cudaMemcpyAsync(ctx->host_err, ctx->dev_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    const unsigned e = *ctx->host_err;
+    if (e)
+    {
+        TK_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(unsigned), ctx->stream));
+        std::string m = "device-side check failed:";
+        if (e & DEV_ERR_TIMEOUT)
+            m += " bounded wait expired;";
+        if (e & DEV_ERR_OVERFLOW)
+            m += " bounded buffer overflow;";
+        if (e & DEV_ERR_BOUNDS)
+            m += " index out of range;";
+        if (e & DEV_ERR_NONFINITE)
+            m += " non-finite value;";
+        throw Error((e & DEV_ERR_TIMEOUT) ? TK_ERR_TIMEOUT : ((e & DEV_ERR_BOUNDS) ? TK_ERR_INVALID_ARG : TK_ERR_INTERNAL),
+                    m);
+    }
+}
+
+int candidates_for(int k)
+{
+    if (k + 8 <= 32)
+        return 32;
+    if (k + 8 <= 64)
+        return 64;
+    return -1;
+}
+
+// Brute kNN into device buffers; returns uncertified rows.
+int64_t knn_device(tk_ctx* ctx, const void* Xd, int dtype, int64_t N, int D, int64_t ldx, int k, int screen,
+                   int32_t* idx_d, double* d2_d)
+{
+    const int kc = candidates_for(k);
+    if (kc < 0)
+        throw Error(TK_ERR_UNSUPPORTED, "brute kNN supports up to 56 neighbours per point (k = " +
+                                            std::to_string(k) + ")");
+    const bool tensor = (screen == TK_SCREEN_TENSOR);
+    Prepared P;
+    prepare_points(ctx, Xd, dtype, N, D, ldx, tensor, P);
+    int32_t* cand_idx = (int32_t*)ctx->scratch.get("knn.cand_idx", sizeof(int32_t) * (size_t)P.Npad * kc);
+    float* cand_val = (float*)ctx->scratch.get("knn.cand_val", sizeof(float) * (size_t)P.Npad * kc);
+    if (tensor)
+        screen_tensor(ctx, P, kc, cand_idx, cand_val);
+    else
+        screen_fp32(ctx, P, kc, cand_idx, cand_val);
+    float c1, c2;
+    screen_error_model(screen, P.Dp, &c1, &c2);
+    const int64_t nf = rerank(ctx, P, Xd, dtype, ldx, k, kc, cand_idx, cand_val, c1, c2, idx_d, d2_d);
+    check_device_errors(ctx);
+    return nf;
+}
+
+void validate_points(const void* X, int dtype, int64_t N, int D, int64_t ldx)
+{
+    check_dtype(dtype);
+    if (N <= 0)
+        throw Error(TK_ERR_NO_DATA, "No data to embed");
+    if (!X)
+        throw Error(TK_ERR_INVALID_ARG, "X is NULL");
+    if (D <= 0 || ldx < D)
+        throw Error(TK_ERR_INVALID_ARG, "need D >= 1 and ldx >= D");
+    if (N >= ((int64_t)1 << 31) - 256)
+        throw Error(TK_ERR_INVALID_ARG, "N must be below 2^31 (int32 indices)");
+}
+
+template <typename F>
+int guarded(tk_ctx* ctx, F&& f)
+{
+    if (!ctx)
+        return TK_ERR_INVALID_ARG;
+    try
+    {
+        TK_CUDA(cudaSetDevice(ctx->device));
+        f();
+        ctx->last_error.clear();
+        return TK_OK;
+    }
+    catch (const Error& e)
+    {
+        ctx->last_error = e.what();
+        log(ctx, TK_LOG_ERROR, e.what());
+        return e.status;
+    }
+    catch (const std::bad_alloc&)
+    {
+        ctx->last_error = "Not enough memory";
+        return TK_ERR_OOM;
+    }
+    catch (const std::exception& e)
+    {
+        ctx->last_error = e.what();
+        return TK_ERR_INTERNAL;
+    }
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+} // namespace
+} // namespace tk
+
+using namespace tk;
+
+extern "C" {
+
+const char* tk_version(void) { return TK_VERSION_STRING; }
+
+void tk_params_default(tk_params* p)
+{
+    if (!p)
+        return;
+    p->method = TK_METHOD_KLLE;
+    p->num_neighbors = 5;
+    p->target_dimension = 2;
+    p->klle_shift = 1e-3;
+    p->nullspace_shift = 1e-9;
+    p->check_connectivity = 1;
+    p->screen = TK_SCREEN_TENSOR;
+    p->cancel_function = nullptr;
+}
+
+const char* tk_status_string(int s)
+{
+    switch (s)
+    {
+    case TK_OK: return "ok";
+    case TK_ERR_INVALID_ARG: return "wrong parameter";
+    case TK_ERR_NO_DATA: return "no data";
+    case TK_ERR_OOM: return "not enough memory";
+    case TK_ERR_CUDA: return "CUDA error";
+    case TK_ERR_TIMEOUT: return "device wait timed out";
+    case TK_ERR_CANCELLED: return "cancelled";
+    case TK_ERR_BUFFER_TOO_SMALL: return "buffer too small";
+    case TK_ERR_UNSUPPORTED: return "unsupported";
+    case TK_ERR_NO_DEVICE: return "no sm_103 device";
+    case TK_ERR_INTERNAL: return "internal error";
+    default: return "unknown status";
+    }
+}
+
+int tk_ctx_create(int device, void* stream, tk_ctx** out)
+{
+    if (!out)
+        return TK_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+    {
+        cudaGetLastError();
+        return TK_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+        return TK_ERR_NO_DEVICE;
+    if (!(prop.major == 10 && prop.minor == 3))
+        return TK_ERR_NO_DEVICE;
+    tk_ctx* ctx = new (std::nothrow) tk_ctx();
+    if (!ctx)
+        return TK_ERR_OOM;
+    ctx->device = device;
+    ctx->num_sms = prop.multiProcessorCount;
+    int rc = guarded(ctx, [&] {
+        if (stream)
+        {
+            ctx->stream = (cudaStream_t)stream;
+            ctx->own_stream = false;
+        }
+        else
+        {
+            TK_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+            ctx->own_stream = true;
+        }
+        TK_CUDA(cudaMalloc(&ctx->dev_err, 256));
+        TK_CUDA(cudaMemset(ctx->dev_err, 0, 256));
+        TK_CUDA(cudaMallocHost(&ctx->host_err, 256));
+        TK_CUDA(cudaMallocHost(&ctx->host_i64, 16 * sizeof(int64_t)));
+        for (auto& e : ctx->ev)
+            TK_CUDA(cudaEventCreate(&e));
+    });
+    if (rc != TK_OK)
+    {
+        tk_ctx_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return TK_OK;
+}
+
+int tk_ctx_destroy(tk_ctx* ctx)
+{
+    if (!ctx)
+        return TK_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    ctx->scratch.release_all();
+    if (ctx->dev_err)
+        cudaFree(ctx->dev_err);
+    if (ctx->host_err)
+        cudaFreeHost(ctx->host_err);
+    if (ctx->host_i64)
+        cudaFreeHost(ctx->host_i64);
+    for (auto& e : ctx->ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (ctx->own_stream && ctx->stream)
+        cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return TK_OK;
+}
+
+const char* tk_last_error(const tk_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int tk_set_log_callback(tk_ctx* ctx, tk_log_fn fn, void* user)
+{
+    if (!ctx)
+        return TK_ERR_INVALID_ARG;
+    ctx->log_fn = fn;
+    ctx->log_user = user;
+    return TK_OK;
+}
+
+int tk_ctx_synchronize(tk_ctx* ctx)
+{
+    return guarded(ctx, [&] { TK_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int tk_knn_brute(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, int k, int screen,
+                 int32_t* idx_out, double* d2_out, tk_knn_stats* stats)
+{
+    return guarded(ctx, [&] {
+        validate_points(X, dtype, N, D, ldx);
+        if (k < 1 || k > N - 1)
+            throw Error(TK_ERR_INVALID_ARG, "k must lie in [1, N-1]");
+        if (screen != TK_SCREEN_TENSOR && screen != TK_SCREEN_FP32)
+            throw Error(TK_ERR_INVALID_ARG, "unknown screen engine");
+        if (!idx_out)
+            throw Error(TK_ERR_INVALID_ARG, "idx_out is NULL");
+        int64_t ldd;
+        const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "io.X");
+        bool ih, dh;
+        int32_t* idx_d = device_out(ctx, idx_out, (size_t)N * k, "io.idx", &ih);
+        double* d2_d = device_out(ctx, d2_out, (size_t)N * k, "io.d2", &dh);
+        const int64_t nf = knn_device(ctx, Xd, dtype, N, D, ldd, k, screen, idx_d, d2_d);
+        if (ih)
+            copy_back(ctx, idx_out, idx_d, (size_t)N * k);
+        if (dh)
+            copy_back(ctx, d2_out, d2_d, (size_t)N * k);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (stats)
+        {
+            stats->rows_uncertified = nf;
+            stats->candidates = candidates_for(k);
+            stats->screen = screen;
+        }
+    });
+}
+
+int tk_check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx, int* connected)
+{
+    return guarded(ctx, [&] {
+        if (N <= 0)
+            throw Error(TK_ERR_NO_DATA, "No data");
+        if (k < 1 || !idx || !connected)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        const int32_t* idx_d = device_array(ctx, idx, (size_t)N * k, "io.idx_in");
+        const bool c = check_connected(ctx, N, k, idx_d);
+        check_device_errors(ctx);
+        *connected = c ? 1 : 0;
+    });
+}
+
+int tk_lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+                   double klle_shift, double* W_out)
+{
+    return guarded(ctx, [&] {
+        validate_points(X, dtype, N, D, ldx);
+        if (k < 1 || !idx || !W_out)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        int64_t ldd;
+        const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "io.X");
+        const int32_t* idx_d = device_array(ctx, idx, (size_t)N * k, "io.idx_in");
+        bool wh;
+        double* W_d = device_out(ctx, W_out, (size_t)N * k, "io.W", &wh);
+        lle_weights(ctx, Xd, dtype, N, D, ldd, idx_d, k, klle_shift, W_d);
+        check_device_errors(ctx);
+        if (wh)
+            copy_back(ctx, W_out, W_d, (size_t)N * k);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int tk_ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+                  int td, double* V_out)
+{
+    return guarded(ctx, [&] {
+        validate_points(X, dtype, N, D, ldx);
+        if (k < 1 || !idx || !V_out)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        int64_t ldd;
+        const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "io.X");
+        const int32_t* idx_d = device_array(ctx, idx, (size_t)N * k, "io.idx_in");
+        bool vh;
+        double* V_d = device_out(ctx, V_out, (size_t)N * k * td, "io.V", &vh);
+        ltsa_basis(ctx, Xd, dtype, N, D, ldd, idx_d, k, td, V_d);
+        check_device_errors(ctx);
+        if (vh)
+            copy_back(ctx, V_out, V_d, (size_t)N * k * td);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, int64_t* nnz_io)
+{
+    return guarded(ctx, [&] {
+        if (N <= 0)
+            throw Error(TK_ERR_NO_DATA, "No data");
+        if (method != TK_METHOD_KLLE && method != TK_METHOD_KLTSA)
+            throw Error(TK_ERR_UNSUPPORTED, "unsupported method");
+        if (k < 1 || !idx || !weights || !nnz_io || (method == TK_METHOD_KLTSA && td < 1))
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        const size_t wcount = (size_t)N * k * (method == TK_METHOD_KLTSA ? td : 1);
+        const int32_t* idx_d = device_array(ctx, idx, (size_t)N * k, "io.idx_in");
+        const double* w_d = device_array(ctx, weights, wcount, "io.w_in");
+        bool rh = false;
+        int64_t* rp_d = row_ptr ? device_out(ctx, row_ptr, (size_t)N + 1, "io.rowptr", &rh)
+                                : (int64_t*)ctx->scratch.get("io.rowptr", sizeof(int64_t) * ((size_t)N + 1));
+        const int64_t cap = *nnz_io;
+        const int64_t nnz = assemble(ctx, method, N, k, td, idx_d, w_d, shift, rp_d, nullptr, nullptr, true);
+        check_device_errors(ctx);
+        if (rh)
+            copy_back(ctx, row_ptr, rp_d, (size_t)N + 1);
+        *nnz_io = nnz;
+        if (!col_idx || !vals)
+        {
+            TK_CUDA(cudaStreamSynchronize(ctx->stream));
+            return;
+        }
+        if (cap < nnz)
+            throw Error(TK_ERR_BUFFER_TOO_SMALL, "CSR capacity " + std::to_string(cap) + " < nnz " +
+                                                     std::to_string(nnz));
+        bool ch, vh;
+        int32_t* c_d = device_out(ctx, col_idx, (size_t)nnz, "io.col", &ch);
+        double* v_d = device_out(ctx, vals, (size_t)nnz, "io.vals", &vh);
+        assemble(ctx, method, N, k, td, idx_d, w_d, shift, rp_d, c_d, v_d, false);
+        check_device_errors(ctx);
+        if (ch)
+            copy_back(ctx, col_idx, c_d, (size_t)nnz);
+        if (vh)
+            copy_back(ctx, vals, v_d, (size_t)nnz);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int dtype, int64_t N, int D,
+                      int64_t ldx, tk_operator_info* info)
+{
+    return guarded(ctx, [&] {
+        ctx->op_valid = false;
+        if (!params)
+            throw Error(TK_ERR_INVALID_ARG, "params is NULL");
+        const tk_params& p = *params;
+        if (p.method != TK_METHOD_KLLE && p.method != TK_METHOD_KLTSA)
+            throw Error(TK_ERR_UNSUPPORTED, "unsupported method");
+        check_dtype(dtype);
+        // ImplementationBase (methods/base.hpp:38-44): no data, target dimension in [1, N)
+        if (N <= 0)
+            throw Error(TK_ERR_NO_DATA, "No data to embed");
+        validate_points(X, dtype, N, D, ldx);
+        if (!(p.target_dimension >= 1 && p.target_dimension < N))
+            throw Error(TK_ERR_INVALID_ARG, "[1, " + std::to_string(N) +
+                                                ") range check failed for target dimension, its value is " +
+                                                std::to_string(p.target_dimension));
+        // DynamicImplementation::embedUsing (methods.hpp:30-31): one cancel poll
+        if (p.cancel_function && p.cancel_function())
+            throw Error(TK_ERR_CANCELLED, "cancelled");
+        // find_neighbors_with (methods/base.hpp:85): num_neighbors in [3, N)
+        if (!(p.num_neighbors >= 3 && p.num_neighbors < N))
+            throw Error(TK_ERR_INVALID_ARG, "[3, " + std::to_string(N) +
+                                                ") range check failed for number of neighbors, its value is " +
+                                                std::to_string(p.num_neighbors));
+        if (p.screen != TK_SCREEN_TENSOR && p.screen != TK_SCREEN_FP32)
+            throw Error(TK_ERR_INVALID_ARG, "unknown screen engine");
+        const int td = p.target_dimension;
+
+        cudaStream_t st = ctx->stream;
+        TK_CUDA(cudaEventRecord(ctx->ev[0], st));
+        int64_t ldd;
+        const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "op.X");
+
+        // find_neighbors (neighbors/neighbors.hpp:173-213): clamp, brute, connectivity retry
+        int k = p.num_neighbors;
+        int retries = 0;
+        int64_t uncert = 0;
+        int32_t* idx_d = nullptr;
+        float ms_knn = 0.f, ms_conn = 0.f;
+        for (;;)
+        {
+            if (k > N - 1)
+            {
+                log(ctx, TK_LOG_WARNING,
+                    "Number of neighbors is greater than number of objects to embed. Using greatest possible "
+                    "number of neighbors.");
+                k = (int)(N - 1);
+            }
+            idx_d = (int32_t*)ctx->scratch.get("op.idx", sizeof(int32_t) * (size_t)N * k);
+            TK_CUDA(cudaEventRecord(ctx->ev[1], st));
+            uncert = knn_device(ctx, Xd, dtype, N, D, ldd, k, p.screen, idx_d, nullptr);
+            TK_CUDA(cudaEventRecord(ctx->ev[2], st));
+            bool connected = true;
+            if (p.check_connectivity)
+            {
+                connected = check_connected(ctx, N, k, idx_d);
+                check_device_errors(ctx);
+            }
+            TK_CUDA(cudaEventRecord(ctx->ev[3], st));
+            TK_CUDA(cudaEventSynchronize(ctx->ev[3]));
+            ms_knn += elapsed(ctx->ev[1], ctx->ev[2]);
+            ms_conn += elapsed(ctx->ev[2], ctx->ev[3]);
+            if (connected)
+            {
+                log(ctx, TK_LOG_INFO, "The neighborhood graph with " + std::to_string(k) + " neighbors is connected.");
+                break;
+            }
+            log(ctx, TK_LOG_WARNING, "The neighborhood graph with " + std::to_string(k) +
+                                         " neighbors is not connected. Recomputing with a larger number of "
+                                         "neighbors " + std::to_string(2 * k) + ".");
+            k *= 2;
+            ++retries;
+        }
+
+        // weights
+        TK_CUDA(cudaEventRecord(ctx->ev[4], st));
+        const size_t wcount = (size_t)N * k * (p.method == TK_METHOD_KLTSA ? td : 1);
+        double* w_d = (double*)ctx->scratch.get("op.w", sizeof(double) * wcount);
+        if (p.method == TK_METHOD_KLLE)
+            lle_weights(ctx, Xd, dtype, N, D, ldd, idx_d, k, p.klle_shift, w_d);
+        else
+            ltsa_basis(ctx, Xd, dtype, N, D, ldd, idx_d, k, td, w_d);
+        TK_CUDA(cudaEventRecord(ctx->ev[5], st));
+
+        // M
+        int64_t* rp_d = (int64_t*)ctx->scratch.get("op.rowptr", sizeof(int64_t) * ((size_t)N + 1));
+        const int64_t nnz_bound = N * (int64_t)(k + 1) * (k + 1);
+        (void)nnz_bound;
+        const int64_t nnz = assemble(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, nullptr,
+                                     nullptr, true);
+        int32_t* col_d = (int32_t*)ctx->scratch.get("op.col", sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1));
+        double* val_d = (double*)ctx->scratch.get("op.vals", sizeof(double) * (size_t)std::max<int64_t>(nnz, 1));
+        assemble(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, col_d, val_d, false);
+        TK_CUDA(cudaEventRecord(ctx->ev[6], st));
+        check_device_errors(ctx);
+
+        tk_operator_info& o = ctx->op;
+        std::memset(&o, 0, sizeof(o));
+        o.n = N;
+        o.k = k;
+        o.method = p.method;
+        o.target_dimension = td;
+        o.connectivity_retries = retries;
+        o.nnz = nnz;
+        o.rows_uncertified = uncert;
+        o.stage_ms[0] = ms_knn;
+        o.stage_ms[1] = ms_conn;
+        o.stage_ms[2] = elapsed(ctx->ev[4], ctx->ev[5]);
+        o.stage_ms[3] = elapsed(ctx->ev[5], ctx->ev[6]);
+        o.stage_ms[4] = elapsed(ctx->ev[0], ctx->ev[6]);
+        ctx->op_valid = true;
+        if (info)
+            *info = o;
+    });
+}
+
+int tk_operator_get_info(const tk_ctx* ctx, tk_operator_info* info)
+{
+    if (!ctx || !info)
+        return TK_ERR_INVALID_ARG;
+    if (!ctx->op_valid)
+        return TK_ERR_INVALID_ARG;
+    *info = ctx->op;
+    return TK_OK;
+}
+
+int tk_operator_device_views(tk_ctx* ctx, const int32_t** idx, const double** weights, const int64_t** row_ptr,
+                             const int32_t** col_idx, const double** vals)
+{
+    if (!ctx || !ctx->op_valid)
+        return TK_ERR_INVALID_ARG;
+    auto& bufs = ctx->scratch.bufs;
+    if (idx)
+        *idx = (const int32_t*)bufs["op.idx"].ptr;
+    if (weights)
+        *weights = (const double*)bufs["op.w"].ptr;
+    if (row_ptr)
+        *row_ptr = (const int64_t*)bufs["op.rowptr"].ptr;
+    if (col_idx)
+        *col_idx = (const int32_t*)bufs["op.col"].ptr;
+    if (vals)
+        *vals = (const double*)bufs["op.vals"].ptr;
+    return TK_OK;
+}
+
+int tk_operator_copy(tk_ctx* ctx, int32_t* idx, double* weights, int64_t* row_ptr, int32_t* col_idx, double* vals)
+{
+    return guarded(ctx, [&] {
+        if (!ctx->op_valid)
+            throw Error(TK_ERR_INVALID_ARG, "no operator held by this context");
+        const tk_operator_info& o = ctx->op;
+        auto& bufs = ctx->scratch.bufs;
+        const size_t nk = (size_t)o.n * o.k;
+        const size_t wc = nk * (o.method == TK_METHOD_KLTSA ? o.target_dimension : 1);
+        auto cp = [&](void* dst, const char* name, size_t bytes) {
+            if (!dst || bytes == 0)
+                return;
+            TK_CUDA(cudaMemcpyAsync(dst, bufs[name].ptr, bytes, cudaMemcpyDefault, ctx->stream));
+        };
+        cp(idx, "op.idx", nk * sizeof(int32_t));
+        cp(weights, "op.w", wc * sizeof(double));
+        cp(row_ptr, "op.rowptr", ((size_t)o.n + 1) * sizeof(int64_t));
+        cp(col_idx, "op.col", (size_t)o.nnz * sizeof(int32_t));
+        cp(vals, "op.vals", (size_t)o.nnz * sizeof(double));
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+} // extern "C"

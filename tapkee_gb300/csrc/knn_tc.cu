@@ -1,0 +1,483 @@
+// knn_tc.cu -- tensor-core (tcgen05) distance screen for sm_103a.
+//
+// Each CTA owns QT blocks of 128 queries (sorted order) and streams every
+// candidate tile of 128 points through a STAGES-deep TMA pipeline. The dot
+// products x.y run on the 5th-generation tensor cores as an fp16 split GEMM
+// with FP32 accumulation in tensor memory:
+//      x.y ~ 2^-2s (h_x.h_y + h_x.l_y + l_x.h_y),   2^s x = h_x + l_x (fp16 hi/lo)
+// (about 22 significant bits; the dropped l_x.l_y term is below 2^-22 |x||y|).
+// Accumulators (128 lanes x 128 columns FP32 per query block) are
+// double-buffered in TMEM so the MMA of tile t+1 overlaps the epilogue of tile t.
+//
+// Warp roles (320 threads):
+//   warps 0..7  epilogue: tcgen05.ld the accumulator rows, form
+//               a - |x|^2 = |y|^2 - 2 x.y, and keep per query row (one thread per
+//               row) the KC smallest values in a sorted register list; entries at
+//               or above the row's KC-th value are rejected with one compare;
+//   warp  8     TMA producer (one thread): A tiles once, then B hi/lo tiles;
+//   warp  9     TMEM allocator and MMA issuer (one thread).
+// Every mbarrier wait is bounded by a wall-clock limit: on expiry the CTA records
+// DEV_ERR_TIMEOUT, drains the copies and MMAs it issued (again bounded), frees
+// its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+
+#include <cfloat>
+
+#include "screen_common.cuh"
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+constexpr int TC_N = 128;      // candidates per stage (MMA N)
+constexpr int TC_M = 128;      // queries per A tile (MMA M)
+constexpr int TC_THREADS = 320;
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per single wait
+
+template <int DP>
+struct TcCfg
+{
+    static constexpr int QT = (DP <= 64) ? 2 : 1;  // A tiles (query blocks) per CTA
+    static constexpr int KATOMS = DP / 64;         // 128-byte swizzle atoms along K
+    static constexpr int ATOM_BYTES = 128 * 128;   // 128 rows x 128 B
+    static constexpr int A_BYTES = QT * 2 * KATOMS * ATOM_BYTES;
+    static constexpr int STAGES = (DP <= 64) ? 4 : 2;
+    static constexpr int B_STAGE_BYTES = 2 * KATOMS * ATOM_BYTES;
+    static constexpr int ACC_COLS = QT * TC_N;
+    static constexpr int TMEM_COLS = 2 * ACC_COLS;  // 512 or 256, power of two
+    static constexpr int EPI_WARPS = 4 * QT;
+    static constexpr int MMAS_PER_STAGE = QT * 3 * (DP / 16);
+    static constexpr size_t SMEM = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES + 1024 /*align*/ + 256;
+};
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; returns false (and raises the CTA abort flag) on expiry or when
+// another role already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort, unsigned* err)
+{
+    if (mbar_try(bar, parity))
+        return true;
+    const uint64_t t0 = gtimer();
+    for (uint32_t it = 1;; ++it)
+    {
+        if (mbar_try(bar, parity))
+            return true;
+        if ((it & 63u) == 0u)
+        {
+            if (*abort)
+                return false;
+            if (gtimer() - t0 > WAIT_LIMIT_NS)
+            {
+                *abort = 1;
+                atomicOr(err, DEV_ERR_TIMEOUT);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
+// groups 1024 B apart (SBO), version bit 46 set.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// kind::f16 instruction descriptor: D=F32, A=B=F16, K-major both, N=128, M=128
+constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+
+__device__ __forceinline__ void umma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int t = 0; t < 16; ++t)
+        v[t] = __uint_as_float(r[t]);
+}
+
+// Branchless sorted insertion into a register list (ascending).
+template <int KC>
+__device__ __forceinline__ void reg_insert(float (&L)[KC], int32_t (&I)[KC], float v, int32_t id)
+{
+#pragma unroll
+    for (int s = KC - 1; s > 0; --s)
+    {
+        const bool sh = v < L[s - 1];
+        const bool pl = !sh && (v < L[s]);
+        L[s] = sh ? L[s - 1] : (pl ? v : L[s]);
+        I[s] = sh ? I[s - 1] : (pl ? id : I[s]);
+    }
+    if (v < L[0])
+    {
+        L[0] = v;
+        I[0] = id;
+    }
+}
+
+struct TcBarriers
+{
+    uint64_t full[4], empty[4], tfull[2], tempty[2], afull, fin;
+    uint32_t tmem_base;
+    int abort;
+};
+
+template <int DP, int KC>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_screen_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
+                const float* __restrict__ nrm, const float* __restrict__ scale_log2, int64_t Npad,
+                int32_t* __restrict__ cand_idx, float* __restrict__ cand_val, unsigned* err)
+{
+    using C = TcCfg<DP>;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned operand region
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char* gbase = smem_raw + (base - raw);
+    const uint32_t A_s = base;
+    const uint32_t B_s = base + C::A_BYTES;
+    TcBarriers& Bar = *reinterpret_cast<TcBarriers*>(gbase + C::A_BYTES + C::STAGES * C::B_STAGE_BYTES);
+    volatile int* abort = &Bar.abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = (int)(Npad / TC_N);
+    const int64_t q0 = (int64_t)blockIdx.x * (C::QT * TC_M);
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < C::STAGES; ++s)
+        {
+            mbar_init(smem_u32(&Bar.full[s]), 1);
+            mbar_init(smem_u32(&Bar.empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b)
+        {
+            mbar_init(smem_u32(&Bar.tfull[b]), 1);
+            mbar_init(smem_u32(&Bar.tempty[b]), C::EPI_WARPS);
+        }
+        mbar_init(smem_u32(&Bar.afull), 1);
+        mbar_init(smem_u32(&Bar.fin), 1);
+        Bar.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 9)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&Bar.tmem_base)),
+                     "r"(C::TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = Bar.tmem_base;
+
+    if (warp == 8)
+    {
+        // ------------------------------------------------------------ producer
+        if (lane == 0)
+        {
+            const uint32_t afull = smem_u32(&Bar.afull);
+            mbar_expect_tx(afull, C::A_BYTES);
+            for (int qt = 0; qt < C::QT; ++qt)
+                for (int part = 0; part < 2; ++part)
+                    for (int ka = 0; ka < C::KATOMS; ++ka)
+                        tma_load_2d(A_s + ((qt * 2 + part) * C::KATOMS + ka) * C::ATOM_BYTES, part ? &tm_lo : &tm_hi,
+                                    ka * 64, (int)(q0 + qt * TC_M), afull);
+            ZigZag zz((int)blockIdx.x * C::QT, ntiles);
+            int issued = 0;
+            for (int it = 0; it < ntiles; ++it)
+            {
+                const int tile = zz.next();
+                const int slot = it % C::STAGES;
+                const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
+                if (!mbar_wait(smem_u32(&Bar.empty[slot]), ph ^ 1u, abort, err))
+                    break;
+                const uint32_t fb = smem_u32(&Bar.full[slot]);
+                mbar_expect_tx(fb, C::B_STAGE_BYTES);
+                for (int part = 0; part < 2; ++part)
+                    for (int ka = 0; ka < C::KATOMS; ++ka)
+                        tma_load_2d(B_s + slot * C::B_STAGE_BYTES + (part * C::KATOMS + ka) * C::ATOM_BYTES,
+                                    part ? &tm_lo : &tm_hi, ka * 64, tile * TC_N, fb);
+                issued = it + 1;
+            }
+            if (*abort)
+            {
+                // drain the loads still in flight (bounded)
+                volatile int no_abort = 0;
+                mbar_wait(afull, 0u, &no_abort, err);
+                for (int j = (issued > C::STAGES ? issued - C::STAGES : 0); j < issued; ++j)
+                    mbar_wait(smem_u32(&Bar.full[j % C::STAGES]), (uint32_t)(j / C::STAGES) & 1u, &no_abort, err);
+            }
+        }
+    }
+    else if (warp == 9)
+    {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0)
+        {
+            bool ok = mbar_wait(smem_u32(&Bar.afull), 0u, abort, err);
+            tc_fence_after();
+            int issued_any = 0;
+            for (int it = 0; ok && it < ntiles; ++it)
+            {
+                const int slot = it % C::STAGES;
+                const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
+                const int buf = it & 1;
+                const uint32_t bph = (uint32_t)(it >> 1) & 1u;
+                if (!mbar_wait(smem_u32(&Bar.full[slot]), ph, abort, err))
+                    break;
+                if (!mbar_wait(smem_u32(&Bar.tempty[buf]), bph ^ 1u, abort, err))
+                    break;
+                tc_fence_after();
+                const uint32_t bstage = B_s + slot * C::B_STAGE_BYTES;
+#pragma unroll
+                for (int qt = 0; qt < C::QT; ++qt)
+                {
+                    const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
+                    uint32_t acc = 0;
+#pragma unroll
+                    for (int prod = 0; prod < 3; ++prod)
+                    {
+                        const int apart = (prod == 2) ? 1 : 0;  // l_x . h_y
+                        const int bpart = (prod == 1) ? 1 : 0;  // h_x . l_y
+#pragma unroll
+                        for (int kk = 0; kk < DP / 16; ++kk)
+                        {
+                            const int ka = kk >> 2;
+                            const uint32_t koff = (uint32_t)(kk & 3) * 32u;
+                            const uint64_t ad = umma_desc(A_s + ((qt * 2 + apart) * C::KATOMS + ka) * C::ATOM_BYTES + koff);
+                            const uint64_t bd = umma_desc(bstage + (bpart * C::KATOMS + ka) * C::ATOM_BYTES + koff);
+                            umma_f16(d, ad, bd, acc);
+                            acc = 1;
+                        }
+                    }
+                }
+                umma_commit(smem_u32(&Bar.empty[slot]));
+                umma_commit(smem_u32(&Bar.tfull[buf]));
+                issued_any = 1;
+            }
+            if (issued_any)
+            {
+                // every MMA this thread issued (and its barrier arrivals) completes
+                // before TMEM is freed and the CTA's shared memory is released
+                volatile int no_abort = 0;
+                umma_commit(smem_u32(&Bar.fin));
+                mbar_wait(smem_u32(&Bar.fin), 0u, &no_abort, err);
+            }
+        }
+    }
+    else if (warp < C::EPI_WARPS)
+    {
+        // ------------------------------------------------------------ epilogue
+        const int quad = warp & 3;
+        const int qt = warp >> 2;
+        const int row = quad * 32 + lane;
+        const int64_t q = q0 + qt * TC_M + row;
+        const float nq = nrm[q];
+        const float m2 = -2.0f * exp2f(-2.0f * scale_log2[0]);
+        float L[KC];
+        int32_t I[KC];
+#pragma unroll
+        for (int s = 0; s < KC; ++s)
+        {
+            L[s] = FLT_MAX;
+            I[s] = -1;
+        }
+        ZigZag zz((int)blockIdx.x * C::QT, ntiles);
+        for (int it = 0; it < ntiles; ++it)
+        {
+            const int tile = zz.next();
+            const int buf = it & 1;
+            const uint32_t bph = (uint32_t)(it >> 1) & 1u;
+            // tcgen05.ld is warp-collective: leave the loop as a whole warp
+            const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf]), bph, abort, err);
+            if (!__all_sync(0xffffffffu, ok))
+                break;
+            tc_fence_after();
+            const int64_t c0 = (int64_t)tile * TC_N;
+            const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
+            float cmp = L[KC - 1];
+#pragma unroll 1
+            for (int ch = 0; ch < TC_N / 16; ++ch)
+            {
+                float v[16];
+                tmem_ld16(tacc + ch * 16, v);
+                const float4* np = reinterpret_cast<const float4*>(nrm + c0 + ch * 16);
+#pragma unroll
+                for (int g = 0; g < 4; ++g)
+                {
+                    const float4 n4 = __ldg(np + g);
+                    const float nn[4] = {n4.x, n4.y, n4.z, n4.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                    {
+                        const float t = fmaf(m2, v[g * 4 + e], nn[e]);
+                        if (t < cmp)
+                        {
+                            reg_insert<KC>(L, I, t, (int32_t)(c0 + ch * 16 + g * 4 + e));
+                            cmp = L[KC - 1];
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(smem_u32(&Bar.tempty[buf]));
+        }
+#pragma unroll
+        for (int s = 0; s < KC; ++s)
+        {
+            cand_idx[q * KC + s] = I[s];
+            cand_val[q * KC + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 9)
+    {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS));
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn)
+    {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        TK_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p)
+            throw Error(TK_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int Dp)
+{
+    const cuuint64_t dims[2] = {(cuuint64_t)Dp, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)Dp * 2};
+    const cuuint32_t box[2] = {64, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, (void*)base, dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        throw Error(TK_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+}
+
+template <int DP, int KC>
+void launch(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
+{
+    using C = TcCfg<DP>;
+    static_assert(C::SMEM <= 227 * 1024, "shared memory budget");
+    CUtensorMap mh, ml;
+    make_map(&mh, P.xh, P.Npad, P.Dp);
+    make_map(&ml, P.xl, P.Npad, P.Dp);
+    TK_CUDA(cudaFuncSetAttribute(k_screen_tc<DP, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+    const int grid = (int)(P.Npad / (C::QT * TC_M));
+    k_screen_tc<DP, KC><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, P.nrm, P.rmax + 1, P.Npad, cand_idx,
+                                                                    cand_val, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+}
+
+} // namespace
+
+bool tensor_screen_supported(int Dp) { return Dp == 64 || Dp == 128; }
+
+void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
+{
+    if (!P.xh || !P.xl)
+        throw Error(TK_ERR_INTERNAL, "tensor screen needs the fp16 split layout");
+    if (P.Dp == 64)
+    {
+        if (kc == 32)
+            launch<64, 32>(ctx, P, cand_idx, cand_val);
+        else
+            launch<64, 64>(ctx, P, cand_idx, cand_val);
+    }
+    else if (P.Dp == 128)
+    {
+        if (kc == 32)
+            launch<128, 32>(ctx, P, cand_idx, cand_val);
+        else
+            launch<128, 64>(ctx, P, cand_idx, cand_val);
+    }
+    else
+        throw Error(TK_ERR_UNSUPPORTED, "the tensor-core screen supports D <= 128 (padded to 64 or 128); use the "
+                                        "FP32 screen for D = " +
+                                            std::to_string(P.D));
+}
+
+} // namespace tk

@@ -1,0 +1,326 @@
+// lle.cu -- LLE reconstruction weights, one warp per point.
+//
+// Per point x with neighbours n_0..n_{k-1} (routines/locally_linear.hpp:107-131):
+//   C_ab = (n_a - x).(n_b - x)          the reference's kernel form
+//                                       k(x,x)-k(x,n_a)-k(x,n_b)+k(n_a,n_b)
+//   C   += klle_shift * trace(C) * I
+//   w    = C^{-1} 1,  w /= sum(w)
+// The Gram is accumulated in FP32 from difference vectors staged through shared
+// memory in 32-dimension chunks, factorised by an FP32 Cholesky, and the solve
+// is refined against a float-float residual r = 1 - (C_true + s_true I) w built
+// from the exact differences (two refinement steps when k > D, where C is rank
+// deficient and its conditioning is set by klle_shift; one otherwise).
+#include <cfloat>
+
+#include "ff.cuh"
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+__device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
+{
+    return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
+}
+
+template <int KP>
+struct LleSmem
+{
+    float Zh[KP][33];
+    float Zl[KP][33];
+    float C[KP][KP + 1];
+    float vh[32], vl[32];
+    float r[KP];
+    float w[KP];
+};
+
+template <int KP>
+__device__ __forceinline__ void chol_solve(LleSmem<KP>& S, int lane)
+{
+    // forward L y = r
+    for (int j = 0; j < KP; ++j)
+    {
+        __syncwarp();
+        const float yj = S.r[j] / S.C[j][j];
+        __syncwarp();
+        if (lane == 0)
+            S.r[j] = yj;
+        for (int rr = j + 1 + lane; rr < KP; rr += 32)
+            S.r[rr] = fmaf(-S.C[rr][j], yj, S.r[rr]);
+    }
+    // backward L^T x = y
+    for (int j = KP - 1; j >= 0; --j)
+    {
+        __syncwarp();
+        const float xj = S.r[j] / S.C[j][j];
+        __syncwarp();
+        if (lane == 0)
+            S.r[j] = xj;
+        for (int rr = lane; rr < j; rr += 32)
+            S.r[rr] = fmaf(-S.C[j][rr], xj, S.r[rr]);
+    }
+    __syncwarp();
+}
+
+template <int KP, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, int64_t N, int D, int64_t ldx,
+                                                    const int32_t* __restrict__ idx, int k, double klle_shift,
+                                                    double* __restrict__ W, unsigned* err)
+{
+    constexpr int NB4 = KP / 4;
+    constexpr int NBLK = NB4 * (NB4 + 1) / 2;
+    constexpr int PERL = (NBLK + 31) / 32;
+    constexpr int NPL = (KP + 31) / 32;  // neighbours per lane
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    LleSmem<KP>& S = reinterpret_cast<LleSmem<KP>*>(smem_raw)[wib];
+    const int64_t warp = (int64_t)blockIdx.x * WARPS + wib;
+    const int64_t nwarps = (int64_t)gridDim.x * WARPS;
+
+    // (I, J) 4x4 blocks of the upper triangle owned by this lane
+    int bI[PERL], bJ[PERL];
+#pragma unroll
+    for (int m = 0; m < PERL; ++m)
+    {
+        int b = lane + 32 * m, I = 0;
+        if (b >= NBLK)
+            b = 0;
+        while (b >= NB4 - I)
+        {
+            b -= NB4 - I;
+            ++I;
+        }
+        bI[m] = I;
+        bJ[m] = I + b;
+    }
+
+    for (int64_t i = warp; i < N; i += nwarps)
+    {
+        int nb[NPL];
+#pragma unroll
+        for (int s = 0; s < NPL; ++s)
+        {
+            const int a = lane + 32 * s;
+            nb[s] = (a < k) ? idx[i * k + a] : 0;
+            if (a < k && (nb[s] < 0 || nb[s] >= N))
+            {
+                atomicOr(err, DEV_ERR_BOUNDS);
+                nb[s] = 0;
+            }
+        }
+
+        // ---- FP32 Gram ----
+        float acc[PERL][16];
+#pragma unroll
+        for (int m = 0; m < PERL; ++m)
+#pragma unroll
+            for (int t = 0; t < 16; ++t)
+                acc[m][t] = 0.f;
+        for (int d0 = 0; d0 < D; d0 += 32)
+        {
+            const int d = d0 + lane;
+            const double xi = (d < D) ? ldx_elem(X, dtype, i * ldx + d) : 0.0;
+#pragma unroll 4
+            for (int a = 0; a < KP; ++a)
+            {
+                const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
+                float v = 0.f;
+                if (a < k && d < D)
+                    v = (float)(ldx_elem(X, dtype, (int64_t)nba * ldx + d) - xi);
+                S.Zh[a][lane] = v;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int m = 0; m < PERL; ++m)
+            {
+                if (lane + 32 * m < NBLK)
+                {
+                    const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
+#pragma unroll 8
+                    for (int dd = 0; dd < 32; ++dd)
+                    {
+                        float av[4], bv[4];
+#pragma unroll
+                        for (int t = 0; t < 4; ++t)
+                        {
+                            av[t] = S.Zh[I4 + t][dd];
+                            bv[t] = S.Zh[J4 + t][dd];
+                        }
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c)
+                                acc[m][r * 4 + c] = fmaf(av[r], bv[c], acc[m][r * 4 + c]);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int m = 0; m < PERL; ++m)
+            if (lane + 32 * m < NBLK)
+            {
+                const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c)
+                    {
+                        S.C[I4 + r][J4 + c] = acc[m][r * 4 + c];
+                        S.C[J4 + c][I4 + r] = acc[m][r * 4 + c];
+                    }
+            }
+        __syncwarp();
+        float trace = 0.f;
+        for (int a = 0; a < k; ++a)
+            trace += S.C[a][a];
+        __syncwarp();
+        const float shift = (float)klle_shift * trace;
+        for (int a = lane; a < KP; a += 32)
+        {
+            if (a < k)
+                S.C[a][a] += shift;
+            else
+                S.C[a][a] = 1.f;  // padding rows/columns are zero: identity block
+            S.r[a] = (a < k) ? 1.f : 0.f;
+        }
+        __syncwarp();
+
+        // ---- FP32 Cholesky (lower, in place) ----
+        for (int j = 0; j < KP; ++j)
+        {
+            const float ljj = sqrtf(fmaxf(S.C[j][j], FLT_MIN));
+            __syncwarp();
+            for (int rr = j + 1 + lane; rr < KP; rr += 32)
+                S.C[rr][j] /= ljj;
+            if (lane == 0)
+                S.C[j][j] = ljj;
+            __syncwarp();
+            for (int rr = j + 1 + lane; rr < KP; rr += 32)
+            {
+                const float lrj = S.C[rr][j];
+                for (int c = j + 1; c <= rr; ++c)
+                    S.C[rr][c] = fmaf(-lrj, S.C[c][j], S.C[rr][c]);
+            }
+            __syncwarp();
+        }
+        chol_solve<KP>(S, lane);
+        for (int a = lane; a < KP; a += 32)
+            S.w[a] = (a < k) ? S.r[a] : 0.f;
+        __syncwarp();
+
+        // ---- float-float residual refinement ----
+        const int iters = (k > D) ? 2 : 1;
+        for (int itr = 0; itr < iters; ++itr)
+        {
+            ff sa[NPL], ta[NPL];
+#pragma unroll
+            for (int s = 0; s < NPL; ++s)
+            {
+                sa[s] = ff_zero();
+                ta[s] = ff_zero();
+            }
+            for (int d0 = 0; d0 < D; d0 += 32)
+            {
+                const int d = d0 + lane;
+                const double xi = (d < D) ? ldx_elem(X, dtype, i * ldx + d) : 0.0;
+                for (int a = 0; a < KP; ++a)
+                {
+                    const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
+                    float h = 0.f, l = 0.f;
+                    if (a < k && d < D)
+                    {
+                        const double z = ldx_elem(X, dtype, (int64_t)nba * ldx + d) - xi;
+                        h = (float)z;
+                        l = (float)(z - (double)h);
+                    }
+                    S.Zh[a][lane] = h;
+                    S.Zl[a][lane] = l;
+                }
+                __syncwarp();
+                // v_d = sum_b w_b z_bd for d = d0 + lane
+                ff v = ff_zero();
+                for (int b = 0; b < k; ++b)
+                    v = ff_fma(v, S.w[b], 0.f, S.Zh[b][lane], S.Zl[b][lane]);
+                S.vh[lane] = v.hi;
+                S.vl[lane] = v.lo;
+                __syncwarp();
+#pragma unroll
+                for (int s = 0; s < NPL; ++s)
+                {
+                    const int a = lane + 32 * s;
+                    if (a < k)
+                        for (int dd = 0; dd < 32; ++dd)
+                        {
+                            const float zh = S.Zh[a][dd], zl = S.Zl[a][dd];
+                            sa[s] = ff_fma(sa[s], zh, zl, S.vh[dd], S.vl[dd]);
+                            ta[s] = ff_fma(ta[s], zh, zl, zh, zl);
+                        }
+                }
+                __syncwarp();
+            }
+            // exact trace = sum_a |z_a|^2
+            ff tr = ff_zero();
+#pragma unroll
+            for (int s = 0; s < NPL; ++s)
+                tr = ff_add(tr, ta[s]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                tr = ff_add(tr, ff_shfl_xor(tr, o));
+            const double shift_true = klle_shift * ff_to_double(tr);
+#pragma unroll
+            for (int s = 0; s < NPL; ++s)
+            {
+                const int a = lane + 32 * s;
+                if (a < KP)
+                    S.r[a] = (a < k) ? (float)(1.0 - ff_to_double(sa[s]) - shift_true * (double)S.w[a]) : 0.f;
+            }
+            __syncwarp();
+            chol_solve<KP>(S, lane);
+            for (int a = lane; a < k; a += 32)
+                S.w[a] += S.r[a];
+            __syncwarp();
+        }
+
+        // ---- normalise and store ----
+        double sum = 0.0;
+        for (int a = lane; a < k; a += 32)
+            sum += (double)S.w[a];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        for (int a = lane; a < k; a += 32)
+            W[i * k + a] = (double)S.w[a] / sum;
+        __syncwarp();
+    }
+}
+
+template <int KP, int WARPS>
+void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+            double klle_shift, double* W)
+{
+    const size_t smem = sizeof(LleSmem<KP>) * WARPS;
+    TK_CUDA(cudaFuncSetAttribute(k_lle<KP, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t want = (N + WARPS - 1) / WARPS;
+    const int grid = (int)std::min<int64_t>(want, (int64_t)ctx->num_sms * 16);
+    k_lle<KP, WARPS><<<grid, WARPS * 32, smem, ctx->stream>>>(X, dtype, N, D, ldx, idx, k, klle_shift, W,
+                                                               ctx->dev_err);
+    TK_CHECK_LAUNCH();
+}
+
+} // namespace
+
+void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+                 double klle_shift, double* W)
+{
+    if (k <= 16)
+        launch<16, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
+    else if (k <= 32)
+        launch<32, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
+    else if (k <= 64)
+        launch<64, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
+    else
+        throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 64 neighbours");
+}
+
+} // namespace tk

@@ -1,0 +1,301 @@
+// ltsa.cu -- LTSA local tangent bases, one warp per point.
+//
+// Per point with neighbours n_0..n_{k-1} (routines/locally_linear.hpp:45-63):
+//   K_ab = k(n_a, n_b), double-centred (centerMatrix, utils/matrix.hpp:12-19),
+//   V    = eigenvectors of the td largest eigenvalues,
+// and the alignment block is P = (1/k) 1 1^T + V V^T (G = [1/sqrt(k) 1, V]).
+// The double-centred Gram equals Zc Zc^T with Zc the neighbours minus their
+// mean, which is what is accumulated here (in FP32, from FP64-centred
+// coordinates, avoiding the cancellation of the raw kernel form). The
+// eigen-decomposition is a cyclic Jacobi in shared memory with the round-robin
+// (tournament) ordering: each round applies k/2 disjoint rotations in parallel.
+// Points whose gap lambda_td - lambda_{td+1} is below 1e-6 of lambda_max have an
+// ill-conditioned tangent space; they are redone with an FP64 Jacobi.
+#include <cfloat>
+#include <cmath>
+
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+__device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
+{
+    return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
+}
+
+template <int M, typename T>
+struct JacobiSmem
+{
+    T A[M][M + 1];
+    T V[M][M + 1];
+    T rc[M / 2], rs[M / 2];
+    int rp[M / 2], rq[M / 2];
+    float Z[M][33];
+};
+
+// Parallel cyclic Jacobi on the symmetric M x M matrix S.A (one warp). On exit
+// diag(A) holds the eigenvalues and the columns of V the eigenvectors.
+template <int M, typename T>
+__device__ void warp_jacobi(JacobiSmem<M, T>& S, int lane, int max_sweeps)
+{
+    for (int t = lane; t < M * M; t += 32)
+        S.V[t / M][t % M] = (t / M == t % M) ? T(1) : T(0);
+    __syncwarp();
+    for (int sweep = 0; sweep < max_sweeps; ++sweep)
+    {
+        // convergence test: off-diagonal vs diagonal mass
+        T off = 0, dia = 0;
+        for (int t = lane; t < M * M; t += 32)
+        {
+            const T v = S.A[t / M][t % M];
+            if (t / M == t % M)
+                dia += v * v;
+            else
+                off += v * v;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+            dia += __shfl_xor_sync(0xffffffffu, dia, o);
+        }
+        const T tol = sizeof(T) == 8 ? T(1e-30) : T(1e-14);
+        if (off <= tol * dia || dia == T(0))
+            break;
+        for (int round = 0; round < M - 1; ++round)
+        {
+            if (lane < M / 2)
+            {
+                auto pos = [&](int t) { return t == 0 ? 0 : 1 + ((t - 1 + round) % (M - 1)); };
+                int p = pos(lane), q = pos(M - 1 - lane);
+                if (p > q)
+                {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                const T apq = S.A[p][q], app = S.A[p][p], aqq = S.A[q][q];
+                T c = T(1), s = T(0);
+                if (apq != T(0))
+                {
+                    const T theta = (aqq - app) / (T(2) * apq);
+                    const T tt = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+                    c = T(1) / sqrt(tt * tt + T(1));
+                    s = tt * c;
+                }
+                S.rp[lane] = p;
+                S.rq[lane] = q;
+                S.rc[lane] = c;
+                S.rs[lane] = s;
+            }
+            __syncwarp();
+            // rows: A[p,:], A[q,:]
+            for (int e = lane; e < (M / 2) * M; e += 32)
+            {
+                const int i = e / M, j = e % M;
+                const int p = S.rp[i], q = S.rq[i];
+                const T c = S.rc[i], s = S.rs[i];
+                const T apj = S.A[p][j], aqj = S.A[q][j];
+                S.A[p][j] = c * apj - s * aqj;
+                S.A[q][j] = s * apj + c * aqj;
+            }
+            __syncwarp();
+            // columns: A[:,p], A[:,q] and V[:,p], V[:,q]
+            for (int e = lane; e < (M / 2) * M; e += 32)
+            {
+                const int i = e / M, j = e % M;
+                const int p = S.rp[i], q = S.rq[i];
+                const T c = S.rc[i], s = S.rs[i];
+                const T ajp = S.A[j][p], ajq = S.A[j][q];
+                S.A[j][p] = c * ajp - s * ajq;
+                S.A[j][q] = s * ajp + c * ajq;
+                const T vjp = S.V[j][p], vjq = S.V[j][q];
+                S.V[j][p] = c * vjp - s * vjq;
+                S.V[j][q] = s * vjp + c * vjq;
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Builds the centred neighbour Gram of point i into S.A (type T, M x M, zero padded).
+template <int M, typename T>
+__device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
+                             const int32_t* nbrs, int k)
+{
+    for (int t = lane; t < M * M; t += 32)
+        S.A[t / M][t % M] = T(0);
+    __syncwarp();
+    for (int d0 = 0; d0 < D; d0 += 32)
+    {
+        const int d = d0 + lane;
+        double mean = 0.0;
+        if (d < D)
+            for (int a = 0; a < k; ++a)
+                mean += ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d);
+        mean /= (double)k;
+        for (int a = 0; a < M; ++a)
+            S.Z[a][lane] = (a < k && d < D) ? (float)(ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d) - mean) : 0.f;
+        __syncwarp();
+        for (int e = lane; e < M * M; e += 32)
+        {
+            const int a = e / M, b = e % M;
+            if (b < a || a >= k || b >= k)
+                continue;
+            T s = T(0);
+            for (int dd = 0; dd < 32; ++dd)
+                s += (T)S.Z[a][dd] * (T)S.Z[b][dd];
+            S.A[a][b] += s;
+            if (a != b)
+                S.A[b][a] += s;
+        }
+        __syncwarp();
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__(128) k_ltsa(const void* X, int dtype, int64_t N, int D, int64_t ldx,
+                                              const int32_t* __restrict__ idx, int k, int td, double* V,
+                                              int32_t* refine, unsigned* nrefine)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    JacobiSmem<M, float>& S = reinterpret_cast<JacobiSmem<M, float>*>(smem_raw)[wib];
+    __shared__ int nb_s[4][M];
+    const int64_t nw = (int64_t)gridDim.x * 4;
+    for (int64_t i = (int64_t)blockIdx.x * 4 + wib; i < N; i += nw)
+    {
+        for (int a = lane; a < k; a += 32)
+            nb_s[wib][a] = idx[i * k + a];
+        __syncwarp();
+        centred_gram<M, float>(S, lane, X, dtype, ldx, D, nb_s[wib], k);
+        warp_jacobi<M, float>(S, lane, 30);
+        // order eigenvalues (lane 0, M <= 32): top td indices
+        __shared__ int top_s[4][8];
+        if (lane == 0)
+        {
+            float lmax = -FLT_MAX;
+            int chosen[9];
+            for (int t = 0; t <= td && t < M; ++t)
+            {
+                int best = -1;
+                float bv = -FLT_MAX;
+                for (int c = 0; c < M; ++c)
+                {
+                    bool used = false;
+                    for (int u = 0; u < t; ++u)
+                        used |= (chosen[u] == c);
+                    if (!used && S.A[c][c] > bv)
+                    {
+                        bv = S.A[c][c];
+                        best = c;
+                    }
+                }
+                chosen[t] = best;
+                if (t == 0)
+                    lmax = bv;
+            }
+            for (int t = 0; t < td; ++t)
+                top_s[wib][t] = chosen[t];
+            const float gap = S.A[chosen[td - 1]][chosen[td - 1]] - (td < M ? S.A[chosen[td]][chosen[td]] : 0.f);
+            if (!(gap > 1e-6f * fabsf(lmax)))
+                refine[atomicAdd(nrefine, 1u)] = (int32_t)i;
+        }
+        __syncwarp();
+        for (int e = lane; e < k * td; e += 32)
+        {
+            const int a = e / td, t = e % td;
+            V[(i * k + a) * td + t] = (double)S.V[a][top_s[wib][td - 1 - t]];
+        }
+        __syncwarp();
+    }
+}
+
+// FP64 redo of the points flagged for a small eigen-gap (one warp per block).
+template <int M>
+__global__ void __launch_bounds__(32) k_ltsa_fp64(const void* X, int dtype, int64_t N, int D, int64_t ldx,
+                                                  const int32_t* __restrict__ idx, int k, int td, double* V,
+                                                  const int32_t* refine, const unsigned* nrefine)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    JacobiSmem<M, double>& S = *reinterpret_cast<JacobiSmem<M, double>*>(smem_raw);
+    __shared__ int nb_s[M];
+    __shared__ int top_s[8];
+    const int lane = threadIdx.x;
+    const unsigned nr = *nrefine;
+    for (unsigned r = blockIdx.x; r < nr; r += gridDim.x)
+    {
+        const int64_t i = refine[r];
+        for (int a = lane; a < k; a += 32)
+            nb_s[a] = idx[i * k + a];
+        __syncwarp();
+        centred_gram<M, double>(S, lane, X, dtype, ldx, D, nb_s, k);
+        warp_jacobi<M, double>(S, lane, 60);
+        if (lane == 0)
+        {
+            int chosen[8];
+            for (int t = 0; t < td; ++t)
+            {
+                int best = -1;
+                double bv = -1e300;
+                for (int c = 0; c < M; ++c)
+                {
+                    bool used = false;
+                    for (int u = 0; u < t; ++u)
+                        used |= (chosen[u] == c);
+                    if (!used && S.A[c][c] > bv)
+                    {
+                        bv = S.A[c][c];
+                        best = c;
+                    }
+                }
+                chosen[t] = best;
+                top_s[t] = best;
+            }
+        }
+        __syncwarp();
+        for (int e = lane; e < k * td; e += 32)
+        {
+            const int a = e / td, t = e % td;
+            V[(i * k + a) * td + t] = S.V[a][top_s[td - 1 - t]];
+        }
+        __syncwarp();
+    }
+}
+
+template <int M>
+void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k, int td,
+            double* V)
+{
+    cudaStream_t st = ctx->stream;
+    int32_t* refine = (int32_t*)ctx->scratch.get("ltsa.refine", sizeof(int32_t) * (size_t)N);
+    unsigned* nrefine = (unsigned*)ctx->scratch.get("ltsa.nrefine", 16);
+    TK_CUDA(cudaMemsetAsync(nrefine, 0, 16, st));
+    const size_t smem = sizeof(JacobiSmem<M, float>) * 4;
+    TK_CUDA(cudaFuncSetAttribute(k_ltsa<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = (int)std::min<int64_t>((N + 3) / 4, (int64_t)ctx->num_sms * 16);
+    k_ltsa<M><<<grid, 128, smem, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine);
+    TK_CHECK_LAUNCH();
+    const size_t smem64 = sizeof(JacobiSmem<M, double>);
+    TK_CUDA(cudaFuncSetAttribute(k_ltsa_fp64<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem64));
+    k_ltsa_fp64<M><<<ctx->num_sms * 4, 32, smem64, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine);
+    TK_CHECK_LAUNCH();
+}
+
+} // namespace
+
+void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+                int td, double* V)
+{
+    if (td < 1 || td > 8 || td >= k)
+        throw Error(TK_ERR_INVALID_ARG, "LTSA needs 1 <= target_dimension <= 8 and target_dimension < k");
+    if (k <= 16)
+        launch<16>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
+    else if (k <= 32)
+        launch<32>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
+    else
+        throw Error(TK_ERR_UNSUPPORTED, "LTSA bases support up to 32 neighbours");
+}
+
+} // namespace tk

@@ -1,0 +1,505 @@
+// prep.cu -- lays the point cloud out for distance screening.
+//
+// Steps (all on the context stream, no host synchronisation):
+//   1. column mean mu (FP64, deterministic two-level reduction);
+//   2. a 16-dimensional random sketch s_i = G^T (x_i - mu) of every point, its
+//      16x16 covariance (deterministic per-warp partials) and R = max |x_i - mu|;
+//   3. the 3 leading principal directions of the sketch (subspace iteration on
+//      one warp) and the 3-D projection of every point;
+//   4. a Morton-bucket counting sort of the projections, giving perm
+//      (sorted position -> original index): points close in space get close
+//      positions, so a query block finds its neighbours in the first candidate
+//      tiles it visits and its top-K threshold tightens immediately;
+//   5. the screening layout in sorted order: centred FP32 rows xc (Dp-padded),
+//      their squared norms, fp16 hi/lo splits of 2^s * xc for the tensor screen,
+//      and the exact FP64 kernel diagonal k(i,i) (original order) for the re-rank.
+// The ordering only affects speed: the re-rank and certification make the
+// final neighbour sets independent of it.
+#include <cuda_fp16.h>
+
+#include <cfloat>
+#include <cmath>
+
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+constexpr int SKETCH = 16;
+
+__device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
+{
+    return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// order-preserving float <-> uint encoding for atomic min/max
+__device__ __forceinline__ unsigned f2ord(float f)
+{
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// 1. column sums: block b sums rows [b*rpb, (b+1)*rpb) for all columns.
+__global__ void k_colsum_partial(const void* X, int dtype, int64_t N, int D, int64_t ldx, int64_t rpb,
+                                 double* partial)
+{
+    __shared__ double red[4][64];
+    const int lane64 = threadIdx.x & 63, grp = threadIdx.x >> 6;  // 4 row groups of 64 columns
+    const int64_t r0 = (int64_t)blockIdx.x * rpb;
+    const int64_t r1 = min(N, r0 + rpb);
+    for (int c0 = 0; c0 < D; c0 += 64)
+    {
+        const int c = c0 + lane64;
+        double s = 0.0;
+        if (c < D)
+            for (int64_t r = r0 + grp; r < r1; r += 4)
+                s += ldx_elem(X, dtype, r * ldx + c);
+        red[grp][lane64] = s;
+        __syncthreads();
+        if (grp == 0 && c < D)
+            partial[(int64_t)blockIdx.x * D + c] = ((red[0][lane64] + red[1][lane64]) + red[2][lane64]) + red[3][lane64];
+        __syncthreads();
+    }
+}
+
+__global__ void k_colsum_final(const double* partial, int nblk, int D, int64_t N, double* mean)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < D; c += gridDim.x * blockDim.x)
+    {
+        double s = 0.0;
+        for (int b = 0; b < nblk; ++b)
+            s += partial[(int64_t)b * D + c];
+        mean[c] = s / (double)N;
+    }
+}
+
+// deterministic pseudo-random sketch matrix entry in [-1, 1)
+__device__ __forceinline__ float sketch_g(int d, int j)
+{
+    unsigned h = (unsigned)d * 0x9E3779B1u ^ ((unsigned)j * 0x85EBCA77u + 0x27d4eb2fu);
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return (float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f;
+}
+
+__global__ void k_gen_sketch(int D, float* G)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < D * SKETCH; t += gridDim.x * blockDim.x)
+        G[t] = sketch_g(t / SKETCH, t % SKETCH);
+}
+
+// 2. sketch covariance partials per warp + R = max |x - mu|.
+__global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx, const double* mean,
+                         const float* G, double* cov_partial /* nwarps x 136 */, unsigned* rmax_ord)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    // upper-triangle pairs (a<=b) of the 16x16 covariance owned by this lane: p = lane + 32 m
+    int pa[5], pb[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+    {
+        int p = lane + 32 * m, a = 0;
+        if (p >= 136)
+            p = 0;
+        while (p >= SKETCH - a)
+        {
+            p -= SKETCH - a;
+            ++a;
+        }
+        pa[m] = a;
+        pb[m] = a + p;
+    }
+    double acc[5] = {0, 0, 0, 0, 0};
+    float rloc = 0.f;
+    for (int64_t i = warp; i < N; i += nwarps)
+    {
+        float s[SKETCH];
+#pragma unroll
+        for (int j = 0; j < SKETCH; ++j)
+            s[j] = 0.f;
+        double r2 = 0.0;
+        for (int d = lane; d < D; d += 32)
+        {
+            const double v = ldx_elem(X, dtype, i * ldx + d) - mean[d];
+            r2 += v * v;
+            const float vf = (float)v;
+            const float4* g = reinterpret_cast<const float4*>(G + (size_t)d * SKETCH);
+#pragma unroll
+            for (int q = 0; q < SKETCH / 4; ++q)
+            {
+                const float4 gq = g[q];
+                s[4 * q + 0] = fmaf(gq.x, vf, s[4 * q + 0]);
+                s[4 * q + 1] = fmaf(gq.y, vf, s[4 * q + 1]);
+                s[4 * q + 2] = fmaf(gq.z, vf, s[4 * q + 2]);
+                s[4 * q + 3] = fmaf(gq.w, vf, s[4 * q + 3]);
+            }
+        }
+        r2 = warp_sum_d(r2);
+        rloc = fmaxf(rloc, (float)sqrt(r2));
+#pragma unroll
+        for (int j = 0; j < SKETCH; ++j)
+            s[j] = warp_sum_f(s[j]);
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+        {
+            float sa = 0.f, sb = 0.f;
+#pragma unroll
+            for (int j = 0; j < SKETCH; ++j)
+            {
+                sa = (j == pa[m]) ? s[j] : sa;
+                sb = (j == pb[m]) ? s[j] : sb;
+            }
+            acc[m] += (double)sa * (double)sb;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+    {
+        const int p = lane + 32 * m;
+        if (p < 136)
+            cov_partial[warp * 136 + p] = acc[m];
+    }
+    if (rloc > 0.f)
+        atomicMax(rmax_ord, f2ord(rloc));
+}
+
+// 3. top-3 principal directions of the 16x16 sketch covariance by subspace
+// iteration (one warp), then H = G V3 (D x 3) for the projection.
+__global__ void k_pca3(const double* cov_partial, int64_t nwarps, int D, float* H, const unsigned* rmax_ord,
+                       float* rmax)
+{
+    __shared__ double C[SKETCH][SKETCH];
+    __shared__ double V[SKETCH][3];
+    __shared__ double T[SKETCH][3];
+    const int t = threadIdx.x;
+    for (int p = t; p < 136; p += blockDim.x)
+    {
+        double s = 0.0;
+        for (int64_t w = 0; w < nwarps; ++w)
+            s += cov_partial[w * 136 + p];
+        int a = 0, rem = p;
+        while (rem >= SKETCH - a)
+        {
+            rem -= SKETCH - a;
+            ++a;
+        }
+        C[a][a + rem] = s;
+        C[a + rem][a] = s;
+    }
+    if (t < SKETCH)
+        for (int c = 0; c < 3; ++c)
+            V[t][c] = (t % 3 == c) ? 1.0 : 0.01 * (t + 1) * (c + 1);
+    __syncthreads();
+    for (int it = 0; it < 60; ++it)
+    {
+        if (t < SKETCH)
+            for (int c = 0; c < 3; ++c)
+            {
+                double s = 0.0;
+                for (int j = 0; j < SKETCH; ++j)
+                    s += C[t][j] * V[j][c];
+                T[t][c] = s;
+            }
+        __syncthreads();
+        if (t == 0)
+        {
+            // modified Gram-Schmidt on the 3 columns of T
+            for (int c = 0; c < 3; ++c)
+            {
+                for (int p = 0; p < c; ++p)
+                {
+                    double dot = 0.0;
+                    for (int j = 0; j < SKETCH; ++j)
+                        dot += T[j][c] * T[j][p];
+                    for (int j = 0; j < SKETCH; ++j)
+                        T[j][c] -= dot * T[j][p];
+                }
+                double nrm = 0.0;
+                for (int j = 0; j < SKETCH; ++j)
+                    nrm += T[j][c] * T[j][c];
+                nrm = sqrt(nrm);
+                for (int j = 0; j < SKETCH; ++j)
+                    V[j][c] = nrm > 0.0 ? T[j][c] / nrm : (j == c ? 1.0 : 0.0);
+            }
+        }
+        __syncthreads();
+    }
+    for (int d = t; d < D; d += blockDim.x)
+        for (int c = 0; c < 3; ++c)
+        {
+            float s = 0.f;
+            for (int j = 0; j < SKETCH; ++j)
+                s = fmaf(sketch_g(d, j), (float)V[j][c], s);
+            H[d * 3 + c] = s;
+        }
+    if (t == 0)
+        *rmax = (*rmax_ord == 0u) ? 0.f : ord2f(*rmax_ord);
+}
+
+// projection p_i = H^T (x_i - mu) and its bounding box
+__global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ldx, const double* mean,
+                          const float* H, float* proj, unsigned* bbox /* 6: min x3, max x3 */)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int64_t i = warp; i < N; i += nwarps)
+    {
+        float p[3] = {0.f, 0.f, 0.f};
+        for (int d = lane; d < D; d += 32)
+        {
+            const float v = (float)(ldx_elem(X, dtype, i * ldx + d) - mean[d]);
+            p[0] = fmaf(H[d * 3 + 0], v, p[0]);
+            p[1] = fmaf(H[d * 3 + 1], v, p[1]);
+            p[2] = fmaf(H[d * 3 + 2], v, p[2]);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+        {
+            p[c] = warp_sum_f(p[c]);
+            mn[c] = fminf(mn[c], p[c]);
+            mx[c] = fmaxf(mx[c], p[c]);
+        }
+        if (lane < 3)
+            proj[i * 3 + lane] = lane == 0 ? p[0] : (lane == 1 ? p[1] : p[2]);
+    }
+    if (lane == 0 && mn[0] <= mx[0])
+        for (int c = 0; c < 3; ++c)
+        {
+            atomicMin(&bbox[c], f2ord(mn[c]));
+            atomicMax(&bbox[3 + c], f2ord(mx[c]));
+        }
+}
+
+__device__ __forceinline__ unsigned spread3(unsigned v)  // 10 bits -> every third bit
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void k_codes(const float* proj, int64_t N, const unsigned* bbox, int shift, unsigned* bucket,
+                        unsigned* hist)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        unsigned q[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+        {
+            const float lo = ord2f(bbox[c]), hi = ord2f(bbox[3 + c]);
+            const float span = hi - lo;
+            float t = span > 0.f ? (proj[i * 3 + c] - lo) / span : 0.f;
+            t = fminf(fmaxf(t, 0.f), 1.f);
+            q[c] = min(1023u, (unsigned)(t * 1024.f));
+        }
+        const unsigned code = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
+        const unsigned b = code >> shift;
+        bucket[i] = b;
+        atomicAdd(&hist[b], 1u);
+    }
+}
+
+// exclusive scan of nb counters by one block of 1024 threads
+__global__ void k_scan(unsigned* hist, int nb)
+{
+    __shared__ unsigned part[1024];
+    const int t = threadIdx.x;
+    const int per = (nb + 1023) / 1024;
+    const int b0 = t * per, b1 = min(nb, b0 + per);
+    unsigned s = 0;
+    for (int b = b0; b < b1; ++b)
+        s += hist[b];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        unsigned v = (t >= o) ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    unsigned run = part[t] - s;
+    for (int b = b0; b < b1; ++b)
+    {
+        const unsigned c = hist[b];
+        hist[b] = run;
+        run += c;
+    }
+}
+
+__global__ void k_scatter(const unsigned* bucket, int64_t N, unsigned* offs, int32_t* perm)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const unsigned pos = atomicAdd(&offs[bucket[i]], 1u);
+        perm[pos] = (int32_t)i;
+    }
+}
+
+// 5. screening layout in sorted order (one warp per row).
+__global__ void k_layout(const void* X, int dtype, int64_t N, int64_t Npad, int D, int Dp, int64_t ldx,
+                         const double* mean, const int32_t* perm, const float* rmax, float* xc, float* nrm,
+                         __half* xh, __half* xl, double* kdiag, float* scale_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    // xh/xl hold xc * 2^s with R * 2^s < 2^14 (fp16 max is 65504)
+    int e = 0;
+    const float R = *rmax;
+    frexpf(R > 0.f ? R : 1.f, &e);
+    const int s = 14 - e;
+    const float scale = ldexpf(1.f, s);
+    if (warp == 0 && lane == 0 && scale_out)
+        *scale_out = (float)s;
+    for (int64_t p = warp; p < Npad; p += nwarps)
+    {
+        const bool valid = p < N;
+        const int64_t i = valid ? perm[p] : 0;
+        double n2 = 0.0, k2 = 0.0;
+        for (int d = lane; d < Dp; d += 32)
+        {
+            float v = 0.f;
+            if (valid && d < D)
+            {
+                const double x = ldx_elem(X, dtype, i * ldx + d);
+                k2 += x * x;
+                v = (float)(x - mean[d]);
+                n2 += (double)v * (double)v;
+            }
+            xc[p * Dp + d] = v;
+            if (xh)
+            {
+                const float vs = v * scale;
+                const __half h = __float2half_rn(vs);
+                const __half l = __float2half_rn(vs - __half2float(h));
+                xh[p * Dp + d] = h;
+                xl[p * Dp + d] = l;
+            }
+        }
+        n2 = warp_sum_d(n2);
+        k2 = warp_sum_d(k2);
+        if (lane == 0)
+        {
+            nrm[p] = valid ? (float)n2 : __int_as_float(0x7f800000);
+            if (valid)
+                kdiag[i] = k2;
+        }
+    }
+}
+
+} // namespace
+
+void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, bool tensor,
+                    Prepared& P)
+{
+    cudaStream_t st = ctx->stream;
+    P.N = N;
+    P.D = D;
+    P.Dp = ((D + 63) / 64) * 64;
+    P.Npad = ((N + 255) / 256) * 256;
+    const int sms = ctx->num_sms;
+
+    // 1. mean
+    const int nblk = (int)std::min<int64_t>(4 * sms, std::max<int64_t>(1, (N + 63) / 64));
+    const int64_t rpb = (N + nblk - 1) / nblk;
+    double* partial = (double*)ctx->scratch.get("prep.partial", sizeof(double) * (size_t)nblk * D);
+    double* mean = (double*)ctx->scratch.get("prep.mean", sizeof(double) * D);
+    k_colsum_partial<<<nblk, 256, 0, st>>>(X, dtype, N, D, ldx, rpb, partial);
+    TK_CHECK_LAUNCH();
+    k_colsum_final<<<(D + 255) / 256, 256, 0, st>>>(partial, nblk, D, N, mean);
+    TK_CHECK_LAUNCH();
+
+    // 2. sketch covariance and R
+    const int sk_blocks = 2 * sms;
+    const int64_t sk_warps = (int64_t)sk_blocks * 8;
+    double* covp = (double*)ctx->scratch.get("prep.covp", sizeof(double) * sk_warps * 136);
+    unsigned* small = (unsigned*)ctx->scratch.get("prep.small", 64 * sizeof(unsigned));
+    // small[0] = rmax ord, small[8..13] = bbox
+    float* rmax = (float*)ctx->scratch.get("prep.rmax", 2 * sizeof(float));
+    unsigned init[16];
+    for (int c = 0; c < 16; ++c)
+        init[c] = 0u;
+    init[8] = init[9] = init[10] = 0xffffffffu;  // bbox min (ordered encoding)
+    TK_CUDA(cudaMemcpyAsync(small, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    float* G = (float*)ctx->scratch.get("prep.G", sizeof(float) * SKETCH * (size_t)D);
+    k_gen_sketch<<<(D * SKETCH + 255) / 256, 256, 0, st>>>(D, G);
+    TK_CHECK_LAUNCH();
+    k_sketch<<<sk_blocks, 256, 0, st>>>(X, dtype, N, D, ldx, mean, G, covp, small);
+    TK_CHECK_LAUNCH();
+
+    // 3. principal directions and projection
+    float* H = (float*)ctx->scratch.get("prep.H", sizeof(float) * 3 * (size_t)D);
+    k_pca3<<<1, 256, 0, st>>>(covp, sk_warps, D, H, small, rmax);
+    TK_CHECK_LAUNCH();
+    float* proj = (float*)ctx->scratch.get("prep.proj", sizeof(float) * 3 * (size_t)N);
+    k_project<<<2 * sms, 256, 0, st>>>(X, dtype, N, D, ldx, mean, H, proj, small + 8);
+    TK_CHECK_LAUNCH();
+
+    // 4. Morton-bucket counting sort (about one point per bucket)
+    int bits = 10;
+    while (bits < 24 && ((int64_t)1 << bits) < N)
+        ++bits;
+    const int nb = 1 << bits;
+    const int shift = 30 - bits;
+    unsigned* bucket = (unsigned*)ctx->scratch.get("prep.bucket", sizeof(unsigned) * (size_t)N);
+    unsigned* hist = (unsigned*)ctx->scratch.get("prep.hist", sizeof(unsigned) * (size_t)nb);
+    TK_CUDA(cudaMemsetAsync(hist, 0, sizeof(unsigned) * (size_t)nb, st));
+    k_codes<<<2 * sms, 256, 0, st>>>(proj, N, small + 8, shift, bucket, hist);
+    TK_CHECK_LAUNCH();
+    k_scan<<<1, 1024, 0, st>>>(hist, nb);
+    TK_CHECK_LAUNCH();
+    P.perm = (int32_t*)ctx->scratch.get("prep.perm", sizeof(int32_t) * (size_t)N);
+    k_scatter<<<2 * sms, 256, 0, st>>>(bucket, N, hist, P.perm);
+    TK_CHECK_LAUNCH();
+
+    // 5. layout
+    P.xc = (float*)ctx->scratch.get("prep.xc", sizeof(float) * (size_t)P.Npad * P.Dp);
+    P.nrm = (float*)ctx->scratch.get("prep.nrm", sizeof(float) * (size_t)P.Npad);
+    P.kdiag = (double*)ctx->scratch.get("prep.kdiag", sizeof(double) * (size_t)N);
+    if (tensor)
+    {
+        P.xh = (uint16_t*)ctx->scratch.get("prep.xh", sizeof(uint16_t) * (size_t)P.Npad * P.Dp);
+        P.xl = (uint16_t*)ctx->scratch.get("prep.xl", sizeof(uint16_t) * (size_t)P.Npad * P.Dp);
+    }
+    else
+    {
+        P.xh = P.xl = nullptr;
+    }
+    P.rmax = rmax;
+    k_layout<<<4 * sms, 256, 0, st>>>(X, dtype, N, P.Npad, D, P.Dp, ldx, mean, P.perm, rmax, P.xc, P.nrm,
+                                      (__half*)P.xh, (__half*)P.xl, P.kdiag, rmax + 1);
+    TK_CHECK_LAUNCH();
+}
+
+} // namespace tk

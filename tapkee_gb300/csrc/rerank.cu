@@ -1,0 +1,269 @@
+// rerank.cu -- exact FP64 re-rank of screened candidates, certification, and the
+// exact fallback for rows the screen cannot certify.
+//
+// Distances are the reference's kernel-trick form (neighbors/neighbors.hpp:49-52)
+//   d2(i,j) = k(i,i) - 2 k(i,j) + k(j,j),  k = FP64 dot of the input rows
+// (squared: sqrt is monotone and the ranking is what is returned). The k
+// nearest other points are taken in (d2, index) order.
+//
+// Certification. The screen returns, per query, the KC candidates with the
+// smallest approximate values a_j and their largest value T. With the error
+// model |a_j - d2_j| <= eps = c1 (|x|^2 + R^2) + c2 |x| R (R = max |x - mean|,
+// see screen_error_model), every point outside the list has d2 >= T - eps. If
+// the exact k-th smallest d2 among the candidates, e_k, satisfies e_k < T - eps,
+// no outside point can enter the top k and the row is exact. Otherwise the row
+// goes to the fallback, which scans all N points with an FP32 direct-difference
+// filter (relative error <= (D + 4) 2^-23) against e_k, then ranks the few
+// survivors in FP64.
+#include <cfloat>
+#include <cmath>
+
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+constexpr int FB_CAP = 4096;  // fallback survivors per row
+
+__device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
+{
+    return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
+}
+
+__device__ __forceinline__ double kdot(const void* X, int dtype, int64_t ldx, int D, int64_t a, int64_t b)
+{
+    double s = 0.0;
+    if (dtype == TK_F64)
+    {
+        const double* xa = reinterpret_cast<const double*>(X) + a * ldx;
+        const double* xb = reinterpret_cast<const double*>(X) + b * ldx;
+        for (int d = 0; d < D; ++d)
+            s = fma(xa[d], xb[d], s);
+    }
+    else
+    {
+        const float* xa = reinterpret_cast<const float*>(X) + a * ldx;
+        const float* xb = reinterpret_cast<const float*>(X) + b * ldx;
+        for (int d = 0; d < D; ++d)
+            s = fma((double)xa[d], (double)xb[d], s);
+    }
+    return s;
+}
+
+__device__ __forceinline__ bool key_less(double da, int ja, double db, int jb)
+{
+    return da < db || (da == db && ja < jb);
+}
+
+// One warp per query position p (sorted order). Lanes own candidates
+// l, l+32 (KC <= 64).
+template <int KC>
+__global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k, const int32_t* perm,
+                         const double* kdiag, const float* nrm, const float* rmax, const int32_t* cand_idx,
+                         const float* cand_val, float c1, float c2, int32_t* idx_out, double* d2_out,
+                         int32_t* failed, double* failed_ub, unsigned* nfailed)
+{
+    constexpr int PER = (KC + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const double R = (double)*rmax;
+    for (int64_t p = warp; p < N; p += nwarps)
+    {
+        const int64_t i = perm[p];
+        const double kii = kdiag[i];
+        double d[PER];
+        int j[PER];
+#pragma unroll
+        for (int s = 0; s < PER; ++s)
+        {
+            const int slot = lane + 32 * s;
+            d[s] = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+            j[s] = 0x7fffffff - slot;                          // distinct, ranks last
+            if (slot < KC)
+            {
+                const int c = cand_idx[p * KC + slot];
+                if (c >= 0 && c < N)
+                {
+                    const int64_t jj = perm[c];
+                    if (jj != i)
+                    {
+                        d[s] = kii - 2.0 * kdot(X, dtype, ldx, D, i, jj) + kdiag[jj];
+                        j[s] = (int)jj;
+                    }
+                }
+            }
+        }
+        // rank of every element among the KC (d, j) keys
+        int rank[PER];
+#pragma unroll
+        for (int s = 0; s < PER; ++s)
+            rank[s] = 0;
+#pragma unroll
+        for (int so = 0; so < PER; ++so)
+            for (int m = 0; m < 32; ++m)
+            {
+                const double dm = __shfl_sync(0xffffffffu, d[so], m);
+                const int jm = __shfl_sync(0xffffffffu, j[so], m);
+#pragma unroll
+                for (int s = 0; s < PER; ++s)
+                    rank[s] += key_less(dm, jm, d[s], j[s]) ? 1 : 0;
+            }
+        // e_k = value of rank k-1
+        double ek = -1.0;
+#pragma unroll
+        for (int s = 0; s < PER; ++s)
+            if (rank[s] == k - 1)
+                ek = d[s];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            ek = fmax(ek, __shfl_xor_sync(0xffffffffu, ek, o));
+        const float T = cand_val[p * KC + KC - 1];
+        const double nx = (double)nrm[p];
+        const double eps = (double)c1 * (nx + R * R) + (double)c2 * sqrt(nx) * R;
+        const bool full = T < FLT_MAX;  // list not full: every point was kept
+        const bool certified = !full || (ek < (double)T - eps);
+        if (certified)
+        {
+#pragma unroll
+            for (int s = 0; s < PER; ++s)
+                if (rank[s] < k)
+                {
+                    idx_out[i * k + rank[s]] = j[s];
+                    if (d2_out)
+                        d2_out[i * k + rank[s]] = d[s];
+                }
+        }
+        else if (lane == 0)
+        {
+            const unsigned f = atomicAdd(nfailed, 1u);
+            failed[f] = (int32_t)p;
+            failed_ub[f] = ek;
+        }
+    }
+}
+
+// Exact fallback: one CTA per failed row (persistent over the failed list).
+__global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k,
+                                                  const int32_t* perm, const double* kdiag, const int32_t* failed,
+                                                  const double* failed_ub, const unsigned* nfailed,
+                                                  int32_t* idx_out, double* d2_out, unsigned* err)
+{
+    __shared__ int32_t sj[FB_CAP];
+    __shared__ double sd[FB_CAP];
+    __shared__ unsigned cnt;
+    __shared__ float xq[1024];
+    const unsigned nf = *nfailed;
+    for (unsigned f = blockIdx.x; f < nf; f += gridDim.x)
+    {
+        const int64_t p = failed[f];
+        const int64_t i = perm[p];
+        const double ub = failed_ub[f];
+        const double kii = kdiag[i];
+        // FP32 direct-difference filter with a relative slack covering its error
+        const double slack = (double)(D + 8) * 1.1920928955078125e-07;
+        const float thr = (float)(ub * (1.0 + slack) + 4.0 * 2.220446049250313e-16 * (kii + 1.0) * 16.0) * 1.0000005f;
+        if (threadIdx.x == 0)
+            cnt = 0;
+        __syncthreads();
+        for (int64_t jj = threadIdx.x; jj < N; jj += blockDim.x)
+        {
+            if (jj == i)
+                continue;
+            float acc = 0.f;
+            for (int d0 = 0; d0 < D; d0 += 1024)
+            {
+                // D > 1024 is handled in chunks without caching the query
+                for (int d = d0; d < min(D, d0 + 1024); ++d)
+                {
+                    const float v = (float)(ldx_elem(X, dtype, jj * ldx + d) - ldx_elem(X, dtype, i * ldx + d));
+                    acc = fmaf(v, v, acc);
+                }
+            }
+            if (acc <= thr)
+            {
+                const unsigned s = atomicAdd(&cnt, 1u);
+                if (s < FB_CAP)
+                    sj[s] = (int32_t)jj;
+                else
+                    atomicOr(err, DEV_ERR_OVERFLOW);
+            }
+        }
+        __syncthreads();
+        const unsigned n = min(cnt, (unsigned)FB_CAP);
+        for (unsigned t = threadIdx.x; t < n; t += blockDim.x)
+            sd[t] = kii - 2.0 * kdot(X, dtype, ldx, D, i, sj[t]) + kdiag[sj[t]];
+        __syncthreads();
+        if (n < (unsigned)k && threadIdx.x == 0)
+            atomicOr(err, DEV_ERR_BOUNDS);
+        for (unsigned t = threadIdx.x; t < n; t += blockDim.x)
+        {
+            unsigned r = 0;
+            for (unsigned m = 0; m < n; ++m)
+                r += key_less(sd[m], sj[m], sd[t], sj[t]) ? 1u : 0u;
+            if (r < (unsigned)k)
+            {
+                idx_out[i * k + r] = sj[t];
+                if (d2_out)
+                    d2_out[i * k + r] = sd[t];
+            }
+        }
+        __syncthreads();
+    }
+    (void)xq;
+}
+
+} // namespace
+
+void screen_error_model(int screen, int Dp, float* c1, float* c2)
+{
+    const double u = 5.9604644775390625e-08;  // 2^-24
+    // c1 covers rounding of the centred coordinates and of the FP32 norms and
+    // the final a = |x|^2 + |y|^2 - 2 x.y evaluation.
+    *c1 = (float)(16.0 * u);
+    if (screen == TK_SCREEN_FP32)
+    {
+        // sequential FP32 FMA accumulation of Dp products: |err| <= Dp u sum|x_d y_d| <= Dp u |x||y|
+        *c2 = (float)(2.0 * (Dp + 4) * u * 2.0);
+    }
+    else
+    {
+        // fp16 split x = h + l (|l| <= 2^-11 |x|, l rounded to 2^-22 |x|), dropped l*l
+        // term (<= 2^-22 |x||y|), and FP32 tensor-core accumulation of 3 Dp / 16
+        // K-steps, each assumed to add at most 2 ulp (truncating adds), plus the
+        // intra-instruction sum (8 ulp): all relative to |x||y|.
+        const double split = 3.0 * 2.384185791015625e-07;          // 3 * 2^-22
+        const double accum = (3.0 * Dp / 16.0 * 2.0 + 8.0) * 2.0 * u;  // ulp = 2^-23
+        *c2 = (float)(2.0 * (split + accum) * 2.0);
+    }
+}
+
+int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t ldx, int k, int kc,
+               const int32_t* cand_idx, const float* cand_val, float eps_c1, float eps_c2, int32_t* idx_out,
+               double* d2_out)
+{
+    cudaStream_t st = ctx->stream;
+    const int64_t N = P.N;
+    int32_t* failed = (int32_t*)ctx->scratch.get("rerank.failed", sizeof(int32_t) * (size_t)N);
+    double* failed_ub = (double*)ctx->scratch.get("rerank.failed_ub", sizeof(double) * (size_t)N);
+    unsigned* nfailed = (unsigned*)ctx->scratch.get("rerank.nfailed", 16);
+    TK_CUDA(cudaMemsetAsync(nfailed, 0, 16, st));
+    const int blocks = 8 * ctx->num_sms;
+    if (kc == 32)
+        k_rerank<32><<<blocks, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, P.nrm, P.rmax, cand_idx,
+                                             cand_val, eps_c1, eps_c2, idx_out, d2_out, failed, failed_ub, nfailed);
+    else if (kc == 64)
+        k_rerank<64><<<blocks, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, P.nrm, P.rmax, cand_idx,
+                                             cand_val, eps_c1, eps_c2, idx_out, d2_out, failed, failed_ub, nfailed);
+    else
+        throw Error(TK_ERR_INTERNAL, "rerank: unsupported candidate count");
+    TK_CHECK_LAUNCH();
+    k_fallback<<<ctx->num_sms, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, failed, failed_ub, nfailed,
+                                             idx_out, d2_out, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, nfailed, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    TK_CUDA(cudaStreamSynchronize(st));
+    return (int64_t) * reinterpret_cast<unsigned*>(ctx->host_i64);
+}
+
+} // namespace tk

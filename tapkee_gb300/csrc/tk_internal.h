@@ -1,0 +1,138 @@
+// tk_internal.h -- shared declarations of the GB300 local-neighborhood operator.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+
+#include "../../include/tapkee_gb300.h"
+
+namespace tk {
+
+// Internal error carrying a tk_status; converted to a return code at the C ABI.
+struct Error : public std::runtime_error
+{
+    int status;
+    Error(int s, const std::string& msg) : std::runtime_error(msg), status(s) {}
+};
+
+#define TK_CUDA(call)                                                                                        \
+    do                                                                                                       \
+    {                                                                                                        \
+        cudaError_t err__ = (call);                                                                          \
+        if (err__ != cudaSuccess)                                                                            \
+        {                                                                                                    \
+            if (err__ == cudaErrorMemoryAllocation)                                                          \
+                throw ::tk::Error(TK_ERR_OOM, std::string("out of device memory at ") + #call);             \
+            throw ::tk::Error(TK_ERR_CUDA, std::string(cudaGetErrorString(err__)) + " at " + __FILE__ + ":" + \
+                                               std::to_string(__LINE__));                                   \
+        }                                                                                                    \
+    } while (0)
+
+#define TK_CHECK_LAUNCH() TK_CUDA(cudaGetLastError())
+
+// Device-side error word bits (written by kernels instead of trapping).
+enum : unsigned
+{
+    DEV_ERR_TIMEOUT = 1u,       // a bounded spin-wait gave up
+    DEV_ERR_OVERFLOW = 2u,      // a bounded buffer overflowed
+    DEV_ERR_BOUNDS = 4u,        // an index check failed
+    DEV_ERR_NONFINITE = 8u      // non-finite input where finite is required
+};
+
+// Grow-only named scratch arena of a context.
+struct Scratch
+{
+    struct Buf
+    {
+        void* ptr = nullptr;
+        size_t bytes = 0;
+    };
+    std::unordered_map<std::string, Buf> bufs;
+    void* get(const std::string& name, size_t bytes);
+    void release_all();
+};
+
+// Layout of the prepared (screening) copy of the point cloud.
+struct Prepared
+{
+    int64_t N = 0;      // points
+    int64_t Npad = 0;   // rows padded to the screening tile (multiple of 256)
+    int D = 0;          // input dimension
+    int Dp = 0;         // padded dimension (multiple of 64)
+    float* xc = nullptr;        // Npad x Dp centred FP32 coordinates, sorted order
+    float* nrm = nullptr;       // Npad squared norms of xc (+inf for padding rows)
+    uint16_t* xh = nullptr;     // Npad x Dp fp16 high parts of scale*xc (tensor screen)
+    uint16_t* xl = nullptr;     // Npad x Dp fp16 low parts
+    int32_t* perm = nullptr;    // sorted position -> original index
+    double* kdiag = nullptr;    // N exact k(i,i) in FP64, original order
+    float* rmax = nullptr;      // device scalar: max |xc|
+    float scale_log2 = 0.f;     // xh/xl hold xc * 2^scale_log2
+};
+
+} // namespace tk
+
+struct tk_ctx
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string last_error;
+    tk_log_fn log_fn = nullptr;
+    void* log_user = nullptr;
+    tk::Scratch scratch;
+    unsigned* dev_err = nullptr;      // device error word
+    unsigned* host_err = nullptr;     // pinned mirror
+    int64_t* host_i64 = nullptr;      // pinned small readback area (16 entries)
+    cudaEvent_t ev[8] = {};
+    int num_sms = 0;
+    // operator held by the context
+    tk_operator_info op{};
+    bool op_valid = false;
+};
+
+namespace tk {
+
+void log(tk_ctx* ctx, int level, const std::string& msg);
+
+// ---- kernel launchers (one translation unit each) -------------------------
+
+// prep.cu: centre, order spatially and lay out the point cloud for screening.
+void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, bool tensor,
+                    Prepared& out);
+
+// knn_simt.cu / knn_tc.cu: screening, K candidates per row (sorted-space indices).
+constexpr int KCAND_MAX = 64;
+void screen_fp32(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
+void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
+bool tensor_screen_supported(int Dp);
+
+// rerank.cu: exact FP64 re-rank, certification and exact fallback.
+// Returns the number of uncertified rows (device -> host read).
+int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t ldx, int k, int kc,
+               const int32_t* cand_idx, const float* cand_val, float eps_c1, float eps_c2, int32_t* idx_out,
+               double* d2_out);
+
+// connectivity.cu
+bool check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx);
+
+// lle.cu
+void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                 int k, double klle_shift, double* W);
+
+// ltsa.cu
+void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                int k, int td, double* V);
+
+// assemble.cu: returns nnz; writes row_ptr/col/vals when non-null (device ptrs).
+int64_t assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                 double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, bool count_only);
+
+// Screening error model (see rerank.cu): |approx - exact| <= c1 (|x|^2 + R^2) + c2 |x| R.
+void screen_error_model(int screen, int Dp, float* c1, float* c2);
+
+} // namespace tk

@@ -1,0 +1,59 @@
+"""CSR assembly of M through the C ABI vs the oracle's setFromTriplets (GPU).
+Given identical W, structure is exact and values agree to 1e-12 relative; two
+runs are bit-identical."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tapkee_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("method", ["lle", "ltsa"])
+def test_assembly_matches_oracle(ctx, golden, method):
+    if method == "lle":
+        X = datasets.swiss_roll(2000, seed=0)
+        idx = golden["lle_idx_oracle_order"]
+        w = oracle.lle_weights(X, idx, 1e-3)
+        m = 0
+    else:
+        X = datasets.lifted_s_curve(1500, d=8, seed=11, noise=0.02, dtype=np.float64)
+        idx = golden["ltsa_idx_oracle_order"]
+        w = golden["ltsa_V"]
+        m = 1
+    rp, col, vals = ctx.assemble(method, idx, w, 1e-9)
+    rr, rc, rv = oracle.assemble(m, idx, w, 1e-9)
+    assert np.array_equal(rp, rr)
+    assert np.array_equal(col, rc)
+    assert np.abs(vals - rv).max() <= 1e-12 * np.abs(rv).max()
+
+
+def test_assembly_is_deterministic_and_symmetric(ctx):
+    X = datasets.lifted_swiss_roll(6000, 64, seed=3)
+    idx, _, _ = oracle.knn_brute(X, 16)
+    W = oracle.lle_weights(X, idx, 1e-3)
+    a = ctx.assemble("lle", idx, W, 1e-9)
+    b = ctx.assemble("lle", idx, W, 1e-9)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    import scipy.sparse as sp
+    M = sp.csr_matrix((a[2], a[1], a[0]), shape=(6000, 6000))
+    assert abs(M - M.T).max() == 0.0
+
+
+def test_hub_rows_use_the_large_table(ctx):
+    # a hub: point 0 is every other point's neighbour -> in-degree N-1
+    rng = np.random.default_rng(0)
+    N, k = 1200, 8
+    idx = np.zeros((N, k), np.int32)
+    for i in range(N):
+        pool = np.setdiff1d(np.arange(N), [i, 0])
+        rest = rng.choice(pool, size=k - 1, replace=False)
+        idx[i] = np.concatenate([[0], rest]) if i != 0 else rng.choice(pool, size=k, replace=False)
+    W = rng.random((N, k))
+    W /= W.sum(1, keepdims=True)
+    rp, col, vals = ctx.assemble("lle", idx, W, 1e-9)
+    rr, rc, rv = oracle.assemble(0, idx, W, 1e-9)
+    assert np.array_equal(rp, rr) and np.array_equal(col, rc)
+    assert np.abs(vals - rv).max() <= 1e-12 * np.abs(rv).max()

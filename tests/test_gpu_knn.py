@@ -1,0 +1,99 @@
+"""Brute kNN through the C ABI vs the CPU oracle (GPU).
+
+Bar: neighbour index sets bit-exact; rows ordered by (FP64 distance, index);
+squared distances equal to FP64 within 1e-12 relative."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tapkee_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+SCREENS = ["tensor", "fp32"]
+
+
+def _ordered(X, idx):
+    X = np.asarray(X, np.float64)
+    d = ((X[idx] - X[:, None, :]) ** 2).sum(-1)
+    order = np.array([np.lexsort((idx[i], d[i])) for i in range(len(idx))])
+    return np.take_along_axis(idx, order, 1), np.take_along_axis(d, order, 1)
+
+
+@pytest.mark.parametrize("screen", SCREENS)
+def test_line_known_answer(ctx, screen):
+    # test/unit/neighbors.cpp:92-127 through the GPU path
+    N, k = 100, 10
+    X = np.arange(N, dtype=np.float32).reshape(N, 1)
+    idx = ctx.knn_brute(X, k, screen=screen)
+    for i in range(N):
+        s = set(idx[i].tolist())
+        assert len(s) == k and i not in s
+        for j in range(min(i, k // 2)):
+            assert i - j - 1 in s
+        for j in range(min(N - i - 1, k // 2)):
+            assert i + j + 1 in s
+
+
+@pytest.mark.parametrize("screen", SCREENS)
+def test_swiss_roll_2000_bit_exact(ctx, golden, screen):
+    X = datasets.swiss_roll(2000, seed=0)
+    idx, d2, st = ctx.knn_brute(X, 12, screen=screen, return_distances=True, return_stats=True)
+    ref = golden["lle_idx"]  # oracle sets ordered by (distance, index)
+    assert np.array_equal(idx, ref)
+    _, dref = _ordered(X, ref)
+    assert np.abs(d2 - dref).max() <= 1e-12 * dref.max()
+
+
+@pytest.mark.parametrize("screen", SCREENS)
+@pytest.mark.parametrize("n,d,k,dtype", [(3000, 64, 16, np.float32), (2500, 32, 20, np.float32),
+                                         (1800, 128, 24, np.float64), (1200, 16, 40, np.float32)])
+def test_lifted_rolls_match_oracle(ctx, screen, n, d, k, dtype):
+    X = datasets.lifted_swiss_roll(n, d, seed=n + d, dtype=dtype)
+    idx = ctx.knn_brute(X, k, screen=screen)
+    ref, _, _ = oracle.knn_brute(X, k)
+    ref_sorted, _ = _ordered(X, ref)
+    assert np.array_equal(idx, ref_sorted)
+
+
+@pytest.mark.parametrize("screen", SCREENS)
+def test_small_and_ragged_sizes(ctx, screen):
+    for n, k in [(2, 1), (3, 2), (33, 5), (257, 31), (300, 56)]:
+        X = np.random.default_rng(n).normal(size=(n, 5)).astype(np.float32)
+        idx = ctx.knn_brute(X, k, screen=screen)
+        ref, _, _ = oracle.knn_brute(X, k)
+        assert np.array_equal(idx, _ordered(X, ref)[0]), (n, k)
+
+
+@pytest.mark.parametrize("screen", SCREENS)
+def test_duplicate_points_tie_break_by_index(ctx, screen):
+    # 40 copies of 5 distinct points: many exact ties; ties resolve by index
+    base = np.random.default_rng(1).normal(size=(5, 3))
+    X = np.repeat(base, 40, axis=0).astype(np.float64)
+    k = 6
+    idx = ctx.knn_brute(X, k, screen=screen)
+    for i in range(len(X)):
+        same = [j for j in range(len(X)) if j != i and (X[j] == X[i]).all()]
+        assert idx[i].tolist() == same[:k]
+
+
+def test_invalid_arguments(ctx):
+    import tapkee_gb300 as tk
+    X = np.zeros((10, 3), np.float32)
+    with pytest.raises(tk.WrongParameterError):
+        ctx.knn_brute(X, 10)
+    with pytest.raises(tk.WrongParameterError):
+        ctx.knn_brute(X, 0)
+    with pytest.raises(tk.NoDataError):
+        ctx.knn_brute(np.zeros((0, 3), np.float32), 1)
+    with pytest.raises(tk.UnsupportedMethodError):
+        ctx.knn_brute(np.random.default_rng(0).normal(size=(100, 3)), 60)
+
+
+def test_device_resident_inputs(ctx):
+    import torch
+    X = datasets.lifted_swiss_roll(2048, 64, seed=9)
+    Xd = torch.from_numpy(X).cuda()
+    idx_d = ctx.knn_brute(Xd, 16)
+    assert idx_d.is_cuda
+    idx_h = ctx.knn_brute(X, 16)
+    assert np.array_equal(idx_d.cpu().numpy(), idx_h)

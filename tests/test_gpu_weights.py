@@ -1,0 +1,48 @@
+"""LLE weights and LTSA bases through the C ABI vs the CPU oracle (GPU).
+Tolerance: 1e-5 relative (max |err| / max |ref|) for W and for P = V V^T."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tapkee_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def test_lle_weights_k_greater_than_d(ctx, golden):
+    # Swiss roll D=3, k=12: rank-deficient Gram, conditioning set by klle_shift
+    X = datasets.swiss_roll(2000, seed=0)
+    idx = golden["lle_idx"]
+    W = ctx.lle_weights(X, idx, 1e-3)
+    ref = oracle.lle_weights(X, idx, 1e-3)
+    assert _rel(W, ref) < TOL
+    assert np.allclose(W.sum(1), 1.0, atol=1e-12)
+
+
+@pytest.mark.parametrize("n,d,k", [(4000, 64, 16), (3000, 128, 24), (2000, 32, 20), (1500, 16, 32), (800, 8, 48)])
+def test_lle_weights_lifted(ctx, n, d, k):
+    X = datasets.lifted_swiss_roll(n, d, seed=n)
+    idx, _, _ = oracle.knn_brute(X, k)
+    W = ctx.lle_weights(X, idx, 1e-3)
+    ref = oracle.lle_weights(X, idx, 1e-3)
+    assert _rel(W, ref) < TOL, _rel(W, ref)
+
+
+def _P(V, k):
+    return np.einsum("nat,nbt->nab", V, V) + 1.0 / k
+
+
+@pytest.mark.parametrize("n,d,k,td", [(1500, 8, 12, 2), (3000, 32, 20, 2), (2000, 16, 10, 3), (1000, 64, 30, 2)])
+def test_ltsa_basis(ctx, n, d, k, td):
+    X = datasets.lifted_s_curve(n, d, seed=n, noise=0.02)
+    idx, _, _ = oracle.knn_brute(X, k)
+    V = ctx.ltsa_basis(X, idx, td)
+    ref = oracle.ltsa_basis(X, idx, td)
+    assert _rel(_P(V, k), _P(ref, k)) < TOL
+    # orthonormal columns
+    assert np.abs(np.einsum("nat,nas->nts", V, V) - np.eye(td)).max() < 1e-5

@@ -1,0 +1,126 @@
+"""CPU oracle pinned against the reference's known-answer test and the
+third-party fixtures (no GPU)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import oracle
+from tapkee_gb300 import datasets
+
+
+def _line_kat(idx, N, k):
+    """Port of test/unit/neighbors.cpp:92-127 (BruteKernelNeighbors) assertions."""
+    for i in range(N):
+        row = list(idx[i])
+        assert len(row) == k
+        s = set(row)
+        assert len(s) == k, "repeated neighbours"
+        assert i not in s, "a point is its own neighbour"
+        k_left = min(i, k // 2)
+        k_right = min(N - i - 1, k // 2)
+        for j in range(k_left):
+            assert i - j - 1 in s
+        for j in range(k_right):
+            assert i + j + 1 in s
+
+
+def test_oracle_line_known_answer():
+    N, k = 100, 10
+    X = np.arange(N, dtype=np.float64).reshape(N, 1)
+    idx, k_used = oracle.find_neighbors(X, k, check_connectivity=True)
+    assert k_used == k
+    _line_kat(idx, N, k)
+
+
+def test_oracle_knn_matches_golden(golden):
+    X = datasets.swiss_roll(2000, seed=0)
+    idx, _, cnt = oracle.knn_brute(X, 12)
+    assert (cnt == 12).all()
+    assert np.array_equal(idx, golden["lle_idx_oracle_order"])
+
+
+def test_oracle_weights_vs_sklearn_fixture(golden):
+    X = datasets.swiss_roll(2000, seed=0)
+    idx = golden["lle_idx_oracle_order"]
+    W = oracle.lle_weights(X, idx, 1e-3)
+    assert np.abs(W - golden["lle_W"]).max() < 1e-12
+    assert np.abs(W - golden["lle_W_sklearn"]).max() / np.abs(W).max() < 1e-9
+    assert np.allclose(W.sum(1), 1.0, atol=1e-12)
+
+
+def test_oracle_assembly_equals_scipy_algebra(golden):
+    X = datasets.swiss_roll(2000, seed=0)
+    idx = golden["lle_idx_oracle_order"]
+    W = golden["lle_W"]
+    N, k = idx.shape
+    rp, col, vals = oracle.assemble(0, idx, W, 1e-9)
+    M = sp.csr_matrix((vals, col, rp), shape=(N, N)).toarray()
+    Wm = sp.csr_matrix((W.ravel(), idx.ravel(), np.arange(0, N * k + 1, k)), shape=(N, N))
+    IW = sp.eye(N) - Wm
+    ref = (IW.T @ IW).toarray() + 1e-9 * np.eye(N)
+    assert np.abs(M - ref).max() < 1e-12
+    assert int(rp[-1]) == int(golden["lle_nnz"])
+    # CSR columns ascending per row; M symmetric
+    for r in range(0, N, 97):
+        c = col[rp[r]:rp[r + 1]]
+        assert np.all(np.diff(c) > 0)
+    assert np.abs(M - M.T).max() == 0.0
+
+
+def _angles(A, B):
+    qa, _ = np.linalg.qr(A)
+    qb, _ = np.linalg.qr(B)
+    s = np.linalg.svd(qa.T @ qb, compute_uv=False)
+    return np.arccos(np.clip(s, -1, 1))
+
+
+def test_oracle_lle_embedding_vs_sklearn_fixture(golden):
+    E = golden["lle_embedding"]
+    assert _angles(E, golden["lle_embedding_sklearn"]).max() < 1e-4
+
+
+def test_oracle_ltsa_vs_sklearn_fixture(golden):
+    Xs = datasets.lifted_s_curve(1500, d=8, seed=11, noise=0.02, dtype=np.float64)
+    idx = golden["ltsa_idx_oracle_order"]
+    V = oracle.ltsa_basis(Xs, idx, 2)
+    P = np.einsum("nat,nbt->nab", V, V)
+    Pg = np.einsum("nat,nbt->nab", golden["ltsa_V"], golden["ltsa_V"])
+    assert np.abs(P - Pg).max() < 1e-10
+    rp, col, vals = oracle.assemble(1, idx, V, 1e-9)
+    assert int(rp[-1]) == int(golden["ltsa_nnz"])
+    assert _angles(golden["ltsa_embedding"], golden["ltsa_embedding_sklearn"]).max() < 1e-4
+
+
+def test_oracle_ltsa_projector_is_orthogonal_projector():
+    Xs = datasets.lifted_s_curve(600, d=6, seed=2, noise=0.01, dtype=np.float64)
+    idx, _, _ = oracle.knn_brute(Xs, 10)
+    V = oracle.ltsa_basis(Xs, idx, 2)
+    G = np.concatenate([np.full((600, 10, 1), 1 / np.sqrt(10)), V], axis=2)
+    GtG = np.einsum("nat,nas->nts", G, G)
+    assert np.abs(GtG - np.eye(3)).max() < 1e-10
+
+
+def test_oracle_connectivity_retry_two_clusters():
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(60, 2))
+    b = rng.normal(size=(60, 2)) + 100.0
+    X = np.concatenate([a, b])
+    idx, _, _ = oracle.knn_brute(X, 5)
+    assert not oracle.is_connected(idx)
+    idx2, k_used = oracle.find_neighbors(X, 5)
+    # 5 -> 10 -> 20 -> 40 -> 80: the first k that reaches across the clusters
+    assert k_used > 5 and oracle.is_connected(idx2)
+
+
+def test_oracle_k_clamped_to_n_minus_one():
+    X = np.arange(8, dtype=np.float64).reshape(8, 1)
+    idx, k_used = oracle.find_neighbors(X, 50)
+    assert k_used == 7 and idx.shape == (8, 7)
+
+
+@pytest.mark.parametrize("n", [2, 3, 17])
+def test_oracle_small_inputs(n):
+    X = np.random.default_rng(n).normal(size=(n, 3))
+    idx, _, cnt = oracle.knn_brute(X, n - 1)
+    for i in range(n):
+        assert set(idx[i]) == set(range(n)) - {i}
