@@ -1,0 +1,329 @@
+"""Benchmark of the local-neighborhood stage (LLE, N=200k, D=64, k=16).
+
+One step = one run of the whole stage on device-resident points: brute kNN
+(distance screen + exact re-rank), connectivity check, LLE weights and CSR
+assembly of M (tk_local_operator). Prints one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+* value        points/s of the tensor-core (tcgen05) screen path, inputs in HBM,
+               L2 flushed between steps (a 512 MB write, outside the timed events)
+* fp32_path    the same stage with the plain FP32 CUDA-core screen, same GPU
+* e2e          the public API with pinned host buffers: X copied in, idx / W /
+               CSR copied out inside the timed region
+* roofline     the tensor screen kernel: algorithmic 2 N^2 D flops per launch over
+               its CUDA-event time, against the measured bf16 peak
+* cpu_baseline the CPU oracle (a port of the reference's FP64 routines) on a
+               bounded sample of query rows, all host threads
+--impl reference times that CPU port alone (the reference itself needs Eigen,
+which is not available to build it).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LLE kNN+weights points/s (N=200k,D=64,k=16): mixed-TC vs plain FP32, same GPU"
+N_DEF, D_DEF, K_DEF = 200_000, 64, 16
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "knn_tc_screen_lle_n200k_d64_k16.md")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per screen launch from the committed ncu summary, if any."""
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline(X, k, sample, threads):
+    """Oracle port: brute kNN of `sample` query rows against all N (the
+    reference's per-query loop) plus their LLE weights; points/s extrapolated."""
+    from oracle import oracle
+    rng = np.random.default_rng(123)
+    rows = np.sort(rng.choice(len(X), size=sample, replace=False)).astype(np.int64)
+    X64 = np.ascontiguousarray(X, dtype=np.float64)
+    t0 = time.perf_counter()
+    idx = oracle.knn_brute_rows(X64, k, rows, nthreads=threads)
+    t1 = time.perf_counter()
+    oracle.lle_weights_rows(X64, rows, idx, 1e-3, nthreads=threads)
+    t2 = time.perf_counter()
+    per_point = (t2 - t0) / len(rows)
+    return {"rows": rows, "idx": idx, "knn_s": t1 - t0, "weights_s": t2 - t1, "value": 1.0 / per_point,
+            "X64": X64}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEF)
+    ap.add_argument("--d", type=int, default=D_DEF)
+    ap.add_argument("--k", type=int, default=K_DEF)
+    ap.add_argument("--fp32-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=2000)
+    ap.add_argument("--no-fp32", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    threads = os.cpu_count() or 1
+
+    from tapkee_gb300 import datasets
+    X = datasets.lifted_swiss_roll(args.n, args.d, seed=1)
+    workload = {"workload": f"LLE lifted Swiss roll N={args.n} D={args.d} k={args.k} float32, klle_shift=1e-3",
+                "n": args.n, "d": args.d, "k": args.k, "method": "KernelLocallyLinearEmbedding",
+                "neighbors_method": "Brute", "l2": "flushed between steps (512 MB write)",
+                "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        # the reference's CPU path (oracle port; the reference needs Eigen to build)
+        if rank != 0:
+            return
+        from oracle import oracle
+        oracle.build()
+        sample = max(200, args.cpu_sample // 2)
+        vals = []
+        for _ in range(args.warmup):
+            cpu_baseline(X, args.k, sample, threads)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            vals.append(cpu_baseline(X, args.k, sample, threads)["value"])
+        el = time.perf_counter() - t0
+        v = statistics.median(vals)
+        line = {"metric": METRIC, "value": v, "unit": "points/s", "impl": "reference", "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded lifted Swiss roll)", "config": workload,
+                "cpu_baseline": {"value": v, "unit": "points/s", "cores": threads, "kind": "port",
+                                 "sample": f"{sample} query rows per step: FP64 brute kNN against all N "
+                                           f"(reference per-query loop, OpenMP over queries) + their LLE weights; "
+                                           f"points/s extrapolated to N"},
+                "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    import tapkee_gb300 as tk
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    ctx = tk.Context(local_rank, stream=stream.cuda_stream)
+    Xd = torch.from_numpy(X).cuda()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    lib = ctx.lib
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def run_steps(screen, steps, warmup, sampler=None):
+        for _ in range(warmup):
+            ctx.local_operator(Xd, "lle", num_neighbors=args.k, klle_shift=1e-3, screen=screen, copy_out=False)
+        barrier()
+        if sampler:
+            sampler.start()
+        l0 = lib.tk_kernel_launch_count()
+        times, infos = [], []
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            info = ctx.local_operator(Xd, "lle", num_neighbors=args.k, klle_shift=1e-3, screen=screen,
+                                      copy_out=False)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            infos.append(info)
+        barrier()
+        launches = lib.tk_kernel_launch_count() - l0
+        clocks = sampler.stop() if sampler else None
+        return times, infos, launches, clocks
+
+    sampler = ClockSampler(local_rank)
+    t_tc, inf_tc, launches, clocks = run_steps("tensor", args.steps, args.warmup, sampler)
+    ms_step = float(np.mean(t_tc))
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_step = float(tt.item())
+    value = world * args.n / (ms_step / 1000.0)
+    info = inf_tc[-1]
+    stage = {"knn": float(np.mean([i.stage_ms[0] for i in inf_tc])),
+             "screen_kernel": float(np.mean([i.stage_ms[5] for i in inf_tc])),
+             "connectivity": float(np.mean([i.stage_ms[1] for i in inf_tc])),
+             "weights": float(np.mean([i.stage_ms[2] for i in inf_tc])),
+             "assembly": float(np.mean([i.stage_ms[3] for i in inf_tc]))}
+
+    # plain FP32 CUDA-core screen, same GPU, same stage
+    fp32 = None
+    if not args.no_fp32:
+        t_f, inf_f, _, _ = run_steps("fp32", args.fp32_steps, 1)
+        ms_f = float(np.mean(t_f))
+        fp32 = {"value": args.n / (ms_f / 1000.0), "unit": "points/s", "ms_per_step": ms_f,
+                "screen_kernel_ms": float(np.mean([i.stage_ms[5] for i in inf_f])),
+                "tc_over_fp32": ms_f / ms_step}
+
+    # end to end through the public API with pinned host buffers
+    Xh = torch.from_numpy(X).pin_memory()
+    nnz = int(info.nnz)
+    kk = int(info.k)
+    out_idx = torch.empty((args.n, kk), dtype=torch.int32).pin_memory()
+    out_w = torch.empty((args.n, kk), dtype=torch.float64).pin_memory()
+    out_rp = torch.empty((args.n + 1,), dtype=torch.int64).pin_memory()
+    out_col = torch.empty((nnz,), dtype=torch.int32).pin_memory()
+    out_val = torch.empty((nnz,), dtype=torch.float64).pin_memory()
+    e2e_t = []
+    for it in range(2 + args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.local_operator(Xh, "lle", num_neighbors=args.k, klle_shift=1e-3, screen="tensor", copy_out=False)
+        ctx._check(lib.tk_operator_copy(ctx.ptr, out_idx.data_ptr(), out_w.data_ptr(), out_rp.data_ptr(),
+                                        out_col.data_ptr(), out_val.data_ptr()))
+        e1.record(stream)
+        e1.synchronize()
+        if it >= 2:
+            e2e_t.append(e0.elapsed_time(e1))
+    e2e_ms = float(np.mean(e2e_t))
+    h2d = args.n * args.d * 4
+    d2h = args.n * kk * 4 + args.n * kk * 8 + (args.n + 1) * 8 + nnz * 12
+
+    # parity on the bench workload: TC vs FP32 neighbour tables, and a sample of
+    # rows against the CPU oracle (also the CPU baseline)
+    pk, pk_src = peaks()
+    flops = 2.0 * args.n * args.n * args.d
+    screen_ms = stage["screen_kernel"]
+    achieved = flops / (screen_ms / 1000.0) / 1e12
+    peak = pk.get("bf16_tflops_sustained", 1700.0)
+    roofline = {"kernel": "k_screen_tc (tcgen05 fp16 split GEMM + fused top-K)", "bound": "tensor",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": f"bf16_tflops_sustained of {pk_src}",
+                "algorithmic": "2*N^2*D flops per launch (the executed fp16 split issues 3x that)",
+                "traffic": profile_traffic()}
+
+    line = {"metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp16x3-split screen / f64 re-rank / f32+ff weights",
+            "data": "synthetic (seeded lifted Swiss roll)", "config": workload, "stage_ms": stage,
+            "rows_uncertified": int(info.rows_uncertified), "nnz": nnz, "k_used": kk,
+            "fp32_path": fp32, "roofline": roofline,
+            "e2e": {"value": args.n / (e2e_ms / 1000.0), "unit": "points/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "clocks": clocks, "gpu_launches": int(launches)}
+
+    if rank == 0:
+        try:
+            from oracle import oracle
+            oracle.build()
+            cb = cpu_baseline(X, args.k, args.cpu_sample, threads)
+            rows = cb["rows"]
+            got = np.empty((args.n, kk), np.int32)
+            got_w = np.empty((args.n, kk), np.float64)
+            ctx._check(lib.tk_operator_copy(ctx.ptr, got.ctypes.data, got_w.ctypes.data, None, None, None))
+            mism = sum(set(a.tolist()) != set(b.tolist()) for a, b in zip(got[rows], cb["idx"]))
+            W_ref = oracle.lle_weights_rows(cb["X64"], rows, got[rows], 1e-3, nthreads=threads)
+            w_err = float(np.abs(got_w[rows] - W_ref).max() / np.abs(W_ref).max())
+            line["cpu_baseline"] = {"value": cb["value"], "unit": "points/s", "cores": threads, "kind": "port",
+                                    "sample": f"{len(rows)} query rows: FP64 brute kNN against all N={args.n} "
+                                              f"(reference per-query loop, OpenMP over queries, "
+                                              f"{cb['knn_s']:.2f} s) + their LLE weights; extrapolated"}
+            line["parity"] = {"rows_checked_vs_oracle": len(rows), "neighbor_set_mismatches": int(mism),
+                              "W_max_rel_err": w_err, "W_tolerance": 1e-5}
+        except Exception as e:  # pragma: no cover
+            line["cpu_baseline"] = {"value": None, "unit": "points/s", "cores": threads, "kind": "port",
+                                    "sample": f"failed: {e}"}
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -118,7 +118,8 @@ typedef struct tk_operator_info
     int64_t nnz;              /* non-zeros of M                                     */
     int64_t rows_uncertified; /* see tk_knn_stats                                   */
     float stage_ms[6];        /* device time per stage: knn, connectivity, weights,
-                                 assembly, total, reserved                           */
+                                 assembly, total, and the distance-screen kernel
+                                 alone (last kNN pass)                               */
 } tk_operator_info;
 
 /* ---- context -------------------------------------------------------------- */
@@ -142,6 +143,10 @@ int tk_set_log_callback(tk_ctx* ctx, tk_log_fn fn, void* user);
 
 /* Library version string ("major.minor.patch"). */
 const char* tk_version(void);
+
+/* Number of CUDA kernels this library has launched in this process (all
+ * contexts); a diagnostic for profiling and benchmarks. */
+long long tk_kernel_launch_count(void);
 
 /* ---- stage entry points ----------------------------------------------------- */
 

@@ -49,6 +49,8 @@ def lib():
         L.oracle_is_connected.restype = i32
         L.oracle_lle_weights.argtypes = [dptr, i64, i64, iptr, i32, ctypes.c_double, dptr, i32]
         L.oracle_lle_weights.restype = i32
+        L.oracle_lle_weights_rows.argtypes = [dptr, i64, i64, iptr, i64, iptr, i32, ctypes.c_double, dptr, i32]
+        L.oracle_lle_weights_rows.restype = i32
         L.oracle_ltsa_basis.argtypes = [dptr, i64, i64, iptr, i32, i32, dptr, dptr, i32]
         L.oracle_ltsa_basis.restype = i32
         L.oracle_assemble.argtypes = [i32, i64, i32, i32, iptr, dptr, ctypes.c_double, dptr, dptr, dptr, i64]
@@ -116,6 +118,19 @@ def lle_weights(X, idx, klle_shift=1e-3, nthreads=None):
     W = np.zeros((N, k), np.float64)
     lib().oracle_lle_weights(X.ctypes.data, N, D, idx.ctypes.data, k, float(klle_shift), W.ctypes.data,
                              _threads(nthreads))
+    return W
+
+
+def lle_weights_rows(X, rows, idx_rows, klle_shift=1e-3, nthreads=None):
+    """LLE weights of the points `rows` (int64) with neighbour rows idx_rows."""
+    X = _X64(X)
+    N, D = X.shape
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    idx_rows = np.ascontiguousarray(idx_rows, dtype=np.int32)
+    k = idx_rows.shape[1]
+    W = np.zeros((len(rows), k), np.float64)
+    lib().oracle_lle_weights_rows(X.ctypes.data, N, D, rows.ctypes.data, len(rows), idx_rows.ctypes.data, k,
+                                  float(klle_shift), W.ctypes.data, _threads(nthreads))
     return W
 
 

@@ -264,6 +264,47 @@ int oracle_lle_weights(const double* X, int64_t N, int64_t D, const int32_t* idx
     return 0;
 }
 
+// LLE weights of a subset of points (rows[r] with neighbours idx_rows[r]); same
+// per-point arithmetic as oracle_lle_weights. Used to time / check a bounded
+// sample of a large problem.
+int oracle_lle_weights_rows(const double* X, int64_t N, int64_t D, const int64_t* rows, int64_t nrows,
+                            const int32_t* idx_rows, int k, double klle_shift, double* W_out, int nthreads)
+{
+    (void)N;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+    {
+        std::vector<double> C(k * k), dots(k), rhs(k, 1.0), w(k);
+#pragma omp for schedule(static)
+        for (int64_t r = 0; r < nrows; ++r)
+        {
+            const int64_t i = rows[r];
+            const int32_t* nb = idx_rows + r * k;
+            double kv = kernel_dot(X, D, i, i);
+            for (int a = 0; a < k; ++a)
+                dots[a] = kernel_dot(X, D, i, nb[a]);
+            for (int a = 0; a < k; ++a)
+                for (int b = a; b < k; ++b)
+                {
+                    double v = kv - dots[a] - dots[b] + kernel_dot(X, D, nb[a], nb[b]);
+                    C[a * k + b] = v;
+                    C[b * k + a] = v;
+                }
+            double trace = 0.0;
+            for (int a = 0; a < k; ++a)
+                trace += C[a * k + a];
+            for (int a = 0; a < k; ++a)
+                C[a * k + a] += klle_shift * trace;
+            ldlt_solve(C.data(), k, rhs.data(), w.data());
+            double s = 0.0;
+            for (int a = 0; a < k; ++a)
+                s += w[a];
+            for (int a = 0; a < k; ++a)
+                W_out[r * k + a] = w[a] / s;
+        }
+    }
+    return 0;
+}
+
 // Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (row-major A,
 // destroyed). Eigenvalues ascending in evals; eigenvectors as columns of V
 // (row-major n x n). Restates the published cyclic Jacobi method; the

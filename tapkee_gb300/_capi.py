@@ -74,6 +74,7 @@ SIGNATURES = {
     "tk_status_string": (ctypes.c_char_p, [_I]),
     "tk_set_log_callback": (_I, [_P, LOG_FN, _P]),
     "tk_version": (ctypes.c_char_p, []),
+    "tk_kernel_launch_count": (ctypes.c_longlong, []),
     "tk_knn_brute": (_I, [_P, _P, _I, _I64, _I, _I64, _I, _I, _P, _P, ctypes.POINTER(tk_knn_stats)]),
     "tk_check_connected": (_I, [_P, _I64, _I, _P, ctypes.POINTER(_I)]),
     "tk_lle_weights": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P]),

@@ -403,64 +403,96 @@ __global__ void __launch_bounds__(32)
 
 } // namespace
 
-int64_t assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
-                 double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, bool count_only)
+namespace {
+struct AsmState
 {
-    cudaStream_t st = ctx->stream;
+    int64_t* rptr;
+    int32_t* rev;
+    int* row_nnz;
+    int32_t* big;
+    unsigned* nbig;
+};
+
+AsmState asm_state(tk_ctx* ctx, int64_t N, int k)
+{
     const int64_t nk = N * (int64_t)k;
-    if (nk >= (int64_t)1 << 31)
-        throw Error(TK_ERR_UNSUPPORTED, "assembly supports N*k < 2^31");
-    int* cnt = (int*)ctx->scratch.get("asm.cnt", sizeof(int) * (size_t)N * 2);
-    int* fillc = cnt + N;
-    int64_t* rptr = (int64_t*)ctx->scratch.get("asm.rptr", sizeof(int64_t) * (size_t)(N + 1));
-    int32_t* rev = (int32_t*)ctx->scratch.get("asm.rev", sizeof(int32_t) * (size_t)nk);
-    int* row_nnz = (int*)ctx->scratch.get("asm.rownnz", sizeof(int) * (size_t)N);
-    int32_t* big = (int32_t*)ctx->scratch.get("asm.big", sizeof(int32_t) * (size_t)N);
-    unsigned* nbig = (unsigned*)ctx->scratch.get("asm.nbig", 16);
-    int64_t* rp = row_ptr ? row_ptr : (int64_t*)ctx->scratch.get("asm.rowptr", sizeof(int64_t) * (size_t)(N + 1));
-    const int g = 4 * ctx->num_sms;
+    AsmState a;
+    a.rptr = (int64_t*)ctx->scratch.get("asm.rptr", sizeof(int64_t) * (size_t)(N + 1));
+    a.rev = (int32_t*)ctx->scratch.get("asm.rev", sizeof(int32_t) * (size_t)nk);
+    a.row_nnz = (int*)ctx->scratch.get("asm.rownnz", sizeof(int) * (size_t)N);
+    a.big = (int32_t*)ctx->scratch.get("asm.big", sizeof(int32_t) * (size_t)N);
+    a.nbig = (unsigned*)ctx->scratch.get("asm.nbig", 16);
+    return a;
+}
 
-    TK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)N * 2, st));
-    TK_CUDA(cudaMemsetAsync(nbig, 0, 16, st));
-    k_indeg<<<g, 256, 0, st>>>(idx, nk, N, cnt, ctx->dev_err);
-    TK_CHECK_LAUNCH();
-    k_scan_i64<<<1, 1024, 0, st>>>(cnt, N, rptr);
-    TK_CHECK_LAUNCH();
-    k_fill_rev<<<g, 256, 0, st>>>(idx, nk, rptr, fillc, rev);
-    TK_CHECK_LAUNCH();
-    k_sort_rev<<<g, 256, 0, st>>>(N, rptr, rev);
-    TK_CHECK_LAUNCH();
-
+void set_smem_limits()
+{
     const size_t smem = sizeof(RowTable<HC>) * ROW_WARPS;
     const size_t smem_big = sizeof(RowTable<HC_BIG>);
     TK_CUDA(cudaFuncSetAttribute(k_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     TK_CUDA(cudaFuncSetAttribute(k_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
-    const int64_t want = (N + ROW_WARPS - 1) / ROW_WARPS;
-    const int grid = (int)std::min<int64_t>(want, (int64_t)ctx->num_sms * 8);
+}
 
-    k_rows<false><<<grid, ROW_WARPS * 32, smem, st>>>(method, N, k, td, idx, weights, shift, rptr, rev, row_nnz,
-                                                       nullptr, nullptr, nullptr, big, nbig, ctx->dev_err);
+int rows_grid(tk_ctx* ctx, int64_t N)
+{
+    const int64_t want = (N + ROW_WARPS - 1) / ROW_WARPS;
+    return (int)std::min<int64_t>(want, (int64_t)ctx->num_sms * 8);
+}
+} // namespace
+
+int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, int64_t* row_ptr)
+{
+    cudaStream_t st = ctx->stream;
+    const int64_t nk = N * (int64_t)k;
+    if (nk >= (int64_t)1 << 31)
+        throw Error(TK_ERR_UNSUPPORTED, "assembly supports N*k < 2^31");
+    AsmState a = asm_state(ctx, N, k);
+    int* cnt = (int*)ctx->scratch.get("asm.cnt", sizeof(int) * (size_t)N * 2);
+    int* fillc = cnt + N;
+    const int g = 4 * ctx->num_sms;
+    TK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)N * 2, st));
+    TK_CUDA(cudaMemsetAsync(a.nbig, 0, 16, st));
+    k_indeg<<<g, 256, 0, st>>>(idx, nk, N, cnt, ctx->dev_err);
     TK_CHECK_LAUNCH();
-    k_rows_big<false><<<ctx->num_sms, 32, smem_big, st>>>(method, N, k, td, idx, weights, shift, rptr, rev,
-                                                           row_nnz, nullptr, nullptr, nullptr, big, nbig,
-                                                           ctx->dev_err);
+    k_scan_i64<<<1, 1024, 0, st>>>(cnt, N, a.rptr);
     TK_CHECK_LAUNCH();
-    k_scan_i64<<<1, 1024, 0, st>>>(row_nnz, N, rp);
+    k_fill_rev<<<g, 256, 0, st>>>(idx, nk, a.rptr, fillc, a.rev);
     TK_CHECK_LAUNCH();
-    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, rp + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    k_sort_rev<<<g, 256, 0, st>>>(N, a.rptr, a.rev);
+    TK_CHECK_LAUNCH();
+    set_smem_limits();
+    k_rows<false><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(RowTable<HC>) * ROW_WARPS, st>>>(
+        method, N, k, td, idx, nullptr, 0.0, a.rptr, a.rev, a.row_nnz, nullptr, nullptr, nullptr, a.big, a.nbig,
+        ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    k_rows_big<false><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, nullptr, 0.0,
+                                                                           a.rptr, a.rev, a.row_nnz, nullptr,
+                                                                           nullptr, nullptr, a.big, a.nbig,
+                                                                           ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    k_scan_i64<<<1, 1024, 0, st>>>(a.row_nnz, N, row_ptr);
+    TK_CHECK_LAUNCH();
+    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     TK_CUDA(cudaStreamSynchronize(st));
-    const int64_t nnz = ctx->host_i64[0];
-    if (count_only)
-        return nnz;
-    k_rows<true><<<grid, ROW_WARPS * 32, smem, st>>>(method, N, k, td, idx, weights, shift, rptr, rev, row_nnz, rp,
-                                                      col_idx, vals, big, nbig, ctx->dev_err);
+    return ctx->host_i64[0];
+}
+
+void assemble_numeric(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                      double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals)
+{
+    cudaStream_t st = ctx->stream;
+    AsmState a = asm_state(ctx, N, k);
+    set_smem_limits();
+    k_rows<true><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(RowTable<HC>) * ROW_WARPS, st>>>(
+        method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, row_ptr, col_idx, vals, a.big, a.nbig,
+        ctx->dev_err);
     TK_CHECK_LAUNCH();
-    k_rows_big<true><<<ctx->num_sms, 32, smem_big, st>>>(method, N, k, td, idx, weights, shift, rptr, rev, row_nnz,
-                                                          rp, col_idx, vals, big, nbig, ctx->dev_err);
+    k_rows_big<true><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, weights, shift,
+                                                                          a.rptr, a.rev, a.row_nnz, row_ptr, col_idx,
+                                                                          vals, a.big, a.nbig, ctx->dev_err);
     TK_CHECK_LAUNCH();
-    return nnz;
 }
 
 } // namespace tk

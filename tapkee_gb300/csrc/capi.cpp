@@ -14,6 +14,8 @@
 
 namespace tk {
 
+std::atomic<long long> g_kernel_launches{0};
+
 void* Scratch::get(const std::string& name, size_t bytes)
 {
     Buf& b = bufs[name];
@@ -156,12 +158,13 @@ void check_device_errors(tk_ctx* ctx)
     }
 }
 
+// Candidates kept per query by the screen: at least k + 8 (the self match and a
+// margin for certification).
 int candidates_for(int k)
 {
-    if (k + 8 <= 32)
-        return 32;
-    if (k + 8 <= 64)
-        return 64;
+    for (int kc : {32, 64, 128, 256})
+        if (k + 8 <= kc)
+            return kc;
     return -1;
 }
 
@@ -171,21 +174,37 @@ int64_t knn_device(tk_ctx* ctx, const void* Xd, int dtype, int64_t N, int D, int
 {
     const int kc = candidates_for(k);
     if (kc < 0)
-        throw Error(TK_ERR_UNSUPPORTED, "brute kNN supports up to 56 neighbours per point (k = " +
+        throw Error(TK_ERR_UNSUPPORTED, "brute kNN supports up to 248 neighbours per point (k = " +
                                             std::to_string(k) + ")");
-    const bool tensor = (screen == TK_SCREEN_TENSOR);
+    // The tensor-core screen keeps its candidate lists in registers (KC <= 64);
+    // longer lists (k > 56) use the FP32 screen's shared-memory lists.
+    bool tensor = (screen == TK_SCREEN_TENSOR);
+    if (tensor && kc > 64)
+    {
+        log(ctx, TK_LOG_INFO, "k = " + std::to_string(k) + " > 56: FP32 screen with " + std::to_string(kc) +
+                                  "-entry candidate lists");
+        tensor = false;
+        screen = TK_SCREEN_FP32;
+    }
+    if (tensor && !tensor_screen_supported(((D + 63) / 64) * 64))
+        throw Error(TK_ERR_UNSUPPORTED, "the tensor-core screen supports D <= 128; pass TK_SCREEN_FP32 for D = " +
+                                            std::to_string(D));
     Prepared P;
     prepare_points(ctx, Xd, dtype, N, D, ldx, tensor, P);
     int32_t* cand_idx = (int32_t*)ctx->scratch.get("knn.cand_idx", sizeof(int32_t) * (size_t)P.Npad * kc);
     float* cand_val = (float*)ctx->scratch.get("knn.cand_val", sizeof(float) * (size_t)P.Npad * kc);
+    TK_CUDA(cudaEventRecord(ctx->ev[8], ctx->stream));
     if (tensor)
         screen_tensor(ctx, P, kc, cand_idx, cand_val);
     else
         screen_fp32(ctx, P, kc, cand_idx, cand_val);
+    TK_CUDA(cudaEventRecord(ctx->ev[9], ctx->stream));
     float c1, c2;
     screen_error_model(screen, P.Dp, &c1, &c2);
     const int64_t nf = rerank(ctx, P, Xd, dtype, ldx, k, kc, cand_idx, cand_val, c1, c2, idx_d, d2_d);
     check_device_errors(ctx);
+    ctx->screen_ms = 0.f;
+    cudaEventElapsedTime(&ctx->screen_ms, ctx->ev[8], ctx->ev[9]);
     return nf;
 }
 
@@ -247,6 +266,8 @@ using namespace tk;
 extern "C" {
 
 const char* tk_version(void) { return TK_VERSION_STRING; }
+
+long long tk_kernel_launch_count(void) { return tk::g_kernel_launches.load(); }
 
 void tk_params_default(tk_params* p)
 {
@@ -470,7 +491,7 @@ int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t
         int64_t* rp_d = row_ptr ? device_out(ctx, row_ptr, (size_t)N + 1, "io.rowptr", &rh)
                                 : (int64_t*)ctx->scratch.get("io.rowptr", sizeof(int64_t) * ((size_t)N + 1));
         const int64_t cap = *nnz_io;
-        const int64_t nnz = assemble(ctx, method, N, k, td, idx_d, w_d, shift, rp_d, nullptr, nullptr, true);
+        const int64_t nnz = assemble_symbolic(ctx, method, N, k, td, idx_d, rp_d);
         check_device_errors(ctx);
         if (rh)
             copy_back(ctx, row_ptr, rp_d, (size_t)N + 1);
@@ -486,7 +507,7 @@ int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t
         bool ch, vh;
         int32_t* c_d = device_out(ctx, col_idx, (size_t)nnz, "io.col", &ch);
         double* v_d = device_out(ctx, vals, (size_t)nnz, "io.vals", &vh);
-        assemble(ctx, method, N, k, td, idx_d, w_d, shift, rp_d, c_d, v_d, false);
+        assemble_numeric(ctx, method, N, k, td, idx_d, w_d, shift, rp_d, c_d, v_d);
         check_device_errors(ctx);
         if (ch)
             copy_back(ctx, col_idx, c_d, (size_t)nnz);
@@ -585,13 +606,10 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
 
         // M
         int64_t* rp_d = (int64_t*)ctx->scratch.get("op.rowptr", sizeof(int64_t) * ((size_t)N + 1));
-        const int64_t nnz_bound = N * (int64_t)(k + 1) * (k + 1);
-        (void)nnz_bound;
-        const int64_t nnz = assemble(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, nullptr,
-                                     nullptr, true);
+        const int64_t nnz = assemble_symbolic(ctx, p.method, N, k, td, idx_d, rp_d);
         int32_t* col_d = (int32_t*)ctx->scratch.get("op.col", sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1));
         double* val_d = (double*)ctx->scratch.get("op.vals", sizeof(double) * (size_t)std::max<int64_t>(nnz, 1));
-        assemble(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, col_d, val_d, false);
+        assemble_numeric(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, col_d, val_d);
         TK_CUDA(cudaEventRecord(ctx->ev[6], st));
         check_device_errors(ctx);
 
@@ -609,6 +627,7 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
         o.stage_ms[2] = elapsed(ctx->ev[4], ctx->ev[5]);
         o.stage_ms[3] = elapsed(ctx->ev[5], ctx->ev[6]);
         o.stage_ms[4] = elapsed(ctx->ev[0], ctx->ev[6]);
+        o.stage_ms[5] = ctx->screen_ms;
         ctx->op_valid = true;
         if (info)
             *info = o;

@@ -20,14 +20,15 @@
 namespace tk {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 16, THREADS = 256;
-constexpr int PADM = BM + 4;
+constexpr int BN = 128, BK = 16, THREADS = 256;
 
-template <int KC>
+// BM queries per CTA (128: 8x8 outputs per thread; 64: 4x8, used with the long
+// candidate lists of k > 56), KC candidates kept per query.
+template <int BM, int KC>
 struct SimtSmem
 {
-    float As[2][BK][PADM];
-    float Bs[2][BK][PADM];
+    float As[2][BK][BM + 4];
+    float Bs[2][BK][BN + 4];
     float dist[BM][BN];
     unsigned mask[BM][BN / 32];
     float lv[BM][KC];
@@ -37,13 +38,14 @@ struct SimtSmem
     float nc[BN];    // candidate norms of the current tile
 };
 
-template <int KC>
+template <int BM, int KC>
 __global__ void __launch_bounds__(THREADS, 1)
     k_screen_simt(const float* __restrict__ xc, const float* __restrict__ nrm, int64_t Npad, int Dp,
                   int32_t* __restrict__ cand_idx, float* __restrict__ cand_val)
 {
+    constexpr int TM = BM / 16;  // rows per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SimtSmem<KC>& S = *reinterpret_cast<SimtSmem<KC>*>(smem_raw);
+    SimtSmem<BM, KC>& S = *reinterpret_cast<SimtSmem<BM, KC>*>(smem_raw);
     const int tid = threadIdx.x;
     const int tr = tid >> 4, tc = tid & 15;
     const int64_t q0 = (int64_t)blockIdx.x * BM;
@@ -61,38 +63,36 @@ __global__ void __launch_bounds__(THREADS, 1)
         S.cmp[tid] = FLT_MAX;
     }
 
-    // global -> shared staging: thread loads row (tid>>1), 8 consecutive k values
-    const int lrow = tid >> 1, lk = (tid & 1) * 8;
+    // global -> shared staging (transposed to k-major), float4 per element group
     auto load_chunk = [&](int buf, int64_t c0, int kc) {
-        const float4* ga = reinterpret_cast<const float4*>(xc + (q0 + lrow) * Dp + kc * BK + lk);
-        const float4* gb = reinterpret_cast<const float4*>(xc + (c0 + lrow) * Dp + kc * BK + lk);
-        const float4 a0 = ga[0], a1 = ga[1], b0 = gb[0], b1 = gb[1];
-        S.As[buf][lk + 0][lrow] = a0.x;
-        S.As[buf][lk + 1][lrow] = a0.y;
-        S.As[buf][lk + 2][lrow] = a0.z;
-        S.As[buf][lk + 3][lrow] = a0.w;
-        S.As[buf][lk + 4][lrow] = a1.x;
-        S.As[buf][lk + 5][lrow] = a1.y;
-        S.As[buf][lk + 6][lrow] = a1.z;
-        S.As[buf][lk + 7][lrow] = a1.w;
-        S.Bs[buf][lk + 0][lrow] = b0.x;
-        S.Bs[buf][lk + 1][lrow] = b0.y;
-        S.Bs[buf][lk + 2][lrow] = b0.z;
-        S.Bs[buf][lk + 3][lrow] = b0.w;
-        S.Bs[buf][lk + 4][lrow] = b1.x;
-        S.Bs[buf][lk + 5][lrow] = b1.y;
-        S.Bs[buf][lk + 6][lrow] = b1.z;
-        S.Bs[buf][lk + 7][lrow] = b1.w;
+        for (int e = tid; e < BM * (BK / 4); e += THREADS)
+        {
+            const int row = e / (BK / 4), kq = e % (BK / 4);
+            const float4 a = *reinterpret_cast<const float4*>(xc + (q0 + row) * Dp + kc * BK + kq * 4);
+            S.As[buf][kq * 4 + 0][row] = a.x;
+            S.As[buf][kq * 4 + 1][row] = a.y;
+            S.As[buf][kq * 4 + 2][row] = a.z;
+            S.As[buf][kq * 4 + 3][row] = a.w;
+        }
+        for (int e = tid; e < BN * (BK / 4); e += THREADS)
+        {
+            const int row = e / (BK / 4), kq = e % (BK / 4);
+            const float4 b = *reinterpret_cast<const float4*>(xc + (c0 + row) * Dp + kc * BK + kq * 4);
+            S.Bs[buf][kq * 4 + 0][row] = b.x;
+            S.Bs[buf][kq * 4 + 1][row] = b.y;
+            S.Bs[buf][kq * 4 + 2][row] = b.z;
+            S.Bs[buf][kq * 4 + 3][row] = b.w;
+        }
     };
 
-    ZigZag zz((int)blockIdx.x, ntiles);
+    ZigZag zz((int)((q0 / BN) < ntiles ? (q0 / BN) : 0), ntiles);
     for (int it = 0; it < ntiles; ++it)
     {
         const int tile = zz.next();
         const int64_t c0 = (int64_t)tile * BN;
-        float acc[8][8];
+        float acc[TM][8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < TM; ++i)
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 acc[i][j] = 0.f;
@@ -110,14 +110,21 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int kk = 0; kk < BK; ++kk)
             {
-                const float4 a0 = *reinterpret_cast<const float4*>(&S.As[buf][kk][tr * 8]);
-                const float4 a1 = *reinterpret_cast<const float4*>(&S.As[buf][kk][tr * 8 + 4]);
+                float a[TM];
+#pragma unroll
+                for (int q = 0; q < TM / 4; ++q)
+                {
+                    const float4 aq = *reinterpret_cast<const float4*>(&S.As[buf][kk][tr * TM + 4 * q]);
+                    a[4 * q + 0] = aq.x;
+                    a[4 * q + 1] = aq.y;
+                    a[4 * q + 2] = aq.z;
+                    a[4 * q + 3] = aq.w;
+                }
                 const float4 b0 = *reinterpret_cast<const float4*>(&S.Bs[buf][kk][tc * 4]);
                 const float4 b1 = *reinterpret_cast<const float4*>(&S.Bs[buf][kk][64 + tc * 4]);
-                const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
                 const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
+                for (int i = 0; i < TM; ++i)
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
                         acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
@@ -130,9 +137,9 @@ __global__ void __launch_bounds__(THREADS, 1)
             (&S.mask[0][0])[t] = 0u;
         __syncthreads();
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < TM; ++i)
         {
-            const int r = tr * 8 + i;
+            const int r = tr * TM + i;
             const float cmp = S.cmp[r];
 #pragma unroll
             for (int j = 0; j < 8; ++j)
@@ -175,13 +182,14 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
-template <int KC>
+template <int BM, int KC>
 void launch(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
 {
-    const size_t smem = sizeof(SimtSmem<KC>);
-    TK_CUDA(cudaFuncSetAttribute(k_screen_simt<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = sizeof(SimtSmem<BM, KC>);
+    static_assert(sizeof(SimtSmem<BM, KC>) <= 227 * 1024, "shared memory budget");
+    TK_CUDA(cudaFuncSetAttribute(k_screen_simt<BM, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)(P.Npad / BM);
-    k_screen_simt<KC><<<grid, THREADS, smem, ctx->stream>>>(P.xc, P.nrm, P.Npad, P.Dp, cand_idx, cand_val);
+    k_screen_simt<BM, KC><<<grid, THREADS, smem, ctx->stream>>>(P.xc, P.nrm, P.Npad, P.Dp, cand_idx, cand_val);
     TK_CHECK_LAUNCH();
 }
 
@@ -190,9 +198,13 @@ void launch(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
 void screen_fp32(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
 {
     if (kc == 32)
-        launch<32>(ctx, P, cand_idx, cand_val);
+        launch<128, 32>(ctx, P, cand_idx, cand_val);
     else if (kc == 64)
-        launch<64>(ctx, P, cand_idx, cand_val);
+        launch<128, 64>(ctx, P, cand_idx, cand_val);
+    else if (kc == 128)
+        launch<64, 128>(ctx, P, cand_idx, cand_val);
+    else if (kc == 256)
+        launch<64, 256>(ctx, P, cand_idx, cand_val);
     else
         throw Error(TK_ERR_INTERNAL, "screen_fp32: unsupported candidate count");
 }

@@ -14,6 +14,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "ff.cuh"
 #include "tk_internal.h"
 
 namespace tk {
@@ -32,6 +33,11 @@ struct JacobiSmem
     T rc[M / 2], rs[M / 2];
     int rp[M / 2], rq[M / 2];
     float Z[M][33];
+    float Zl[M][33];     // low parts of the centred coordinates (refinement)
+    float th[32][8], tl[32][8];  // t = Zc^T V for one chunk, float-float
+    double GV[M][8];     // G V for the refined basis
+    double Vt[M][8];     // refined basis
+    double lam[M];
 };
 
 // Parallel cyclic Jacobi on the symmetric M x M matrix S.A (one warp). On exit
@@ -154,6 +160,141 @@ __device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int d
     }
 }
 
+// First-order refinement of the top-td invariant subspace. The FP32 Jacobi gives
+// eigenpairs (lambda_j, u_j) of the FP32 Gram; the residual R = G V - V (V^T G V)
+// of the exact Gram G = Zc Zc^T is formed in float-float from the FP64-centred
+// coordinates, and each top vector is corrected by
+//     v_i += sum_{j not top} u_j (u_j . R_i) / (lambda_i - lambda_j),
+// then the basis is re-orthonormalised in FP64. This removes the FP32 Gram and
+// Jacobi errors to first order (error ~ eps^2 / gap).
+template <int M>
+__device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
+                                const int32_t* nbrs, int k, int td, const int* top)
+{
+    // V_t (FP32 columns of the top eigenvectors, k x td)
+    for (int e = lane; e < M * td; e += 32)
+    {
+        const int a = e / td, t = e % td;
+        S.Vt[a][t] = (a < k) ? (double)S.V[a][top[t]] : 0.0;
+    }
+    __syncwarp();
+    ff acc[8];
+    for (int t = 0; t < 8; ++t)
+        acc[t] = ff_zero();
+    const int a_own = lane;  // this lane accumulates (G V)[a_own][:]
+    for (int d0 = 0; d0 < D; d0 += 32)
+    {
+        const int d = d0 + lane;
+        double mean = 0.0;
+        if (d < D)
+            for (int a = 0; a < k; ++a)
+                mean += ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d);
+        mean /= (double)k;
+        for (int a = 0; a < M; ++a)
+        {
+            float h = 0.f, l = 0.f;
+            if (a < k && d < D)
+            {
+                const double z = ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d) - mean;
+                h = (float)z;
+                l = (float)(z - (double)h);
+            }
+            S.Z[a][lane] = h;
+            S.Zl[a][lane] = l;
+        }
+        __syncwarp();
+        // t_d = sum_a z_ad v_a   (lane = d)
+        for (int t = 0; t < td; ++t)
+        {
+            ff s = ff_zero();
+            for (int a = 0; a < k; ++a)
+                s = ff_fma(s, S.Z[a][lane], S.Zl[a][lane], (float)S.Vt[a][t], 0.f);
+            S.th[lane][t] = s.hi;
+            S.tl[lane][t] = s.lo;
+        }
+        __syncwarp();
+        // (G V)_a += sum_d z_ad t_d   (lane = a)
+        if (a_own < k)
+            for (int dd = 0; dd < 32; ++dd)
+            {
+                const float zh = S.Z[a_own][dd], zl = S.Zl[a_own][dd];
+                for (int t = 0; t < td; ++t)
+                    acc[t] = ff_fma(acc[t], zh, zl, S.th[dd][t], S.tl[dd][t]);
+            }
+        __syncwarp();
+    }
+    if (a_own < M)
+        for (int t = 0; t < td; ++t)
+            S.GV[a_own][t] = (a_own < k) ? ff_to_double(acc[t]) : 0.0;
+    __syncwarp();
+    // Rayleigh quotient Lambda = V^T G V (td x td) and residual R = G V - V Lambda
+    __shared__ double Lam_s[4][8][8];
+    double* Lam = &Lam_s[(threadIdx.x >> 5) & 3][0][0];
+    for (int e = lane; e < td * td; e += 32)
+    {
+        const int i = e / td, j = e % td;
+        double s = 0.0;
+        for (int a = 0; a < k; ++a)
+            s += S.Vt[a][i] * S.GV[a][j];
+        Lam[i * 8 + j] = s;
+    }
+    __syncwarp();
+    // corrections (lane = row a of the basis)
+    double corr[8];
+    for (int t = 0; t < td; ++t)
+        corr[t] = 0.0;
+    for (int j = 0; j < k; ++j)
+    {
+        bool is_top = false;
+        for (int t = 0; t < td; ++t)
+            is_top |= (top[t] == j);
+        if (is_top)
+            continue;
+        const double lj = (double)S.A[j][j];
+        for (int t = 0; t < td; ++t)
+        {
+            // u_j . R_t with R_t = GV_t - sum_s V_s Lam[s][t]
+            double ur = 0.0;
+            for (int a = 0; a < k; ++a)
+            {
+                double r = S.GV[a][t];
+                for (int q = 0; q < td; ++q)
+                    r -= S.Vt[a][q] * Lam[q * 8 + t];
+                ur += (double)S.V[a][j] * r;
+            }
+            const double gap = Lam[t * 8 + t] - lj;
+            if (lane < k && gap != 0.0)
+                corr[t] += (double)S.V[lane][j] * ur / gap;
+        }
+    }
+    __syncwarp();
+    if (lane < k)
+        for (int t = 0; t < td; ++t)
+            S.Vt[lane][t] += corr[t];
+    __syncwarp();
+    // modified Gram-Schmidt (FP64) on the td columns
+    for (int t = 0; t < td; ++t)
+    {
+        for (int q = 0; q < t; ++q)
+        {
+            double dot = 0.0;
+            for (int a = 0; a < k; ++a)
+                dot += S.Vt[a][t] * S.Vt[a][q];
+            __syncwarp();
+            if (lane < k)
+                S.Vt[lane][t] -= dot * S.Vt[lane][q];
+            __syncwarp();
+        }
+        double nrm = 0.0;
+        for (int a = 0; a < k; ++a)
+            nrm += S.Vt[a][t] * S.Vt[a][t];
+        __syncwarp();
+        if (lane < k)
+            S.Vt[lane][t] /= sqrt(nrm);
+        __syncwarp();
+    }
+}
+
 template <int M>
 __global__ void __launch_bounds__(128) k_ltsa(const void* X, int dtype, int64_t N, int D, int64_t ldx,
                                               const int32_t* __restrict__ idx, int k, int td, double* V,
@@ -203,10 +344,14 @@ __global__ void __launch_bounds__(128) k_ltsa(const void* X, int dtype, int64_t 
                 refine[atomicAdd(nrefine, 1u)] = (int32_t)i;
         }
         __syncwarp();
+        int top[8];
+        for (int t = 0; t < td; ++t)
+            top[t] = top_s[wib][td - 1 - t];  // ascending eigenvalue order, like rightCols(td)
+        refine_subspace<M>(S, lane, X, dtype, ldx, D, nb_s[wib], k, td, top);
         for (int e = lane; e < k * td; e += 32)
         {
             const int a = e / td, t = e % td;
-            V[(i * k + a) * td + t] = (double)S.V[a][top_s[wib][td - 1 - t]];
+            V[(i * k + a) * td + t] = S.Vt[a][t];
         }
         __syncwarp();
     }

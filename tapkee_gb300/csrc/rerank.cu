@@ -55,8 +55,8 @@ __device__ __forceinline__ bool key_less(double da, int ja, double db, int jb)
     return da < db || (da == db && ja < jb);
 }
 
-// One warp per query position p (sorted order). Lanes own candidates
-// l, l+32 (KC <= 64).
+// One warp per query position p (sorted order). Lane l owns candidates
+// l, l+32, l+64, ... (KC <= 256).
 template <int KC>
 __global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k, const int32_t* perm,
                          const double* kdiag, const float* nrm, const float* rmax, const int32_t* cand_idx,
@@ -152,7 +152,6 @@ __global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int6
     __shared__ int32_t sj[FB_CAP];
     __shared__ double sd[FB_CAP];
     __shared__ unsigned cnt;
-    __shared__ float xq[1024];
     const unsigned nf = *nfailed;
     for (unsigned f = blockIdx.x; f < nf; f += gridDim.x)
     {
@@ -210,7 +209,6 @@ __global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int6
         }
         __syncthreads();
     }
-    (void)xq;
 }
 
 } // namespace
@@ -249,12 +247,17 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
     unsigned* nfailed = (unsigned*)ctx->scratch.get("rerank.nfailed", 16);
     TK_CUDA(cudaMemsetAsync(nfailed, 0, 16, st));
     const int blocks = 8 * ctx->num_sms;
+#define TK_RERANK(KCV)                                                                                         \
+    k_rerank<KCV><<<blocks, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, P.nrm, P.rmax, cand_idx,    \
+                                          cand_val, eps_c1, eps_c2, idx_out, d2_out, failed, failed_ub, nfailed)
     if (kc == 32)
-        k_rerank<32><<<blocks, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, P.nrm, P.rmax, cand_idx,
-                                             cand_val, eps_c1, eps_c2, idx_out, d2_out, failed, failed_ub, nfailed);
+        TK_RERANK(32);
     else if (kc == 64)
-        k_rerank<64><<<blocks, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, P.nrm, P.rmax, cand_idx,
-                                             cand_val, eps_c1, eps_c2, idx_out, d2_out, failed, failed_ub, nfailed);
+        TK_RERANK(64);
+    else if (kc == 128)
+        TK_RERANK(128);
+    else if (kc == 256)
+        TK_RERANK(256);
     else
         throw Error(TK_ERR_INTERNAL, "rerank: unsupported candidate count");
     TK_CHECK_LAUNCH();

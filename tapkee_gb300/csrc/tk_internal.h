@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -33,7 +34,14 @@ struct Error : public std::runtime_error
         }                                                                                                    \
     } while (0)
 
-#define TK_CHECK_LAUNCH() TK_CUDA(cudaGetLastError())
+// Counts every kernel launch of the library (exported as tk_kernel_launch_count).
+extern std::atomic<long long> g_kernel_launches;
+#define TK_CHECK_LAUNCH()                                                                                   \
+    do                                                                                                      \
+    {                                                                                                       \
+        TK_CUDA(cudaGetLastError());                                                                        \
+        ::tk::g_kernel_launches.fetch_add(1, std::memory_order_relaxed);                                    \
+    } while (0)
 
 // Device-side error word bits (written by kernels instead of trapping).
 enum : unsigned
@@ -88,7 +96,8 @@ struct tk_ctx
     unsigned* dev_err = nullptr;      // device error word
     unsigned* host_err = nullptr;     // pinned mirror
     int64_t* host_i64 = nullptr;      // pinned small readback area (16 entries)
-    cudaEvent_t ev[8] = {};
+    cudaEvent_t ev[12] = {};
+    float screen_ms = 0.f;            // device time of the last distance screen
     int num_sms = 0;
     // operator held by the context
     tk_operator_info op{};
@@ -128,9 +137,13 @@ void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_
 void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
                 int k, int td, double* V);
 
-// assemble.cu: returns nnz; writes row_ptr/col/vals when non-null (device ptrs).
-int64_t assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
-                 double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, bool count_only);
+// assemble.cu: symbolic phase (reverse adjacency, row counts, row_ptr) returns
+// nnz; the numeric phase then fills col_idx/vals (device pointers) using the
+// symbolic state kept in the context's scratch.
+int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
+                          int64_t* row_ptr);
+void assemble_numeric(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                      double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals);
 
 // Screening error model (see rerank.cu): |approx - exact| <= c1 (|x|^2 + R^2) + c2 |x| R.
 void screen_error_model(int screen, int Dp, float* c1, float* c2);
