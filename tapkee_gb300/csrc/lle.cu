@@ -62,13 +62,13 @@ __device__ __forceinline__ void chol_solve(LleSmem<KP>& S, int lane)
     __syncwarp();
 }
 
-template <int KP, int WARPS>
+template <int KP, int WARPS, bool BLOCKED = (KP <= 64)>
 __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, int64_t N, int D, int64_t ldx,
                                                     const int32_t* __restrict__ idx, int k, double klle_shift,
                                                     double* __restrict__ W, unsigned* err)
 {
     constexpr int NB4 = KP / 4;
-    constexpr int NBLK = NB4 * (NB4 + 1) / 2;
+    constexpr int NBLK = BLOCKED ? NB4 * (NB4 + 1) / 2 : 1;
     constexpr int PERL = (NBLK + 31) / 32;
     constexpr int NPL = (KP + 31) / 32;  // neighbours per lane
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -110,6 +110,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         }
 
         // ---- FP32 Gram ----
+        if (!BLOCKED)
+        {
+            for (int t = lane; t < KP * KP; t += 32)
+                S.C[t / KP][t % KP] = 0.f;
+            __syncwarp();
+        }
         float acc[PERL][16];
 #pragma unroll
         for (int m = 0; m < PERL; ++m)
@@ -130,6 +136,22 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
                 S.Zh[a][lane] = v;
             }
             __syncwarp();
+            if (!BLOCKED)
+            {
+                // upper-triangle entries, one lane per entry (large k)
+                for (int e = lane; e < KP * KP; e += 32)
+                {
+                    const int a = e / KP, b = e % KP;
+                    if (b < a || b >= k)
+                        continue;
+                    float sacc = 0.f;
+                    for (int dd = 0; dd < 32; ++dd)
+                        sacc = fmaf(S.Zh[a][dd], S.Zh[b][dd], sacc);
+                    S.C[a][b] += sacc;
+                }
+                __syncwarp();
+                continue;
+            }
 #pragma unroll
             for (int m = 0; m < PERL; ++m)
             {
@@ -156,20 +178,32 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
             }
             __syncwarp();
         }
+        if (BLOCKED)
+        {
 #pragma unroll
-        for (int m = 0; m < PERL; ++m)
-            if (lane + 32 * m < NBLK)
+            for (int m = 0; m < PERL; ++m)
+                if (lane + 32 * m < NBLK)
+                {
+                    const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c)
+                        {
+                            S.C[I4 + r][J4 + c] = acc[m][r * 4 + c];
+                            S.C[J4 + c][I4 + r] = acc[m][r * 4 + c];
+                        }
+                }
+        }
+        else
+        {
+            for (int e = lane; e < KP * KP; e += 32)
             {
-                const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
-#pragma unroll
-                for (int r = 0; r < 4; ++r)
-#pragma unroll
-                    for (int c = 0; c < 4; ++c)
-                    {
-                        S.C[I4 + r][J4 + c] = acc[m][r * 4 + c];
-                        S.C[J4 + c][I4 + r] = acc[m][r * 4 + c];
-                    }
+                const int a = e / KP, b = e % KP;
+                if (b > a)
+                    S.C[b][a] = S.C[a][b];
             }
+        }
         __syncwarp();
         float trace = 0.f;
         for (int a = 0; a < k; ++a)
@@ -319,8 +353,10 @@ void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_
         launch<32, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
     else if (k <= 64)
         launch<64, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
+    else if (k <= 128)
+        launch<128, 1>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
     else
-        throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 64 neighbours");
+        throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 128 neighbours");
 }
 
 } // namespace tk

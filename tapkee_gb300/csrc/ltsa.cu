@@ -228,7 +228,7 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
             S.GV[a_own][t] = (a_own < k) ? ff_to_double(acc[t]) : 0.0;
     __syncwarp();
     // Rayleigh quotient Lambda = V^T G V (td x td) and residual R = G V - V Lambda
-    __shared__ double Lam_s[4][8][8];
+    __shared__ double Lam_s[4][8][8];  // up to 4 warps per block
     double* Lam = &Lam_s[(threadIdx.x >> 5) & 3][0][0];
     for (int e = lane; e < td * td; e += 32)
     {
@@ -295,17 +295,17 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
     }
 }
 
-template <int M>
-__global__ void __launch_bounds__(128) k_ltsa(const void* X, int dtype, int64_t N, int D, int64_t ldx,
+template <int M, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, int64_t N, int D, int64_t ldx,
                                               const int32_t* __restrict__ idx, int k, int td, double* V,
                                               int32_t* refine, unsigned* nrefine)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     JacobiSmem<M, float>& S = reinterpret_cast<JacobiSmem<M, float>*>(smem_raw)[wib];
-    __shared__ int nb_s[4][M];
-    const int64_t nw = (int64_t)gridDim.x * 4;
-    for (int64_t i = (int64_t)blockIdx.x * 4 + wib; i < N; i += nw)
+    __shared__ int nb_s[WARPS][M];
+    const int64_t nw = (int64_t)gridDim.x * WARPS;
+    for (int64_t i = (int64_t)blockIdx.x * WARPS + wib; i < N; i += nw)
     {
         for (int a = lane; a < k; a += 32)
             nb_s[wib][a] = idx[i * k + a];
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(128) k_ltsa(const void* X, int dtype, int64_t 
         centred_gram<M, float>(S, lane, X, dtype, ldx, D, nb_s[wib], k);
         warp_jacobi<M, float>(S, lane, 30);
         // order eigenvalues (lane 0, M <= 32): top td indices
-        __shared__ int top_s[4][8];
+        __shared__ int top_s[WARPS][8];
         if (lane == 0)
         {
             float lmax = -FLT_MAX;
@@ -413,14 +413,16 @@ template <int M>
 void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k, int td,
             double* V)
 {
+    constexpr int WARPS = (M <= 32) ? 4 : 2;
     cudaStream_t st = ctx->stream;
     int32_t* refine = (int32_t*)ctx->scratch.get("ltsa.refine", sizeof(int32_t) * (size_t)N);
     unsigned* nrefine = (unsigned*)ctx->scratch.get("ltsa.nrefine", 16);
     TK_CUDA(cudaMemsetAsync(nrefine, 0, 16, st));
-    const size_t smem = sizeof(JacobiSmem<M, float>) * 4;
-    TK_CUDA(cudaFuncSetAttribute(k_ltsa<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int grid = (int)std::min<int64_t>((N + 3) / 4, (int64_t)ctx->num_sms * 16);
-    k_ltsa<M><<<grid, 128, smem, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine);
+    const size_t smem = sizeof(JacobiSmem<M, float>) * WARPS;
+    static_assert(sizeof(JacobiSmem<M, float>) * WARPS <= 200 * 1024, "shared memory budget");
+    TK_CUDA(cudaFuncSetAttribute(k_ltsa<M, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = (int)std::min<int64_t>((N + WARPS - 1) / WARPS, (int64_t)ctx->num_sms * 16);
+    k_ltsa<M, WARPS><<<grid, WARPS * 32, smem, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine);
     TK_CHECK_LAUNCH();
     const size_t smem64 = sizeof(JacobiSmem<M, double>);
     TK_CUDA(cudaFuncSetAttribute(k_ltsa_fp64<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem64));
@@ -439,8 +441,10 @@ void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t
         launch<16>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
     else if (k <= 32)
         launch<32>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
+    else if (k <= 64)
+        launch<64>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
     else
-        throw Error(TK_ERR_UNSUPPORTED, "LTSA bases support up to 32 neighbours");
+        throw Error(TK_ERR_UNSUPPORTED, "LTSA bases support up to 64 neighbours");
 }
 
 } // namespace tk

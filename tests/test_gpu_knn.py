@@ -57,7 +57,7 @@ def test_lifted_rolls_match_oracle(ctx, screen, n, d, k, dtype):
 
 @pytest.mark.parametrize("screen", SCREENS)
 def test_small_and_ragged_sizes(ctx, screen):
-    for n, k in [(2, 1), (3, 2), (33, 5), (257, 31), (300, 56)]:
+    for n, k in [(2, 1), (3, 2), (33, 5), (257, 31), (300, 56), (400, 100), (600, 200)]:
         X = np.random.default_rng(n).normal(size=(n, 5)).astype(np.float32)
         idx = ctx.knn_brute(X, k, screen=screen)
         ref, _, _ = oracle.knn_brute(X, k)
@@ -86,7 +86,7 @@ def test_invalid_arguments(ctx):
     with pytest.raises(tk.NoDataError):
         ctx.knn_brute(np.zeros((0, 3), np.float32), 1)
     with pytest.raises(tk.UnsupportedMethodError):
-        ctx.knn_brute(np.random.default_rng(0).normal(size=(100, 3)), 60)
+        ctx.knn_brute(np.random.default_rng(0).normal(size=(300, 3)), 250)
 
 
 def test_device_resident_inputs(ctx):
