@@ -49,7 +49,16 @@ struct TcCfg
     static constexpr int TMEM_COLS = 2 * ACC_COLS;  // 512 or 256, power of two
     static constexpr int EPI_WARPS = 4 * QT;
     static constexpr int MMAS_PER_STAGE = QT * 3 * (DP / 16);
-    static constexpr size_t SMEM = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES + 1024 /*align*/ + 256;
+    static constexpr size_t EPI_BYTES = 8 * (128 * 4 + 32 * 17 * 4);  // per-warp norms + stash
+    static constexpr size_t SMEM = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES + 1024 /*align*/ + 256 + EPI_BYTES;
+};
+
+// Per-warp epilogue scratch: the norms of the tile being processed and a
+// 16-value stash per lane for the (rare) groups that beat the row threshold.
+struct EpiWarp
+{
+    float nrm[128];
+    float stash[32][17];
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -163,6 +172,24 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
         v[t] = __uint_as_float(r[t]);
 }
 
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+#pragma unroll
+    for (int t = 0; t < 32; ++t)
+        v[t] = __uint_as_float(r[t]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // Branchless sorted insertion into a register list (ascending).
 template <int KC>
 __device__ __forceinline__ void reg_insert(float (&L)[KC], int32_t (&I)[KC], float v, int32_t id)
@@ -204,6 +231,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t A_s = base;
     const uint32_t B_s = base + C::A_BYTES;
     TcBarriers& Bar = *reinterpret_cast<TcBarriers*>(gbase + C::A_BYTES + C::STAGES * C::B_STAGE_BYTES);
+    EpiWarp* epi = reinterpret_cast<EpiWarp*>(gbase + C::A_BYTES + C::STAGES * C::B_STAGE_BYTES + 256);
     volatile int* abort = &Bar.abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -350,10 +378,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             L[s] = FLT_MAX;
             I[s] = -1;
         }
+        EpiWarp& E = epi[warp];
         ZigZag zz((int)blockIdx.x * C::QT, ntiles);
+        int tile = zz.next();
+        float4 nr = __ldg(reinterpret_cast<const float4*>(nrm + (int64_t)tile * TC_N) + lane);
+        float cmp = L[KC - 1];
         for (int it = 0; it < ntiles; ++it)
         {
-            const int tile = zz.next();
             const int buf = it & 1;
             const uint32_t bph = (uint32_t)(it >> 1) & 1u;
             // tcgen05.ld is warp-collective: leave the loop as a whole warp
@@ -361,28 +392,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (!__all_sync(0xffffffffu, ok))
                 break;
             tc_fence_after();
+            // publish this tile's candidate norms to the warp's slice, prefetch the next
+            *reinterpret_cast<float4*>(&E.nrm[lane * 4]) = nr;
+            __syncwarp();
+            int tile_next = tile;
+            if (it + 1 < ntiles)
+            {
+                tile_next = zz.next();
+                nr = __ldg(reinterpret_cast<const float4*>(nrm + (int64_t)tile_next * TC_N) + lane);
+            }
             const int64_t c0 = (int64_t)tile * TC_N;
             const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
-            float cmp = L[KC - 1];
+            // columns per TMEM wait: 64 with 32-entry lists, 32 with 64-entry lists
+            constexpr int CPW = (KC <= 32) ? 64 : 32;
 #pragma unroll 1
-            for (int ch = 0; ch < TC_N / 16; ++ch)
+            for (int h = 0; h < TC_N / CPW; ++h)
             {
-                float v[16];
-                tmem_ld16(tacc + ch * 16, v);
-                const float4* np = reinterpret_cast<const float4*>(nrm + c0 + ch * 16);
+                float v[CPW];
+                tmem_ld32_nowait(tacc + h * CPW, v);
+                if (CPW == 64)
+                    tmem_ld32_nowait(tacc + h * CPW + 32, v + 32);
+                tmem_wait_ld();
 #pragma unroll
-                for (int g = 0; g < 4; ++g)
+                for (int g = 0; g < CPW / 16; ++g)
                 {
-                    const float4 n4 = __ldg(np + g);
-                    const float nn[4] = {n4.x, n4.y, n4.z, n4.w};
+                    // u = |y|^2 - 2 x.y for 16 candidates; one compare of their minimum
+                    float u[16];
+                    float mn = __int_as_float(0x7f800000);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
+                    for (int q4 = 0; q4 < 4; ++q4)
                     {
-                        const float t = fmaf(m2, v[g * 4 + e], nn[e]);
-                        if (t < cmp)
+                        const float4 n4 = *reinterpret_cast<const float4*>(&E.nrm[h * CPW + g * 16 + q4 * 4]);
+                        u[q4 * 4 + 0] = fmaf(m2, v[g * 16 + q4 * 4 + 0], n4.x);
+                        u[q4 * 4 + 1] = fmaf(m2, v[g * 16 + q4 * 4 + 1], n4.y);
+                        u[q4 * 4 + 2] = fmaf(m2, v[g * 16 + q4 * 4 + 2], n4.z);
+                        u[q4 * 4 + 3] = fmaf(m2, v[g * 16 + q4 * 4 + 3], n4.w);
+                        mn = fminf(mn, fminf(fminf(u[q4 * 4 + 0], u[q4 * 4 + 1]), fminf(u[q4 * 4 + 2], u[q4 * 4 + 3])));
+                    }
+                    if (mn < cmp)
+                    {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e)
+                            E.stash[lane][e] = u[e];
+                        const int32_t cbase = (int32_t)(c0 + h * CPW + g * 16);
+#pragma unroll 1
+                        for (int e = 0; e < 16; ++e)
                         {
-                            reg_insert<KC>(L, I, t, (int32_t)(c0 + ch * 16 + g * 4 + e));
-                            cmp = L[KC - 1];
+                            const float t = E.stash[lane][e];
+                            if (t < cmp)
+                            {
+                                reg_insert<KC>(L, I, t, cbase + e);
+                                cmp = L[KC - 1];
+                            }
                         }
                     }
                 }
@@ -391,6 +452,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             if (lane == 0)
                 mbar_arrive(smem_u32(&Bar.tempty[buf]));
+            tile = tile_next;
         }
 #pragma unroll
         for (int s = 0; s < KC; ++s)

@@ -177,12 +177,23 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
             acc[m] += (double)sa * (double)sb;
         }
     }
+    // per-block partial (fixed order over the block's 8 warps)
+    __shared__ double red[8][160];
+    const int wib = threadIdx.x >> 5;
 #pragma unroll
     for (int m = 0; m < 5; ++m)
     {
         const int p = lane + 32 * m;
         if (p < 136)
-            cov_partial[warp * 136 + p] = acc[m];
+            red[wib][p] = acc[m];
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < 136; p += blockDim.x)
+    {
+        double sacc = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            sacc += red[w][p];
+        cov_partial[(int64_t)blockIdx.x * 136 + p] = sacc;
     }
     if (rloc > 0.f)
         atomicMax(rmax_ord, f2ord(rloc));
@@ -215,7 +226,7 @@ __global__ void k_pca3(const double* cov_partial, int64_t nwarps, int D, float* 
         for (int c = 0; c < 3; ++c)
             V[t][c] = (t % 3 == c) ? 1.0 : 0.01 * (t + 1) * (c + 1);
     __syncthreads();
-    for (int it = 0; it < 60; ++it)
+    for (int it = 0; it < 30; ++it)
     {
         if (t < SKETCH)
             for (int c = 0; c < 3; ++c)
@@ -442,8 +453,7 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
 
     // 2. sketch covariance and R
     const int sk_blocks = 2 * sms;
-    const int64_t sk_warps = (int64_t)sk_blocks * 8;
-    double* covp = (double*)ctx->scratch.get("prep.covp", sizeof(double) * sk_warps * 136);
+    double* covp = (double*)ctx->scratch.get("prep.covp", sizeof(double) * sk_blocks * 136);
     unsigned* small = (unsigned*)ctx->scratch.get("prep.small", 64 * sizeof(unsigned));
     // small[0] = rmax ord, small[8..13] = bbox
     float* rmax = (float*)ctx->scratch.get("prep.rmax", 2 * sizeof(float));
@@ -460,7 +470,7 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
 
     // 3. principal directions and projection
     float* H = (float*)ctx->scratch.get("prep.H", sizeof(float) * 3 * (size_t)D);
-    k_pca3<<<1, 256, 0, st>>>(covp, sk_warps, D, H, small, rmax);
+    k_pca3<<<1, 256, 0, st>>>(covp, sk_blocks, D, H, small, rmax);
     TK_CHECK_LAUNCH();
     float* proj = (float*)ctx->scratch.get("prep.proj", sizeof(float) * 3 * (size_t)N);
     k_project<<<2 * sms, 256, 0, st>>>(X, dtype, N, D, ldx, mean, H, proj, small + 8);
