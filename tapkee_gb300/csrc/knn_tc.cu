@@ -6,14 +6,18 @@
 // with FP32 accumulation in tensor memory:
 //      x.y ~ 2^-2s (h_x.h_y + h_x.l_y + l_x.h_y),   2^s x = h_x + l_x (fp16 hi/lo)
 // (about 22 significant bits; the dropped l_x.l_y term is below 2^-22 |x||y|).
+// One more K=16 MMA per tile multiplies a constant A slice (2^13 everywhere) by
+// a per-candidate column holding -|2^s y|^2 / 2^14 as fp16 hi + lo, so the
+// accumulator is 2^2s (x.y - |y|^2 / 2) and |y|^2 - 2 x.y = -2^(1-2s) acc: the
+// epilogue needs no norm loads, only a running max per row.
 // Accumulators (128 lanes x 128 columns FP32 per query block) are
 // double-buffered in TMEM so the MMA of tile t+1 overlaps the epilogue of tile t.
 //
 // Warp roles (320 threads):
-//   warps 0..7  epilogue: tcgen05.ld the accumulator rows, form
-//               a - |x|^2 = |y|^2 - 2 x.y, and keep per query row (one thread per
-//               row) the KC smallest values in a sorted register list; entries at
-//               or above the row's KC-th value are rejected with one compare;
+//   warps 0..7  epilogue: tcgen05.ld the accumulator rows; per 32 columns one
+//               max and one compare against the row's KC-th value; only groups
+//               that beat it are expanded into the row's sorted register list of
+//               the KC smallest a - |x|^2 = |y|^2 - 2 x.y (one thread per row);
 //   warp  8     TMA producer (one thread): A tiles once, then B hi/lo tiles;
 //   warp  9     TMEM allocator and MMA issuer (one thread).
 // Every mbarrier wait is bounded by a wall-clock limit: on expiry the CTA records
@@ -41,24 +45,20 @@ struct TcCfg
 {
     static constexpr int QT = (DP <= 64) ? 2 : 1;  // A tiles (query blocks) per CTA
     static constexpr int KATOMS = DP / 64;         // 128-byte swizzle atoms along K
-    static constexpr int ATOM_BYTES = 128 * 128;   // 128 rows x 128 B
+    static constexpr int ATOM_BYTES = 128 * 128;   // 128 rows x 128 B (SW128)
+    static constexpr int EXTRA_BYTES = 128 * 32;   // 128 rows x 32 B (SW32): the norm column slice
     static constexpr int A_BYTES = QT * 2 * KATOMS * ATOM_BYTES;
     static constexpr int STAGES = (DP <= 64) ? 4 : 2;
-    static constexpr int B_STAGE_BYTES = 2 * KATOMS * ATOM_BYTES;
+    static constexpr int B_OPER_BYTES = 2 * KATOMS * ATOM_BYTES;        // hi + lo
+    static constexpr int B_STAGE_BYTES = B_OPER_BYTES + EXTRA_BYTES;    // + norm column
     static constexpr int ACC_COLS = QT * TC_N;
     static constexpr int TMEM_COLS = 2 * ACC_COLS;  // 512 or 256, power of two
     static constexpr int EPI_WARPS = 4 * QT;
-    static constexpr int MMAS_PER_STAGE = QT * 3 * (DP / 16);
-    static constexpr size_t EPI_BYTES = 8 * (128 * 4 + 32 * 17 * 4);  // per-warp norms + stash
-    static constexpr size_t SMEM = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES + 1024 /*align*/ + 256 + EPI_BYTES;
-};
-
-// Per-warp epilogue scratch: the norms of the tile being processed and a
-// 16-value stash per lane for the (rare) groups that beat the row threshold.
-struct EpiWarp
-{
-    float nrm[128];
-    float stash[32][17];
+    static constexpr int STASH = 8;                 // values per lane in the slow path
+    static constexpr size_t OFF_AX = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES;
+    static constexpr size_t OFF_BAR = OFF_AX + EXTRA_BYTES;
+    static constexpr size_t OFF_STASH = OFF_BAR + 256;
+    static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 1024 /*align*/;
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -137,6 +137,13 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
 {
     return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Same for the 32-byte-swizzled K=16 slices (rows of 32 B, 8-row groups 256 B apart).
+__device__ __forceinline__ uint64_t umma_desc_sw32(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(256 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
 }
 
 // kind::f16 instruction descriptor: D=F32, A=B=F16, K-major both, N=128, M=128
@@ -219,8 +226,9 @@ struct TcBarriers
 template <int DP, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_screen_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
-                const float* __restrict__ nrm, const float* __restrict__ scale_log2, int64_t Npad,
-                int32_t* __restrict__ cand_idx, float* __restrict__ cand_val, unsigned* err)
+                const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
+                int64_t Npad, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
+                const float* __restrict__ nrm, unsigned* err)
 {
     using C = TcCfg<DP>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -230,8 +238,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     unsigned char* gbase = smem_raw + (base - raw);
     const uint32_t A_s = base;
     const uint32_t B_s = base + C::A_BYTES;
-    TcBarriers& Bar = *reinterpret_cast<TcBarriers*>(gbase + C::A_BYTES + C::STAGES * C::B_STAGE_BYTES);
-    EpiWarp* epi = reinterpret_cast<EpiWarp*>(gbase + C::A_BYTES + C::STAGES * C::B_STAGE_BYTES + 256);
+    const uint32_t AX_s = base + (uint32_t)C::OFF_AX;
+    TcBarriers& Bar = *reinterpret_cast<TcBarriers*>(gbase + C::OFF_BAR);
+    float* stash_all = reinterpret_cast<float*>(gbase + C::OFF_STASH);
     volatile int* abort = &Bar.abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -255,6 +264,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         Bar.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    // constant A slice of the norm step: 2^13 (fp16 0x7000) in every element, so its
+    // swizzled layout is irrelevant
+    for (int t = threadIdx.x; t < C::EXTRA_BYTES / 4; t += blockDim.x)
+        reinterpret_cast<uint32_t*>(gbase + C::OFF_AX)[t] = 0x70007000u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (warp == 9)
     {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&Bar.tmem_base)),
@@ -288,11 +302,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (!mbar_wait(smem_u32(&Bar.empty[slot]), ph ^ 1u, abort, err))
                     break;
                 const uint32_t fb = smem_u32(&Bar.full[slot]);
+                const uint32_t bst = B_s + slot * C::B_STAGE_BYTES;
                 mbar_expect_tx(fb, C::B_STAGE_BYTES);
                 for (int part = 0; part < 2; ++part)
                     for (int ka = 0; ka < C::KATOMS; ++ka)
-                        tma_load_2d(B_s + slot * C::B_STAGE_BYTES + (part * C::KATOMS + ka) * C::ATOM_BYTES,
-                                    part ? &tm_lo : &tm_hi, ka * 64, tile * TC_N, fb);
+                        tma_load_2d(bst + (part * C::KATOMS + ka) * C::ATOM_BYTES, part ? &tm_lo : &tm_hi, ka * 64,
+                                    tile * TC_N, fb);
+                tma_load_2d(bst + C::B_OPER_BYTES, &tm_nrm, 0, tile * TC_N, fb);
                 issued = it + 1;
             }
             if (*abort)
@@ -313,6 +329,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             bool ok = mbar_wait(smem_u32(&Bar.afull), 0u, abort, err);
             tc_fence_after();
             int issued_any = 0;
+            const uint64_t axd = umma_desc_sw32(AX_s);
             for (int it = 0; ok && it < ntiles; ++it)
             {
                 const int slot = it % C::STAGES;
@@ -325,11 +342,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 tc_fence_after();
                 const uint32_t bstage = B_s + slot * C::B_STAGE_BYTES;
+                const uint64_t bxd = umma_desc_sw32(bstage + C::B_OPER_BYTES);
 #pragma unroll
                 for (int qt = 0; qt < C::QT; ++qt)
                 {
                     const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
-                    uint32_t acc = 0;
+                    // norm step first: D = 2^13 (h + l) of -|2^s y|^2 / 2^14
+                    umma_f16(d, axd, bxd, 0u);
 #pragma unroll
                     for (int prod = 0; prod < 3; ++prod)
                     {
@@ -342,8 +361,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                             const uint32_t koff = (uint32_t)(kk & 3) * 32u;
                             const uint64_t ad = umma_desc(A_s + ((qt * 2 + apart) * C::KATOMS + ka) * C::ATOM_BYTES + koff);
                             const uint64_t bd = umma_desc(bstage + (bpart * C::KATOMS + ka) * C::ATOM_BYTES + koff);
-                            umma_f16(d, ad, bd, acc);
-                            acc = 1;
+                            umma_f16(d, ad, bd, 1u);
                         }
                     }
                 }
@@ -369,7 +387,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int row = quad * 32 + lane;
         const int64_t q = q0 + qt * TC_M + row;
         const float nq = nrm[q];
-        const float m2 = -2.0f * exp2f(-2.0f * scale_log2[0]);
+        // |y|^2 - 2 x.y = m2 * acc, m2 = -2^(1-2s) (exact power of two)
+        const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);
+        const float inv_m2 = 1.0f / m2;
+        float* stash = stash_all + (warp * 32 + lane) * (C::STASH + 1);
         float L[KC];
         int32_t I[KC];
 #pragma unroll
@@ -378,13 +399,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             L[s] = FLT_MAX;
             I[s] = -1;
         }
-        EpiWarp& E = epi[warp];
+        float cmp = FLT_MAX;
+        float thr = -__int_as_float(0x7f800000);  // accept everything until the list fills
         ZigZag zz((int)blockIdx.x * C::QT, ntiles);
-        int tile = zz.next();
-        float4 nr = __ldg(reinterpret_cast<const float4*>(nrm + (int64_t)tile * TC_N) + lane);
-        float cmp = L[KC - 1];
         for (int it = 0; it < ntiles; ++it)
         {
+            const int tile = zz.next();
             const int buf = it & 1;
             const uint32_t bph = (uint32_t)(it >> 1) & 1u;
             // tcgen05.ld is warp-collective: leave the loop as a whole warp
@@ -392,15 +412,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (!__all_sync(0xffffffffu, ok))
                 break;
             tc_fence_after();
-            // publish this tile's candidate norms to the warp's slice, prefetch the next
-            *reinterpret_cast<float4*>(&E.nrm[lane * 4]) = nr;
-            __syncwarp();
-            int tile_next = tile;
-            if (it + 1 < ntiles)
-            {
-                tile_next = zz.next();
-                nr = __ldg(reinterpret_cast<const float4*>(nrm + (int64_t)tile_next * TC_N) + lane);
-            }
             const int64_t c0 = (int64_t)tile * TC_N;
             const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
             // columns per TMEM wait: 64 with 32-entry lists, 32 with 64-entry lists
@@ -414,35 +425,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     tmem_ld32_nowait(tacc + h * CPW + 32, v + 32);
                 tmem_wait_ld();
 #pragma unroll
-                for (int g = 0; g < CPW / 16; ++g)
+                for (int s32 = 0; s32 < CPW / 32; ++s32)
                 {
-                    // u = |y|^2 - 2 x.y for 16 candidates; one compare of their minimum
-                    float u[16];
-                    float mn = __int_as_float(0x7f800000);
+                    float gm[4];
 #pragma unroll
-                    for (int q4 = 0; q4 < 4; ++q4)
+                    for (int g = 0; g < 4; ++g)
                     {
-                        const float4 n4 = *reinterpret_cast<const float4*>(&E.nrm[h * CPW + g * 16 + q4 * 4]);
-                        u[q4 * 4 + 0] = fmaf(m2, v[g * 16 + q4 * 4 + 0], n4.x);
-                        u[q4 * 4 + 1] = fmaf(m2, v[g * 16 + q4 * 4 + 1], n4.y);
-                        u[q4 * 4 + 2] = fmaf(m2, v[g * 16 + q4 * 4 + 2], n4.z);
-                        u[q4 * 4 + 3] = fmaf(m2, v[g * 16 + q4 * 4 + 3], n4.w);
-                        mn = fminf(mn, fminf(fminf(u[q4 * 4 + 0], u[q4 * 4 + 1]), fminf(u[q4 * 4 + 2], u[q4 * 4 + 3])));
+                        const float* w = v + s32 * 32 + g * 8;
+                        gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
+                                      fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
                     }
-                    if (mn < cmp)
+                    if (fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3])) > thr)
                     {
 #pragma unroll
-                        for (int e = 0; e < 16; ++e)
-                            E.stash[lane][e] = u[e];
-                        const int32_t cbase = (int32_t)(c0 + h * CPW + g * 16);
-#pragma unroll 1
-                        for (int e = 0; e < 16; ++e)
+                        for (int g = 0; g < 4; ++g)
                         {
-                            const float t = E.stash[lane][e];
-                            if (t < cmp)
+                            if (gm[g] > thr)
                             {
-                                reg_insert<KC>(L, I, t, cbase + e);
-                                cmp = L[KC - 1];
+#pragma unroll
+                                for (int e = 0; e < 8; ++e)
+                                    stash[e] = v[s32 * 32 + g * 8 + e];
+                                const int64_t cb = c0 + h * CPW + s32 * 32 + g * 8;
+#pragma unroll 1
+                                for (int e = 0; e < 8; ++e)
+                                {
+                                    const float t = m2 * stash[e];
+                                    if (t < cmp && cb + e < N)
+                                    {
+                                        reg_insert<KC>(L, I, t, (int32_t)(cb + e));
+                                        cmp = L[KC - 1];
+                                        thr = cmp * inv_m2;
+                                    }
+                                }
                             }
                         }
                     }
@@ -452,7 +466,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             if (lane == 0)
                 mbar_arrive(smem_u32(&Bar.tempty[buf]));
-            tile = tile_next;
         }
 #pragma unroll
         for (int s = 0; s < KC; ++s)
@@ -486,15 +499,15 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int Dp)
+void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int box_cols, CUtensorMapSwizzle sw)
 {
-    const cuuint64_t dims[2] = {(cuuint64_t)Dp, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)Dp * 2};
-    const cuuint32_t box[2] = {64, 128};
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, 128};
     const cuuint32_t estr[2] = {1, 1};
     CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, (void*)base, dims, strides, box, estr,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         throw Error(TK_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
 }
@@ -504,13 +517,14 @@ void launch(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
 {
     using C = TcCfg<DP>;
     static_assert(C::SMEM <= 227 * 1024, "shared memory budget");
-    CUtensorMap mh, ml;
-    make_map(&mh, P.xh, P.Npad, P.Dp);
-    make_map(&ml, P.xl, P.Npad, P.Dp);
+    CUtensorMap mh, ml, mn;
+    make_map(&mh, P.xh, P.Npad, P.Dp, 64, CU_TENSOR_MAP_SWIZZLE_128B);
+    make_map(&ml, P.xl, P.Npad, P.Dp, 64, CU_TENSOR_MAP_SWIZZLE_128B);
+    make_map(&mn, P.xn, P.Npad, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B);
     TK_CUDA(cudaFuncSetAttribute(k_screen_tc<DP, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
     const int grid = (int)(P.Npad / (C::QT * TC_M));
-    k_screen_tc<DP, KC><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, P.nrm, P.rmax + 1, P.Npad, cand_idx,
-                                                                    cand_val, ctx->dev_err);
+    k_screen_tc<DP, KC><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, mn, P.rmax + 1, P.N, P.Npad, cand_idx,
+                                                                    cand_val, P.nrm, ctx->dev_err);
     TK_CHECK_LAUNCH();
 }
 
@@ -520,7 +534,7 @@ bool tensor_screen_supported(int Dp) { return Dp == 64 || Dp == 128; }
 
 void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
 {
-    if (!P.xh || !P.xl)
+    if (!P.xh || !P.xl || !P.xn)
         throw Error(TK_ERR_INTERNAL, "tensor screen needs the fp16 split layout");
     if (P.Dp == 64)
     {

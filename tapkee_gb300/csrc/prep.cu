@@ -380,7 +380,7 @@ __global__ void k_scatter(const unsigned* bucket, int64_t N, unsigned* offs, int
 // 5. screening layout in sorted order (one warp per row).
 __global__ void k_layout(const void* X, int dtype, int64_t N, int64_t Npad, int D, int Dp, int64_t ldx,
                          const double* mean, const int32_t* perm, const float* rmax, float* xc, float* nrm,
-                         __half* xh, __half* xl, double* kdiag, float* scale_out)
+                         __half* xh, __half* xl, __half* xn, double* kdiag, float* scale_out)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -425,6 +425,20 @@ __global__ void k_layout(const void* X, int dtype, int64_t N, int64_t Npad, int 
             nrm[p] = valid ? (float)n2 : __int_as_float(0x7f800000);
             if (valid)
                 kdiag[i] = k2;
+        }
+        if (xn && lane < 16)
+        {
+            // -|2^s xc|^2 / 2^14 as fp16 hi + lo: the tensor screen adds 2^13 (h + l)
+            // = -|2^s y|^2 / 2 to every dot product through one extra K=16 step.
+            // Padding rows stay 0 (the screen skips their indices).
+            __half v = __float2half_rn(0.f);
+            if (valid && lane < 2)
+            {
+                const double t = -n2 * ldexp(1.0, 2 * s) * (1.0 / 16384.0);
+                const __half h = __double2half(t);
+                v = (lane == 0) ? h : __double2half(t - (double)__half2float(h));
+            }
+            xn[p * 16 + lane] = v;
         }
     }
 }
@@ -501,14 +515,15 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     {
         P.xh = (uint16_t*)ctx->scratch.get("prep.xh", sizeof(uint16_t) * (size_t)P.Npad * P.Dp);
         P.xl = (uint16_t*)ctx->scratch.get("prep.xl", sizeof(uint16_t) * (size_t)P.Npad * P.Dp);
+        P.xn = (uint16_t*)ctx->scratch.get("prep.xn", sizeof(uint16_t) * (size_t)P.Npad * 16);
     }
     else
     {
-        P.xh = P.xl = nullptr;
+        P.xh = P.xl = P.xn = nullptr;
     }
     P.rmax = rmax;
     k_layout<<<4 * sms, 256, 0, st>>>(X, dtype, N, P.Npad, D, P.Dp, ldx, mean, P.perm, rmax, P.xc, P.nrm,
-                                      (__half*)P.xh, (__half*)P.xl, P.kdiag, rmax + 1);
+                                      (__half*)P.xh, (__half*)P.xl, (__half*)P.xn, P.kdiag, rmax + 1);
     TK_CHECK_LAUNCH();
 }
 

@@ -233,6 +233,9 @@ void screen_error_model(int screen, int Dp, float* c1, float* c2)
         const double split = 3.0 * 2.384185791015625e-07;          // 3 * 2^-22
         const double accum = (3.0 * Dp / 16.0 * 2.0 + 8.0) * 2.0 * u;  // ulp = 2^-23
         *c2 = (float)(2.0 * (split + accum) * 2.0);
+        // |y|^2 enters through an fp16 hi/lo column (relative 2^-22) and raises the
+        // accumulator magnitude by |y|^2 / 2 over the 3 Dp / 16 + 1 K-steps
+        *c1 += (float)(2.384185791015625e-07 + (3.0 * Dp / 16.0 + 3.0) * 2.0 * u);
     }
 }
 

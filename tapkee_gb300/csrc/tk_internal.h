@@ -76,6 +76,7 @@ struct Prepared
     float* nrm = nullptr;       // Npad squared norms of xc (+inf for padding rows)
     uint16_t* xh = nullptr;     // Npad x Dp fp16 high parts of scale*xc (tensor screen)
     uint16_t* xl = nullptr;     // Npad x Dp fp16 low parts
+    uint16_t* xn = nullptr;     // Npad x 16 fp16: hi/lo of -|2^s xc|^2 / 2^14 (cols 0,1), tensor screen
     int32_t* perm = nullptr;    // sorted position -> original index
     double* kdiag = nullptr;    // N exact k(i,i) in FP64, original order
     float* rmax = nullptr;      // device scalar: max |xc|
