@@ -86,13 +86,15 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
+// try_wait with a suspend-time hint: the thread sleeps in hardware until the
+// phase completes or ~0.5 ms pass, instead of spinning on the issue slots.
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(500000u)
         : "memory");
     return ok != 0;
 }
@@ -108,7 +110,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
     {
         if (mbar_try(bar, parity))
             return true;
-        if ((it & 63u) == 0u)
+        if ((it & 3u) == 0u)
         {
             if (*abort)
                 return false;
@@ -330,6 +332,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc_fence_after();
             int issued_any = 0;
             const uint64_t axd = umma_desc_sw32(AX_s);
+            // descriptors of every A slice (constant) and of stage 0's B slices;
+            // later stages add (stage offset >> 4) to the address field
+            uint64_t adesc[C::QT][2][DP / 16];
+#pragma unroll
+            for (int qt = 0; qt < C::QT; ++qt)
+#pragma unroll
+                for (int part = 0; part < 2; ++part)
+#pragma unroll
+                    for (int kk = 0; kk < DP / 16; ++kk)
+                        adesc[qt][part][kk] = umma_desc(A_s + ((qt * 2 + part) * C::KATOMS + (kk >> 2)) * C::ATOM_BYTES +
+                                                        (uint32_t)(kk & 3) * 32u);
+            uint64_t bdesc0[2][DP / 16];
+#pragma unroll
+            for (int part = 0; part < 2; ++part)
+#pragma unroll
+                for (int kk = 0; kk < DP / 16; ++kk)
+                    bdesc0[part][kk] =
+                        umma_desc(B_s + (part * C::KATOMS + (kk >> 2)) * C::ATOM_BYTES + (uint32_t)(kk & 3) * 32u);
+            const uint64_t bx0 = umma_desc_sw32(B_s + C::B_OPER_BYTES);
             for (int it = 0; ok && it < ntiles; ++it)
             {
                 const int slot = it % C::STAGES;
@@ -341,14 +362,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (!mbar_wait(smem_u32(&Bar.tempty[buf]), bph ^ 1u, abort, err))
                     break;
                 tc_fence_after();
-                const uint32_t bstage = B_s + slot * C::B_STAGE_BYTES;
-                const uint64_t bxd = umma_desc_sw32(bstage + C::B_OPER_BYTES);
+                const uint64_t soff = (uint64_t)((slot * C::B_STAGE_BYTES) >> 4);
 #pragma unroll
                 for (int qt = 0; qt < C::QT; ++qt)
                 {
                     const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
                     // norm step first: D = 2^13 (h + l) of -|2^s y|^2 / 2^14
-                    umma_f16(d, axd, bxd, 0u);
+                    umma_f16(d, axd, bx0 + soff, 0u);
 #pragma unroll
                     for (int prod = 0; prod < 3; ++prod)
                     {
@@ -356,13 +376,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         const int bpart = (prod == 1) ? 1 : 0;  // h_x . l_y
 #pragma unroll
                         for (int kk = 0; kk < DP / 16; ++kk)
-                        {
-                            const int ka = kk >> 2;
-                            const uint32_t koff = (uint32_t)(kk & 3) * 32u;
-                            const uint64_t ad = umma_desc(A_s + ((qt * 2 + apart) * C::KATOMS + ka) * C::ATOM_BYTES + koff);
-                            const uint64_t bd = umma_desc(bstage + (bpart * C::KATOMS + ka) * C::ATOM_BYTES + koff);
-                            umma_f16(d, ad, bd, 1u);
-                        }
+                            umma_f16(d, adesc[qt][apart][kk], bdesc0[bpart][kk] + soff, 1u);
                     }
                 }
                 umma_commit(smem_u32(&Bar.empty[slot]));
