@@ -1,7 +1,7 @@
 // knn_tc.cu -- tensor-core (tcgen05) distance screen for sm_103a.
 //
 // Each CTA owns QT blocks of 128 queries (sorted order) and streams every
-// candidate tile of 64 points through a STAGES-deep TMA pipeline. The dot
+// candidate tile of 128 points through a STAGES-deep TMA pipeline. The dot
 // products x.y run on the 5th-generation tensor cores as an fp16 split GEMM
 // with FP32 accumulation in tensor memory:
 //      x.y ~ 2^-2s (h_x.h_y + h_x.l_y + l_x.h_y),   2^s x = h_x + l_x (fp16 hi/lo)
@@ -10,9 +10,8 @@
 // a per-candidate column holding -|2^s y|^2 / 2^14 as fp16 hi + lo, so the
 // accumulator is 2^2s (x.y - |y|^2 / 2) and |y|^2 - 2 x.y = -2^(1-2s) acc: the
 // epilogue needs no norm loads, only a running max per row.
-// Accumulators (128 lanes x 64 columns FP32 per query block and stage) rotate
-// through 4 TMEM buffers, so the MMA can run up to three candidate tiles ahead
-// of the epilogue.
+// Accumulators (128 lanes x 128 columns FP32 per query block) are
+// double-buffered in TMEM so the MMA of tile t+1 overlaps the epilogue of tile t.
 //
 // Warp roles (320 threads):
 //   warps 0..7  epilogue: tcgen05.ld the accumulator rows; per 32 columns one
@@ -36,7 +35,7 @@
 namespace tk {
 namespace {
 
-constexpr int TC_N = 64;       // candidates per stage (MMA N)
+constexpr int TC_N = 128;      // candidates per stage (MMA N)
 constexpr int TC_M = 128;      // queries per A tile (MMA M)
 constexpr int TC_THREADS = 320;
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per single wait
@@ -44,25 +43,20 @@ constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per single wait
 template <int DP>
 struct TcCfg
 {
-    static constexpr int QT = (DP <= 64) ? 2 : 1;   // A tiles (query blocks of 128) per CTA
-    static constexpr int KATOMS = DP / 64;          // 128-byte swizzle atoms along K
-    static constexpr int A_ATOM = 128 * 128;        // 128 rows x 128 B (SW128)
-    static constexpr int B_ATOM = TC_N * 128;       // TC_N rows x 128 B (SW128)
-    static constexpr int EXTRA_A = 128 * 32;        // constant slice of the norm step (SW32)
-    static constexpr int EXTRA_B = TC_N * 32;       // norm column slice of a stage (SW32)
-    static constexpr int A_BYTES = QT * 2 * KATOMS * A_ATOM;
-    static constexpr int B_OPER_BYTES = 2 * KATOMS * B_ATOM;  // hi + lo
-    static constexpr int B_STAGE_BYTES = B_OPER_BYTES + ((EXTRA_B + 1023) / 1024) * 1024;
-    static constexpr int STASH = 8;                 // values per lane in the slow path
-    static constexpr size_t FIXED = (size_t)A_BYTES + EXTRA_A + 256 + (size_t)8 * 32 * (STASH + 1) * 4 + 1024;
-    static constexpr int STAGES_FIT = (int)((227 * 1024 - FIXED) / B_STAGE_BYTES);
-    static constexpr int STAGES = STAGES_FIT > 8 ? 8 : STAGES_FIT;
-    static constexpr int ACC_COLS = QT * TC_N;      // TMEM columns per accumulator buffer
-    static constexpr int NBUF = 4;                  // accumulator buffers in TMEM
-    static constexpr int TMEM_COLS = NBUF * ACC_COLS;  // 512 or 256, power of two
+    static constexpr int QT = (DP <= 64) ? 2 : 1;  // A tiles (query blocks) per CTA
+    static constexpr int KATOMS = DP / 64;         // 128-byte swizzle atoms along K
+    static constexpr int ATOM_BYTES = 128 * 128;   // 128 rows x 128 B (SW128)
+    static constexpr int EXTRA_BYTES = 128 * 32;   // 128 rows x 32 B (SW32): the norm column slice
+    static constexpr int A_BYTES = QT * 2 * KATOMS * ATOM_BYTES;
+    static constexpr int STAGES = (DP <= 64) ? 4 : 2;
+    static constexpr int B_OPER_BYTES = 2 * KATOMS * ATOM_BYTES;        // hi + lo
+    static constexpr int B_STAGE_BYTES = B_OPER_BYTES + EXTRA_BYTES;    // + norm column
+    static constexpr int ACC_COLS = QT * TC_N;
+    static constexpr int TMEM_COLS = 2 * ACC_COLS;  // 512 or 256, power of two
     static constexpr int EPI_WARPS = 4 * QT;
+    static constexpr int STASH = 8;                 // values per lane in the slow path
     static constexpr size_t OFF_AX = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES;
-    static constexpr size_t OFF_BAR = OFF_AX + EXTRA_A;
+    static constexpr size_t OFF_BAR = OFF_AX + EXTRA_BYTES;
     static constexpr size_t OFF_STASH = OFF_BAR + 256;
     static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 1024 /*align*/;
 };
@@ -154,7 +148,7 @@ __device__ __forceinline__ uint64_t umma_desc_sw32(uint32_t saddr)
            ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
 }
 
-// kind::f16 instruction descriptor: D=F32, A=B=F16, K-major both, N=TC_N, M=128
+// kind::f16 instruction descriptor: D=F32, A=B=F16, K-major both, N=128, M=128
 constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 
 __device__ __forceinline__ void umma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
@@ -172,6 +166,20 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
 
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int t = 0; t < 16; ++t)
+        v[t] = __uint_as_float(r[t]);
+}
 
 __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float* v)
 {
@@ -212,15 +220,14 @@ __device__ __forceinline__ void reg_insert(float (&L)[KC], int32_t (&I)[KC], flo
 
 struct TcBarriers
 {
-    uint64_t full[8], empty[8], tfull[4], tempty[4], afull, fin;
+    uint64_t full[4], empty[4], tfull[2], tempty[2], afull, fin;
     uint32_t tmem_base;
     int abort;
 };
 
 template <int DP, int KC>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_screen_tc(const __grid_constant__ CUtensorMap tma_hi, const __grid_constant__ CUtensorMap tma_lo,
-                const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
+    k_screen_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
                 const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
                 int64_t Npad, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
                 const float* __restrict__ nrm, unsigned* err)
@@ -249,7 +256,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(smem_u32(&Bar.full[s]), 1);
             mbar_init(smem_u32(&Bar.empty[s]), 1);
         }
-        for (int b = 0; b < C::NBUF; ++b)
+        for (int b = 0; b < 2; ++b)
         {
             mbar_init(smem_u32(&Bar.tfull[b]), 1);
             mbar_init(smem_u32(&Bar.tempty[b]), C::EPI_WARPS);
@@ -261,7 +268,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     // constant A slice of the norm step: 2^13 (fp16 0x7000) in every element, so its
     // swizzled layout is irrelevant
-    for (int t = threadIdx.x; t < C::EXTRA_A / 4; t += blockDim.x)
+    for (int t = threadIdx.x; t < C::EXTRA_BYTES / 4; t += blockDim.x)
         reinterpret_cast<uint32_t*>(gbase + C::OFF_AX)[t] = 0x70007000u;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (warp == 9)
@@ -285,9 +292,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (int qt = 0; qt < C::QT; ++qt)
                 for (int part = 0; part < 2; ++part)
                     for (int ka = 0; ka < C::KATOMS; ++ka)
-                        tma_load_2d(A_s + ((qt * 2 + part) * C::KATOMS + ka) * C::A_ATOM, part ? &tma_lo : &tma_hi,
+                        tma_load_2d(A_s + ((qt * 2 + part) * C::KATOMS + ka) * C::ATOM_BYTES, part ? &tm_lo : &tm_hi,
                                     ka * 64, (int)(q0 + qt * TC_M), afull);
-            ZigZag zz((int)blockIdx.x * C::QT * (TC_M / TC_N), ntiles);
+            ZigZag zz((int)blockIdx.x * C::QT, ntiles);
             int issued = 0;
             for (int it = 0; it < ntiles; ++it)
             {
@@ -301,7 +308,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 mbar_expect_tx(fb, C::B_STAGE_BYTES);
                 for (int part = 0; part < 2; ++part)
                     for (int ka = 0; ka < C::KATOMS; ++ka)
-                        tma_load_2d(bst + (part * C::KATOMS + ka) * C::B_ATOM, part ? &tm_lo : &tm_hi, ka * 64,
+                        tma_load_2d(bst + (part * C::KATOMS + ka) * C::ATOM_BYTES, part ? &tm_lo : &tm_hi, ka * 64,
                                     tile * TC_N, fb);
                 tma_load_2d(bst + C::B_OPER_BYTES, &tm_nrm, 0, tile * TC_N, fb);
                 issued = it + 1;
@@ -334,7 +341,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int part = 0; part < 2; ++part)
 #pragma unroll
                     for (int kk = 0; kk < DP / 16; ++kk)
-                        adesc[qt][part][kk] = umma_desc(A_s + ((qt * 2 + part) * C::KATOMS + (kk >> 2)) * C::A_ATOM +
+                        adesc[qt][part][kk] = umma_desc(A_s + ((qt * 2 + part) * C::KATOMS + (kk >> 2)) * C::ATOM_BYTES +
                                                         (uint32_t)(kk & 3) * 32u);
             uint64_t bdesc0[2][DP / 16];
 #pragma unroll
@@ -342,14 +349,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                 for (int kk = 0; kk < DP / 16; ++kk)
                     bdesc0[part][kk] =
-                        umma_desc(B_s + (part * C::KATOMS + (kk >> 2)) * C::B_ATOM + (uint32_t)(kk & 3) * 32u);
+                        umma_desc(B_s + (part * C::KATOMS + (kk >> 2)) * C::ATOM_BYTES + (uint32_t)(kk & 3) * 32u);
             const uint64_t bx0 = umma_desc_sw32(B_s + C::B_OPER_BYTES);
             for (int it = 0; ok && it < ntiles; ++it)
             {
                 const int slot = it % C::STAGES;
                 const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
-                const int buf = it % C::NBUF;
-                const uint32_t bph = (uint32_t)(it / C::NBUF) & 1u;
+                const int buf = it & 1;
+                const uint32_t bph = (uint32_t)(it >> 1) & 1u;
                 if (!mbar_wait(smem_u32(&Bar.full[slot]), ph, abort, err))
                     break;
                 if (!mbar_wait(smem_u32(&Bar.tempty[buf]), bph ^ 1u, abort, err))
@@ -408,12 +415,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         float cmp = FLT_MAX;
         float thr = -__int_as_float(0x7f800000);  // accept everything until the list fills
-        ZigZag zz((int)blockIdx.x * C::QT * (TC_M / TC_N), ntiles);
+        ZigZag zz((int)blockIdx.x * C::QT, ntiles);
         for (int it = 0; it < ntiles; ++it)
         {
             const int tile = zz.next();
-            const int buf = it % C::NBUF;
-            const uint32_t bph = (uint32_t)(it / C::NBUF) & 1u;
+            const int buf = it & 1;
+            const uint32_t bph = (uint32_t)(it >> 1) & 1u;
             // tcgen05.ld is warp-collective: leave the loop as a whole warp
             const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf]), bph, abort, err);
             if (!__all_sync(0xffffffffu, ok))
@@ -422,7 +429,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int64_t c0 = (int64_t)tile * TC_N;
             const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
             // columns per TMEM wait: 64 with 32-entry lists, 32 with 64-entry lists
-            constexpr int CPW = (KC <= 32 && TC_N >= 64) ? 64 : 32;
+            constexpr int CPW = (KC <= 32) ? 64 : 32;
 #pragma unroll 1
             for (int h = 0; h < TC_N / CPW; ++h)
             {
@@ -506,12 +513,11 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int box_cols, int box_rows,
-              CUtensorMapSwizzle sw)
+void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int box_cols, CUtensorMapSwizzle sw)
 {
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, 128};
     const cuuint32_t estr[2] = {1, 1};
     CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, (void*)base, dims, strides, box, estr,
                              CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -525,15 +531,13 @@ void launch(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
 {
     using C = TcCfg<DP>;
     static_assert(C::SMEM <= 227 * 1024, "shared memory budget");
-    CUtensorMap mah, mal, mh, ml, mn;
-    make_map(&mah, P.xh, P.Npad, P.Dp, 64, TC_M, CU_TENSOR_MAP_SWIZZLE_128B);
-    make_map(&mal, P.xl, P.Npad, P.Dp, 64, TC_M, CU_TENSOR_MAP_SWIZZLE_128B);
-    make_map(&mh, P.xh, P.Npad, P.Dp, 64, TC_N, CU_TENSOR_MAP_SWIZZLE_128B);
-    make_map(&ml, P.xl, P.Npad, P.Dp, 64, TC_N, CU_TENSOR_MAP_SWIZZLE_128B);
-    make_map(&mn, P.xn, P.Npad, 16, 16, TC_N, CU_TENSOR_MAP_SWIZZLE_32B);
+    CUtensorMap mh, ml, mn;
+    make_map(&mh, P.xh, P.Npad, P.Dp, 64, CU_TENSOR_MAP_SWIZZLE_128B);
+    make_map(&ml, P.xl, P.Npad, P.Dp, 64, CU_TENSOR_MAP_SWIZZLE_128B);
+    make_map(&mn, P.xn, P.Npad, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B);
     TK_CUDA(cudaFuncSetAttribute(k_screen_tc<DP, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
     const int grid = (int)(P.Npad / (C::QT * TC_M));
-    k_screen_tc<DP, KC><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mah, mal, mh, ml, mn, P.rmax + 1, P.N, P.Npad, cand_idx,
+    k_screen_tc<DP, KC><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, mn, P.rmax + 1, P.N, P.Npad, cand_idx,
                                                                     cand_val, P.nrm, ctx->dev_err);
     TK_CHECK_LAUNCH();
 }
