@@ -40,7 +40,7 @@ constexpr int TC_M = 128;      // queries per A tile (MMA M)
 constexpr int TC_THREADS = 320;
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per single wait
 
-template <int DP, int KC>
+template <int DP>
 struct TcCfg
 {
     static constexpr int QT = (DP <= 64) ? 2 : 1;  // A tiles (query blocks) per CTA
@@ -48,24 +48,17 @@ struct TcCfg
     static constexpr int ATOM_BYTES = 128 * 128;   // 128 rows x 128 B (SW128)
     static constexpr int EXTRA_BYTES = 128 * 32;   // 128 rows x 32 B (SW32): the norm column slice
     static constexpr int A_BYTES = QT * 2 * KATOMS * ATOM_BYTES;
-    // Candidate lists live in shared memory for D <= 64 with 32-entry lists:
-    // the registers they free hold a whole 128-column accumulator row, so each
-    // tile costs one TMEM load round. The lists take the room of two B stages.
-    static constexpr bool LSM = (DP <= 64 && KC == 32);
-    static constexpr int STAGES = LSM ? 2 : ((DP <= 64) ? 4 : 2);
+    static constexpr int STAGES = (DP <= 64) ? 4 : 2;
     static constexpr int B_OPER_BYTES = 2 * KATOMS * ATOM_BYTES;        // hi + lo
     static constexpr int B_STAGE_BYTES = B_OPER_BYTES + EXTRA_BYTES;    // + norm column
     static constexpr int ACC_COLS = QT * TC_N;
     static constexpr int TMEM_COLS = 2 * ACC_COLS;  // 512 or 256, power of two
     static constexpr int EPI_WARPS = 4 * QT;
     static constexpr int STASH = 8;                 // values per lane in the slow path
-    static constexpr int LIST_STRIDE = KC + 1;      // padded row of a shared-memory list
     static constexpr size_t OFF_AX = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES;
     static constexpr size_t OFF_BAR = OFF_AX + EXTRA_BYTES;
     static constexpr size_t OFF_STASH = OFF_BAR + 256;
-    static constexpr size_t OFF_LIST = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4;
-    static constexpr size_t LIST_BYTES = LSM ? (size_t)QT * 128 * LIST_STRIDE * 8 : 0;
-    static constexpr size_t SMEM = OFF_LIST + LIST_BYTES + 1024 /*align*/;
+    static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 1024 /*align*/;
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -239,7 +232,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 int64_t Npad, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
                 const float* __restrict__ nrm, unsigned* err)
 {
-    using C = TcCfg<DP, KC>;
+    using C = TcCfg<DP>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned operand region
     const uint32_t raw = smem_u32(smem_raw);
@@ -400,95 +393,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
     }
-    else if (C::LSM && warp < C::EPI_WARPS)
-    {
-        // ------------------------------------------------------------ epilogue
-        // (lists in shared memory, one TMEM round of 128 columns per tile)
-        const int quad = warp & 3;
-        const int qt = warp >> 2;
-        const int row = quad * 32 + lane;
-        const int64_t q = q0 + qt * TC_M + row;
-        const float nq = nrm[q];
-        const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);
-        const float inv_m2 = 1.0f / m2;
-        float* stash = stash_all + (warp * 32 + lane) * (C::STASH + 1);
-        float* lv = reinterpret_cast<float*>(gbase + C::OFF_LIST) + (qt * 128 + row) * C::LIST_STRIDE;
-        int32_t* li = reinterpret_cast<int32_t*>(gbase + C::OFF_LIST + C::LIST_BYTES / 2) +
-                      (qt * 128 + row) * C::LIST_STRIDE;
-        for (int s = 0; s < KC; ++s)
-        {
-            lv[s] = FLT_MAX;
-            li[s] = -1;
-        }
-        float cmp = FLT_MAX;
-        float thr = -__int_as_float(0x7f800000);  // accept everything until the list fills
-        ZigZag zz((int)blockIdx.x * C::QT, ntiles);
-        for (int it = 0; it < ntiles; ++it)
-        {
-            const int tile = zz.next();
-            const int buf = it & 1;
-            const uint32_t bph = (uint32_t)(it >> 1) & 1u;
-            const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf]), bph, abort, err);
-            if (!__all_sync(0xffffffffu, ok))
-                break;
-            tc_fence_after();
-            const int64_t c0 = (int64_t)tile * TC_N;
-            const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
-            float v[TC_N];
-#pragma unroll
-            for (int c = 0; c < TC_N; c += 32)
-                tmem_ld32_nowait(tacc + c, v + c);
-            tmem_wait_ld();
-            // the accumulator buffer can be refilled while this tile is filtered
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0)
-                mbar_arrive(smem_u32(&Bar.tempty[buf]));
-#pragma unroll
-            for (int s32 = 0; s32 < TC_N / 32; ++s32)
-            {
-                float gm[4];
-#pragma unroll
-                for (int g = 0; g < 4; ++g)
-                {
-                    const float* w = v + s32 * 32 + g * 8;
-                    gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
-                                  fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
-                }
-                if (fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3])) > thr)
-                {
-#pragma unroll
-                    for (int g = 0; g < 4; ++g)
-                    {
-                        if (gm[g] > thr)
-                        {
-#pragma unroll
-                            for (int e = 0; e < 8; ++e)
-                                stash[e] = v[s32 * 32 + g * 8 + e];
-                            const int64_t cb = c0 + s32 * 32 + g * 8;
-#pragma unroll 1
-                            for (int e = 0; e < 8; ++e)
-                            {
-                                const float t = m2 * stash[e];
-                                if (t < cmp && cb + e < N)
-                                {
-                                    list_insert<KC>(lv, li, t, (int32_t)(cb + e));
-                                    cmp = lv[KC - 1];
-                                    thr = cmp * inv_m2;
-                                }
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        for (int s = 0; s < KC; ++s)
-        {
-            cand_idx[q * KC + s] = li[s];
-            cand_val[q * KC + s] = (lv[s] < FLT_MAX) ? lv[s] + nq : FLT_MAX;
-        }
-    }
-    else if (!C::LSM && warp < C::EPI_WARPS)
+    else if (warp < C::EPI_WARPS)
     {
         // ------------------------------------------------------------ epilogue
         const int quad = warp & 3;
@@ -624,7 +529,7 @@ void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int 
 template <int DP, int KC>
 void launch(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
 {
-    using C = TcCfg<DP, KC>;
+    using C = TcCfg<DP>;
     static_assert(C::SMEM <= 227 * 1024, "shared memory budget");
     CUtensorMap mh, ml, mn;
     make_map(&mh, P.xh, P.Npad, P.Dp, 64, CU_TENSOR_MAP_SWIZZLE_128B);
