@@ -14,7 +14,9 @@
 //     source is one lane-parallel batch and every (row, col) sum is formed in
 //     the reference's serial triplet order;
 //   * the table is compacted, sorted by column (bitonic) and written.
-// Two passes: count (keys only) -> exclusive scan -> fill.
+// Two passes: count (keys only) -> exclusive scan -> fill. A row whose distinct
+// columns overflow the 256-slot table is redone by a one-warp kernel with an
+// 8192-slot table.
 //
 //   LLE  row j: source j  -> (j, 1+shift), (n_a, -w_ja)
 //               source r  -> (r, -w_ra), (n_b, w_ra w_rb)       [j = n_a of r]
@@ -28,9 +30,9 @@
 namespace tk {
 namespace {
 
-constexpr int HC = 1024;        // hash slots per warp (normal rows)
-constexpr int HC_BIG = 8192;    // hash slots for rows with a large in-degree
-constexpr int ROW_WARPS = 4;
+constexpr int HC = 256;         // hash slots per warp (normal rows)
+constexpr int HC_BIG = 8192;    // hash slots for rows that overflow HC
+constexpr int ROW_WARPS = 8;
 
 __global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, int* cnt, unsigned* err)
 {
@@ -328,7 +330,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32)
     k_rows(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx, const double* __restrict__ wts,
            double shift, const int64_t* __restrict__ rptr, const int32_t* __restrict__ rev, int* row_nnz,
            const int64_t* __restrict__ row_ptr, int32_t* col_idx, double* vals, int32_t* big_rows,
-           unsigned* nbig, unsigned* err)
+           unsigned* nbig, unsigned char* row_big, unsigned* err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -336,17 +338,31 @@ __global__ void __launch_bounds__(ROW_WARPS * 32)
     const int64_t nw = (int64_t)gridDim.x * ROW_WARPS;
     for (int64_t j = (int64_t)blockIdx.x * ROW_WARPS + wib; j < N; j += nw)
     {
-        const int64_t deg = rptr[j + 1] - rptr[j];
-        if (row_bound(method, k, deg) > (HC * 3) / 4)
+        // rows whose distinct columns do not fit HC go to the large-table kernel:
+        // decided from the bound when it is certain, else by trying
+        if (VALUES)
         {
-            if (!VALUES && lane == 0)
+            if (row_big[j])
+                continue;
+        }
+        else if (row_bound(method, k, rptr[j + 1] - rptr[j]) > (int64_t)HC_BIG)
+        {
+            if (lane == 0)
+            {
+                row_big[j] = 1;
                 big_rows[atomicAdd(nbig, 1u)] = (int32_t)j;
+            }
             continue;
         }
         const bool ok = process_row<HC, VALUES>(T, lane, method, j, k, td, idx, wts, shift, rptr, rev);
         if (!ok)
         {
-            if (lane == 0)
+            if (!VALUES && lane == 0)
+            {
+                row_big[j] = 1;
+                big_rows[atomicAdd(nbig, 1u)] = (int32_t)j;
+            }
+            else if (VALUES && lane == 0)
                 atomicOr(err, DEV_ERR_OVERFLOW);
             continue;
         }
@@ -377,11 +393,6 @@ __global__ void __launch_bounds__(32)
     for (unsigned r = blockIdx.x; r < nb; r += gridDim.x)
     {
         const int64_t j = big_rows[r];
-        const int64_t deg = rptr[j + 1] - rptr[j];
-        if (row_bound(method, k, deg) > (int64_t)HC_BIG * 3 / 4)
-        {
-            // the bound is loose; try anyway and report overflow if it really fills
-        }
         const bool ok = process_row<HC_BIG, VALUES>(T, lane, method, j, k, td, idx, wts, shift, rptr, rev);
         if (!ok)
         {
@@ -411,6 +422,7 @@ struct AsmState
     int* row_nnz;
     int32_t* big;
     unsigned* nbig;
+    unsigned char* row_big;
 };
 
 AsmState asm_state(tk_ctx* ctx, int64_t N, int k)
@@ -422,6 +434,7 @@ AsmState asm_state(tk_ctx* ctx, int64_t N, int k)
     a.row_nnz = (int*)ctx->scratch.get("asm.rownnz", sizeof(int) * (size_t)N);
     a.big = (int32_t*)ctx->scratch.get("asm.big", sizeof(int32_t) * (size_t)N);
     a.nbig = (unsigned*)ctx->scratch.get("asm.nbig", 16);
+    a.row_big = (unsigned char*)ctx->scratch.get("asm.rowbig", (size_t)N);
     return a;
 }
 
@@ -454,6 +467,7 @@ int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     const int g = 4 * ctx->num_sms;
     TK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)N * 2, st));
     TK_CUDA(cudaMemsetAsync(a.nbig, 0, 16, st));
+    TK_CUDA(cudaMemsetAsync(a.row_big, 0, (size_t)N, st));
     k_indeg<<<g, 256, 0, st>>>(idx, nk, N, cnt, ctx->dev_err);
     TK_CHECK_LAUNCH();
     k_scan_i64<<<1, 1024, 0, st>>>(cnt, N, a.rptr);
@@ -465,7 +479,7 @@ int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     set_smem_limits();
     k_rows<false><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(RowTable<HC>) * ROW_WARPS, st>>>(
         method, N, k, td, idx, nullptr, 0.0, a.rptr, a.rev, a.row_nnz, nullptr, nullptr, nullptr, a.big, a.nbig,
-        ctx->dev_err);
+        a.row_big, ctx->dev_err);
     TK_CHECK_LAUNCH();
     k_rows_big<false><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, nullptr, 0.0,
                                                                            a.rptr, a.rev, a.row_nnz, nullptr,
@@ -487,7 +501,7 @@ void assemble_numeric(tk_ctx* ctx, int method, int64_t N, int k, int td, const i
     set_smem_limits();
     k_rows<true><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(RowTable<HC>) * ROW_WARPS, st>>>(
         method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, row_ptr, col_idx, vals, a.big, a.nbig,
-        ctx->dev_err);
+        a.row_big, ctx->dev_err);
     TK_CHECK_LAUNCH();
     k_rows_big<true><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, weights, shift,
                                                                           a.rptr, a.rev, a.row_nnz, row_ptr, col_idx,

@@ -1,10 +1,17 @@
 // rerank.cu -- exact FP64 re-rank of screened candidates, certification, and the
 // exact fallback for rows the screen cannot certify.
 //
-// Distances are the reference's kernel-trick form (neighbors/neighbors.hpp:49-52)
-//   d2(i,j) = k(i,i) - 2 k(i,j) + k(j,j),  k = FP64 dot of the input rows
-// (squared: sqrt is monotone and the ranking is what is returned). The k
-// nearest other points are taken in (d2, index) order.
+// The exact distance is the squared Euclidean distance the reference evaluates
+// in kernel form (neighbors/neighbors.hpp:49-52, sqrt(k(i,i) - 2 k(i,j) + k(j,j)),
+// squared here: sqrt is monotone and only the ranking is returned), computed as
+// sum_d (x_d - y_d)^2 without cancellation:
+//   * float32 input: x_d - y_d is split exactly into hi + lo floats and the
+//     squares are accumulated in float-float (about 48 significant bits), on the
+//     FP32 pipes -- GB300's FP64 rate is a small fraction of its FP32 rate;
+//   * float64 input: differences and sums in FP64.
+// Either is at least as accurate as the reference's FP64 kernel-trick value,
+// whose cancellation error is ~1e-16 |x|^2. The k nearest other points are
+// taken in (d2, index) order.
 //
 // Certification. The screen returns, per query, the KC candidates with the
 // smallest approximate values a_j and their largest value T. With the error
@@ -18,6 +25,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "ff.cuh"
 #include "tk_internal.h"
 
 namespace tk {
@@ -30,26 +38,6 @@ __device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off
     return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
 }
 
-__device__ __forceinline__ double kdot(const void* X, int dtype, int64_t ldx, int D, int64_t a, int64_t b)
-{
-    double s = 0.0;
-    if (dtype == TK_F64)
-    {
-        const double* xa = reinterpret_cast<const double*>(X) + a * ldx;
-        const double* xb = reinterpret_cast<const double*>(X) + b * ldx;
-        for (int d = 0; d < D; ++d)
-            s = fma(xa[d], xb[d], s);
-    }
-    else
-    {
-        const float* xa = reinterpret_cast<const float*>(X) + a * ldx;
-        const float* xb = reinterpret_cast<const float*>(X) + b * ldx;
-        for (int d = 0; d < D; ++d)
-            s = fma((double)xa[d], (double)xb[d], s);
-    }
-    return s;
-}
-
 __device__ __forceinline__ bool key_less(double da, int ja, double db, int jb)
 {
     return da < db || (da == db && ja < jb);
@@ -57,6 +45,34 @@ __device__ __forceinline__ bool key_less(double da, int ja, double db, int jb)
 
 // One warp per query position p (sorted order). Lane l owns candidates
 // l, l+32, l+64, ... (KC <= 256).
+// Exact squared distance between rows a and b (see the header).
+__device__ __forceinline__ double exact_d2(const void* X, int dtype, int64_t ldx, int D, int64_t a, int64_t b)
+{
+    if (dtype == TK_F64)
+    {
+        const double* xa = reinterpret_cast<const double*>(X) + a * ldx;
+        const double* xb = reinterpret_cast<const double*>(X) + b * ldx;
+        double s = 0.0;
+        for (int d = 0; d < D; ++d)
+        {
+            const double z = xa[d] - xb[d];
+            s = fma(z, z, s);
+        }
+        return s;
+    }
+    const float* xa = reinterpret_cast<const float*>(X) + a * ldx;
+    const float* xb = reinterpret_cast<const float*>(X) + b * ldx;
+    ff acc = ff_zero();
+    float cross = 0.f;  // sum of 2 hi lo (relative size 2^-24 of the total)
+    for (int d = 0; d < D; ++d)
+    {
+        const ff z = two_sum(xa[d], -xb[d]);  // exact difference hi + lo
+        acc = ff_add(acc, two_prod(z.hi, z.hi));
+        cross = fmaf(2.f * z.hi, z.lo, cross);
+    }
+    return ff_to_double(acc) + (double)cross;
+}
+
 template <int KC>
 __global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k, const int32_t* perm,
                          const double* kdiag, const float* nrm, const float* rmax, const int32_t* cand_idx,
@@ -71,7 +87,6 @@ __global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N
     for (int64_t p = warp; p < N; p += nwarps)
     {
         const int64_t i = perm[p];
-        const double kii = kdiag[i];
         double d[PER];
         int j[PER];
 #pragma unroll
@@ -88,7 +103,7 @@ __global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N
                     const int64_t jj = perm[c];
                     if (jj != i)
                     {
-                        d[s] = kii - 2.0 * kdot(X, dtype, ldx, D, i, jj) + kdiag[jj];
+                        d[s] = exact_d2(X, dtype, ldx, D, i, jj);
                         j[s] = (int)jj;
                     }
                 }
@@ -161,7 +176,8 @@ __global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int6
         const double kii = kdiag[i];
         // FP32 direct-difference filter with a relative slack covering its error
         const double slack = (double)(D + 8) * 1.1920928955078125e-07;
-        const float thr = (float)(ub * (1.0 + slack) + 4.0 * 2.220446049250313e-16 * (kii + 1.0) * 16.0) * 1.0000005f;
+        const float thr = (float)(ub * (1.0 + slack)) * 1.0000005f + 1e-30f;
+        (void)kii;
         if (threadIdx.x == 0)
             cnt = 0;
         __syncthreads();
@@ -191,7 +207,7 @@ __global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int6
         __syncthreads();
         const unsigned n = min(cnt, (unsigned)FB_CAP);
         for (unsigned t = threadIdx.x; t < n; t += blockDim.x)
-            sd[t] = kii - 2.0 * kdot(X, dtype, ldx, D, i, sj[t]) + kdiag[sj[t]];
+            sd[t] = exact_d2(X, dtype, ldx, D, i, sj[t]);
         __syncthreads();
         if (n < (unsigned)k && threadIdx.x == 0)
             atomicOr(err, DEV_ERR_BOUNDS);
