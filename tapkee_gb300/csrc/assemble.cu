@@ -48,16 +48,40 @@ __global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, 
     }
 }
 
-// exclusive scan of n int counters into int64 offsets (out has n+1 entries), one block
-__global__ void k_scan_i64(const int* in, int64_t n, int64_t* out)
+// Exclusive scan of n int counters into int64 offsets (out has n+1 entries) in
+// three launches: per-segment sums, a one-block scan of the segment sums, and a
+// per-segment scan with its offset. Fixed segments, fixed order: deterministic.
+constexpr int SCAN_SEG = 2048;  // elements per segment (one 256-thread block)
+
+__global__ void k_seg_sums(const int* in, int64_t n, int64_t* seg)
+{
+    __shared__ int64_t red[256];
+    const int64_t b0 = (int64_t)blockIdx.x * SCAN_SEG;
+    int64_t s = 0;
+    for (int t = threadIdx.x; t < SCAN_SEG; t += blockDim.x)
+        if (b0 + t < n)
+            s += in[b0 + t];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
+    {
+        if ((int)threadIdx.x < o)
+            red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        seg[blockIdx.x] = red[0];
+}
+
+__global__ void k_scan_segs(int64_t* seg, int nseg, int64_t* total)
 {
     __shared__ int64_t part[1024];
     const int t = threadIdx.x;
-    const int64_t per = (n + 1023) / 1024;
-    const int64_t b0 = t * per, b1 = min(n, b0 + per);
+    const int per = (nseg + 1023) / 1024;
+    const int b0 = t * per, b1 = min(nseg, b0 + per);
     int64_t s = 0;
-    for (int64_t b = b0; b < b1; ++b)
-        s += in[b];
+    for (int b = b0; b < b1; ++b)
+        s += seg[b];
     part[t] = s;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1)
@@ -68,13 +92,58 @@ __global__ void k_scan_i64(const int* in, int64_t n, int64_t* out)
         __syncthreads();
     }
     int64_t run = part[t] - s;
-    for (int64_t b = b0; b < b1; ++b)
+    for (int b = b0; b < b1; ++b)
     {
-        out[b] = run;
-        run += in[b];
+        const int64_t c = seg[b];
+        seg[b] = run;
+        run += c;
     }
     if (t == 1023)
-        out[n] = part[1023];
+        *total = part[1023];
+}
+
+__global__ void k_seg_scan(const int* in, int64_t n, const int64_t* seg, int64_t* out)
+{
+    constexpr int PER = SCAN_SEG / 256;
+    __shared__ int64_t part[256];
+    const int64_t b0 = (int64_t)blockIdx.x * SCAN_SEG + (int64_t)threadIdx.x * PER;
+    int64_t v[PER];
+    int64_t s = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q)
+    {
+        v[q] = (b0 + q < n) ? in[b0 + q] : 0;
+        s += v[q];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1)
+    {
+        const int64_t x = ((int)threadIdx.x >= o) ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += x;
+        __syncthreads();
+    }
+    int64_t run = seg[blockIdx.x] + part[threadIdx.x] - s;
+#pragma unroll
+    for (int q = 0; q < PER; ++q)
+    {
+        if (b0 + q < n)
+            out[b0 + q] = run;
+        run += v[q];
+    }
+}
+
+void scan_to_offsets(tk_ctx* ctx, const int* in, int64_t n, int64_t* out)
+{
+    const int nseg = (int)((n + SCAN_SEG - 1) / SCAN_SEG);
+    int64_t* seg = (int64_t*)ctx->scratch.get("asm.scanseg", sizeof(int64_t) * (size_t)std::max(nseg, 1));
+    k_seg_sums<<<nseg, 256, 0, ctx->stream>>>(in, n, seg);
+    TK_CHECK_LAUNCH();
+    k_scan_segs<<<1, 1024, 0, ctx->stream>>>(seg, nseg, out + n);
+    TK_CHECK_LAUNCH();
+    k_seg_scan<<<nseg, 256, 0, ctx->stream>>>(in, n, seg, out);
+    TK_CHECK_LAUNCH();
 }
 
 __global__ void k_fill_rev(const int32_t* __restrict__ idx, int64_t nk, const int64_t* rptr, int* fillc,
@@ -470,8 +539,7 @@ int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     TK_CUDA(cudaMemsetAsync(a.row_big, 0, (size_t)N, st));
     k_indeg<<<g, 256, 0, st>>>(idx, nk, N, cnt, ctx->dev_err);
     TK_CHECK_LAUNCH();
-    k_scan_i64<<<1, 1024, 0, st>>>(cnt, N, a.rptr);
-    TK_CHECK_LAUNCH();
+    scan_to_offsets(ctx, cnt, N, a.rptr);
     k_fill_rev<<<g, 256, 0, st>>>(idx, nk, a.rptr, fillc, a.rev);
     TK_CHECK_LAUNCH();
     k_sort_rev<<<g, 256, 0, st>>>(N, a.rptr, a.rev);
@@ -486,8 +554,7 @@ int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, con
                                                                            nullptr, nullptr, a.big, a.nbig,
                                                                            ctx->dev_err);
     TK_CHECK_LAUNCH();
-    k_scan_i64<<<1, 1024, 0, st>>>(a.row_nnz, N, row_ptr);
-    TK_CHECK_LAUNCH();
+    scan_to_offsets(ctx, a.row_nnz, N, row_ptr);
     TK_CUDA(cudaMemcpyAsync(ctx->host_i64, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     TK_CUDA(cudaStreamSynchronize(st));
     return ctx->host_i64[0];

@@ -23,6 +23,19 @@ __device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off
     return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
 }
 
+// x_a - x_b for element d as an unevaluated float sum hi + lo (exact for float32
+// input: two_sum of the two floats; float64 input: the FP64 difference split).
+__device__ __forceinline__ ff diff_ff(const void* X, int dtype, int64_t a_off, int64_t b_off)
+{
+    if (dtype == TK_F64)
+    {
+        const double z = reinterpret_cast<const double*>(X)[a_off] - reinterpret_cast<const double*>(X)[b_off];
+        const float h = (float)z;
+        return ff{h, (float)(z - (double)h)};
+    }
+    return two_sum(reinterpret_cast<const float*>(X)[a_off], -reinterpret_cast<const float*>(X)[b_off]);
+}
+
 template <int KP>
 struct LleSmem
 {
@@ -69,7 +82,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
 {
     constexpr int NB4 = KP / 4;
     constexpr int NBLK = BLOCKED ? NB4 * (NB4 + 1) / 2 : 1;
-    constexpr int PERL = (NBLK + 31) / 32;
+    // (block, dimension group) items: with few blocks the 32-dimension chunk is
+    // split into DG ranges so that all lanes accumulate
+    constexpr int DG = !BLOCKED ? 1 : ((32 / NBLK) >= 3 ? 3 : ((32 / NBLK) >= 1 ? (32 / NBLK) : 1));
+    constexpr int ITEMS = NBLK * DG;
+    constexpr int PERL = (ITEMS + 31) / 32;
+    constexpr int SPAN = (32 + DG - 1) / DG;
     constexpr int NPL = (KP + 31) / 32;  // neighbours per lane
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -77,14 +95,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
     const int64_t warp = (int64_t)blockIdx.x * WARPS + wib;
     const int64_t nwarps = (int64_t)gridDim.x * WARPS;
 
-    // (I, J) 4x4 blocks of the upper triangle owned by this lane
-    int bI[PERL], bJ[PERL];
+    // (I, J) 4x4 blocks of the upper triangle and dimension group of each item of this lane
+    int bI[PERL], bJ[PERL], bG[PERL];
 #pragma unroll
     for (int m = 0; m < PERL; ++m)
     {
-        int b = lane + 32 * m, I = 0;
-        if (b >= NBLK)
-            b = 0;
+        const int itm = lane + 32 * m;
+        int b = (itm < ITEMS) ? itm % NBLK : 0, I = 0;
         while (b >= NB4 - I)
         {
             b -= NB4 - I;
@@ -92,6 +109,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         }
         bI[m] = I;
         bJ[m] = I + b;
+        bG[m] = (itm < ITEMS) ? itm / NBLK : 0;
     }
 
     for (int64_t i = warp; i < N; i += nwarps)
@@ -125,14 +143,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         for (int d0 = 0; d0 < D; d0 += 32)
         {
             const int d = d0 + lane;
-            const double xi = (d < D) ? ldx_elem(X, dtype, i * ldx + d) : 0.0;
 #pragma unroll 4
             for (int a = 0; a < KP; ++a)
             {
                 const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
                 float v = 0.f;
                 if (a < k && d < D)
-                    v = (float)(ldx_elem(X, dtype, (int64_t)nba * ldx + d) - xi);
+                    v = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d).hi;
                 S.Zh[a][lane] = v;
             }
             __syncwarp();
@@ -155,11 +172,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
 #pragma unroll
             for (int m = 0; m < PERL; ++m)
             {
-                if (lane + 32 * m < NBLK)
+                if (lane + 32 * m < ITEMS)
                 {
                     const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
-#pragma unroll 8
-                    for (int dd = 0; dd < 32; ++dd)
+                    const int dlo = bG[m] * SPAN, dhi = min(32, dlo + SPAN);
+#pragma unroll 4
+                    for (int dd = dlo; dd < dhi; ++dd)
                     {
                         float av[4], bv[4];
 #pragma unroll
@@ -180,20 +198,31 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         }
         if (BLOCKED)
         {
+            // dimension groups are summed in a fixed order (group 0 writes, then 1, 2 add)
 #pragma unroll
-            for (int m = 0; m < PERL; ++m)
-                if (lane + 32 * m < NBLK)
-                {
-                    const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
+            for (int g = 0; g < DG; ++g)
+            {
 #pragma unroll
-                    for (int r = 0; r < 4; ++r)
+                for (int m = 0; m < PERL; ++m)
+                    if (lane + 32 * m < ITEMS && bG[m] == g)
+                    {
+                        const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
 #pragma unroll
-                        for (int c = 0; c < 4; ++c)
-                        {
-                            S.C[I4 + r][J4 + c] = acc[m][r * 4 + c];
-                            S.C[J4 + c][I4 + r] = acc[m][r * 4 + c];
-                        }
-                }
+                        for (int r = 0; r < 4; ++r)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c)
+                                if (I4 + r <= J4 + c)  // upper triangle only
+                                    S.C[I4 + r][J4 + c] =
+                                        (g == 0) ? acc[m][r * 4 + c] : S.C[I4 + r][J4 + c] + acc[m][r * 4 + c];
+                    }
+                __syncwarp();
+            }
+            for (int e = lane; e < KP * KP; e += 32)
+            {
+                const int a = e / KP, b = e % KP;
+                if (a > b)
+                    S.C[a][b] = S.C[b][a];
+            }
         }
         else
         {
@@ -257,19 +286,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
             for (int d0 = 0; d0 < D; d0 += 32)
             {
                 const int d = d0 + lane;
-                const double xi = (d < D) ? ldx_elem(X, dtype, i * ldx + d) : 0.0;
                 for (int a = 0; a < KP; ++a)
                 {
                     const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
-                    float h = 0.f, l = 0.f;
+                    ff z = ff_zero();
                     if (a < k && d < D)
-                    {
-                        const double z = ldx_elem(X, dtype, (int64_t)nba * ldx + d) - xi;
-                        h = (float)z;
-                        l = (float)(z - (double)h);
-                    }
-                    S.Zh[a][lane] = h;
-                    S.Zl[a][lane] = l;
+                        z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
+                    S.Zh[a][lane] = z.hi;
+                    S.Zl[a][lane] = z.lo;
                 }
                 __syncwarp();
                 // v_d = sum_b w_b z_bd for d = d0 + lane
@@ -329,329 +353,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
     }
 }
 
-// ---------------------------------------------------------------------------
-// k <= 32: one warp per point, register Cholesky, lane-per-dimension refinement.
-//
-//   Gram   : the 32-dimension chunk of Z = neighbours - x is staged in shared
-//            memory; (4x4 block, dimension group) items spread the upper
-//            triangle over all lanes; partial blocks are summed per entry.
-//   Solve  : lane r holds row r of C; right-looking Cholesky with shuffles,
-//            forward substitution on rows, backward substitution on the
-//            columns of L (one shared-memory transpose).
-//   Refine : lane l owns dimensions l, l+32, ...; with the exact differences
-//            z = hi + lo, v = sum_b w_b z_b and (C w)_a = z_a . v are formed in
-//            float-float lane-locally and reduced across the warp.
-template <int KP>
-struct LleSmallSmem
-{
-    float Z[KP][33];
-    float P[3][KP][KP + 1];  // per dimension-group partial Grams (upper triangle)
-    float Lt[KP][KP + 1];    // L transposed
-    float w[KP];
-    float r[KP];
-    int nb[KP];
-};
-
-template <int KP>
-__device__ __forceinline__ float shfl_f(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-
-// Solves L L^T x = b for the lane-held right-hand side b (lane a < KP holds b_a);
-// Lrow: lane r's row of L, Lcol: lane r's column of L. Returns x_a in lane a.
-template <int KP>
-__device__ __forceinline__ float chol_solve_reg(const float (&Lrow)[KP], const float (&Lcol)[KP], float b, int lane)
-{
-    // forward: L y = b
-#pragma unroll
-    for (int j = 0; j < KP; ++j)
-    {
-        const float yj = shfl_f<KP>(b / Lrow[j], j);
-        if (lane == j)
-            b = yj;
-        else if (lane > j)
-            b = fmaf(-Lrow[j], yj, b);
-    }
-    // backward: L^T x = y
-#pragma unroll
-    for (int j = KP - 1; j >= 0; --j)
-    {
-        const float xj = shfl_f<KP>(b / Lcol[j], j);
-        if (lane == j)
-            b = xj;
-        else if (lane < j)
-            b = fmaf(-Lcol[j], xj, b);
-    }
-    return b;
-}
-
-template <int KP, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_lle_small(const void* X, int dtype, int64_t N, int D, int64_t ldx,
-                                                          const int32_t* __restrict__ idx, int k, double klle_shift,
-                                                          double* __restrict__ W, unsigned* err)
-{
-    constexpr int NB4 = KP / 4;
-    constexpr int NBLK = NB4 * (NB4 + 1) / 2;
-    constexpr int DG = (32 / NBLK) >= 3 ? 3 : ((32 / NBLK) >= 1 ? (32 / NBLK) : 1);
-    constexpr int ITEMS = NBLK * DG;
-    constexpr int PER = (ITEMS + 31) / 32;
-    constexpr int NPL = (KP + 31) / 32;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    LleSmallSmem<KP>& S = reinterpret_cast<LleSmallSmem<KP>*>(smem_raw)[wib];
-    const int64_t nwarps = (int64_t)gridDim.x * WARPS;
-
-    // work items of this lane: (block I, J, dimension range)
-    int iI[PER], iJ[PER], iG[PER], d_lo[PER], d_hi[PER];
-#pragma unroll
-    for (int m = 0; m < PER; ++m)
-    {
-        const int it = lane + 32 * m;
-        const int blk = (it < ITEMS) ? it % NBLK : 0;
-        const int g = (it < ITEMS) ? it / NBLK : 0;
-        int b = blk, I = 0;
-        while (b >= NB4 - I)
-        {
-            b -= NB4 - I;
-            ++I;
-        }
-        iI[m] = I;
-        iJ[m] = I + b;
-        iG[m] = g;
-        const int span = (32 + DG - 1) / DG;
-        d_lo[m] = (it < ITEMS) ? g * span : 0;
-        d_hi[m] = (it < ITEMS) ? min(32, g * span + span) : 0;
-    }
-
-    for (int64_t i = (int64_t)blockIdx.x * WARPS + wib; i < N; i += nwarps)
-    {
-        int nb[NPL];
-#pragma unroll
-        for (int s = 0; s < NPL; ++s)
-        {
-            const int a = lane + 32 * s;
-            nb[s] = (a < k) ? idx[i * k + a] : 0;
-            if (a < k && (nb[s] < 0 || nb[s] >= N))
-            {
-                atomicOr(err, DEV_ERR_BOUNDS);
-                nb[s] = 0;
-            }
-            if (a < KP)
-                S.nb[a] = nb[s];
-        }
-        __syncwarp();
-        // ---- FP32 Gram ----
-        float acc[PER][16];
-#pragma unroll
-        for (int m = 0; m < PER; ++m)
-#pragma unroll
-            for (int t = 0; t < 16; ++t)
-                acc[m][t] = 0.f;
-        for (int d0 = 0; d0 < D; d0 += 32)
-        {
-            const int d = d0 + lane;
-            const double xi = (d < D) ? ldx_elem(X, dtype, i * ldx + d) : 0.0;
-#pragma unroll 4
-            for (int a = 0; a < KP; ++a)
-            {
-                const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
-                float v = 0.f;
-                if (a < k && d < D)
-                    v = (float)(ldx_elem(X, dtype, (int64_t)nba * ldx + d) - xi);
-                S.Z[a][lane] = v;
-            }
-            __syncwarp();
-#pragma unroll
-            for (int m = 0; m < PER; ++m)
-            {
-                if (lane + 32 * m < ITEMS)
-                {
-                    const int I4 = 4 * iI[m], J4 = 4 * iJ[m];
-                    for (int dd = d_lo[m]; dd < d_hi[m]; ++dd)
-                    {
-                        float av[4], bv[4];
-#pragma unroll
-                        for (int t = 0; t < 4; ++t)
-                        {
-                            av[t] = S.Z[I4 + t][dd];
-                            bv[t] = S.Z[J4 + t][dd];
-                        }
-#pragma unroll
-                        for (int r = 0; r < 4; ++r)
-#pragma unroll
-                            for (int c = 0; c < 4; ++c)
-                                acc[m][r * 4 + c] = fmaf(av[r], bv[c], acc[m][r * 4 + c]);
-                    }
-                }
-            }
-            __syncwarp();
-        }
-        // partial blocks -> shared memory (entry (min, max) convention)
-        for (int t = lane; t < DG * KP * (KP + 1); t += 32)
-            (&S.P[0][0][0])[t] = 0.f;
-        __syncwarp();
-#pragma unroll
-        for (int m = 0; m < PER; ++m)
-            if (lane + 32 * m < ITEMS)
-            {
-                const int I4 = 4 * iI[m], J4 = 4 * iJ[m];
-#pragma unroll
-                for (int r = 0; r < 4; ++r)
-#pragma unroll
-                    for (int c = 0; c < 4; ++c)
-                    {
-                        const int a = I4 + r, b = J4 + c;
-                        if (a <= b)
-                            S.P[iG[m]][a][b] = acc[m][r * 4 + c];
-                    }
-            }
-        __syncwarp();
-        // row r of C in lane r
-        float L[KP];
-        float diag = 0.f;
-#pragma unroll
-        for (int c = 0; c < KP; ++c)
-        {
-            const int lo = min(lane, c), hi = max(lane, c);
-            float v = 0.f;
-            if (lane < KP)
-#pragma unroll
-                for (int g = 0; g < DG; ++g)
-                    v += S.P[g][lo][hi];
-            L[c] = v;
-            if (c == lane)
-                diag = v;
-        }
-        float trace = (lane < k) ? diag : 0.f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            trace += __shfl_xor_sync(0xffffffffu, trace, o);
-        const float shift = (float)klle_shift * trace;
-#pragma unroll
-        for (int c = 0; c < KP; ++c)
-            if (c == lane)
-                L[c] = (lane < k) ? L[c] + shift : 1.f;  // padding: identity
-        // ---- Cholesky in registers (lane r: row r) ----
-#pragma unroll
-        for (int j = 0; j < KP; ++j)
-        {
-            const float ljj = sqrtf(fmaxf(shfl_f<KP>(L[j], j), FLT_MIN));
-            if (lane > j)
-                L[j] = L[j] / ljj;
-            else if (lane == j)
-                L[j] = ljj;
-#pragma unroll
-            for (int c = j + 1; c < KP; ++c)
-            {
-                const float lcj = shfl_f<KP>(L[j], c);
-                if (lane >= c)
-                    L[c] = fmaf(-L[j], lcj, L[c]);
-            }
-        }
-        // columns of L (lane r: column r), via shared memory
-        if (lane < KP)
-#pragma unroll
-            for (int c = 0; c < KP; ++c)
-                S.Lt[c][lane] = (c <= lane) ? L[c] : 0.f;
-        __syncwarp();
-        float Lc[KP];
-#pragma unroll
-        for (int m = 0; m < KP; ++m)
-            Lc[m] = (lane < KP) ? S.Lt[lane][m] : 1.f;  // Lc[m] = L[m][lane]
-        __syncwarp();
-        if (lane >= KP)
-#pragma unroll
-            for (int c = 0; c < KP; ++c)
-                L[c] = 1.f;
-        float w = chol_solve_reg<KP>(L, Lc, (lane < k) ? 1.f : 0.f, lane);
-
-        // ---- float-float residual refinement ----
-        const int iters = (k > D) ? 2 : 1;
-        for (int itr = 0; itr < iters; ++itr)
-        {
-            if (lane < KP)
-                S.w[lane] = (lane < k) ? w : 0.f;
-            __syncwarp();
-            ff part[KP];
-#pragma unroll
-            for (int a = 0; a < KP; ++a)
-                part[a] = ff_zero();
-            ff tr = ff_zero();
-            for (int d0 = 0; d0 < D; d0 += 32)
-            {
-                const int d = d0 + lane;
-                if (d < D)
-                {
-                    const double xi = ldx_elem(X, dtype, i * ldx + d);
-                    float zh[KP], zl[KP];
-#pragma unroll
-                    for (int a = 0; a < KP; ++a)
-                    {
-                        const int nba = S.nb[a];
-                        zh[a] = 0.f;
-                        zl[a] = 0.f;
-                        if (a < k)
-                        {
-                            const double z = ldx_elem(X, dtype, (int64_t)nba * ldx + d) - xi;
-                            zh[a] = (float)z;
-                            zl[a] = (float)(z - (double)zh[a]);
-                        }
-                    }
-                    ff v = ff_zero();
-#pragma unroll
-                    for (int b = 0; b < KP; ++b)
-                        v = ff_fma(v, S.w[b], 0.f, zh[b], zl[b]);
-#pragma unroll
-                    for (int a = 0; a < KP; ++a)
-                    {
-                        part[a] = ff_fma(part[a], zh[a], zl[a], v.hi, v.lo);
-                        tr = ff_fma(tr, zh[a], zl[a], zh[a], zl[a]);
-                    }
-                }
-            }
-            // warp all-reduce of the KP partial sums and of the trace
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-            {
-#pragma unroll
-                for (int a = 0; a < KP; ++a)
-                    part[a] = ff_add(part[a], ff_shfl_xor(part[a], o));
-                tr = ff_add(tr, ff_shfl_xor(tr, o));
-            }
-            const double shift_true = klle_shift * ff_to_double(tr);
-            double res = 0.0;
-#pragma unroll
-            for (int a = 0; a < KP; ++a)
-                if (a == lane)
-                    res = 1.0 - ff_to_double(part[a]) - shift_true * (double)w;
-            const float rr = (lane < k) ? (float)res : 0.f;
-            const float delta = chol_solve_reg<KP>(L, Lc, rr, lane);
-            if (lane < k)
-                w += delta;
-            __syncwarp();
-        }
-        // ---- normalise and store ----
-        double sum = (lane < k) ? (double)w : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        if (lane < k)
-            W[i * k + lane] = (double)w / sum;
-        __syncwarp();
-    }
-}
-
-template <int KP, int WARPS>
-void launch_small(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
-                  double klle_shift, double* W)
-{
-    const size_t smem = sizeof(LleSmallSmem<KP>) * WARPS;
-    TK_CUDA(cudaFuncSetAttribute(k_lle_small<KP, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t want = (N + WARPS - 1) / WARPS;
-    const int grid = (int)std::min<int64_t>(want, (int64_t)ctx->num_sms * 16);
-    k_lle_small<KP, WARPS><<<grid, WARPS * 32, smem, ctx->stream>>>(X, dtype, N, D, ldx, idx, k, klle_shift, W,
-                                                                     ctx->dev_err);
-    TK_CHECK_LAUNCH();
-}
-
 template <int KP, int WARPS>
 void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
             double klle_shift, double* W)
@@ -671,9 +372,9 @@ void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_
                  double klle_shift, double* W)
 {
     if (k <= 16)
-        launch_small<16, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
+        launch<16, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
     else if (k <= 32)
-        launch_small<32, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
+        launch<32, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
     else if (k <= 64)
         launch<64, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
     else if (k <= 128)

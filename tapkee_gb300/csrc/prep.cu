@@ -2,17 +2,18 @@
 //
 // Steps (all on the context stream, no host synchronisation):
 //   1. column mean mu (FP64, deterministic two-level reduction);
-//   2. a 16-dimensional random sketch s_i = G^T (x_i - mu) of every point, its
-//      16x16 covariance (deterministic per-warp partials) and R = max |x_i - mu|;
-//   3. the 3 leading principal directions of the sketch (subspace iteration on
-//      one warp) and the 3-D projection of every point;
-//   4. a Morton-bucket counting sort of the projections, giving perm
-//      (sorted position -> original index): points close in space get close
-//      positions, so a query block finds its neighbours in the first candidate
-//      tiles it visits and its top-K threshold tightens immediately;
+//   2. a 16-dimensional random sketch s_i = G^T (x_i - mu) of every point (FP32),
+//      its 16x16 covariance (deterministic per-block partials) and an estimate of
+//      max |x_i - mu| that sets the fp16 scale of the tensor screen;
+//   3. the 3 leading principal directions of the sketch (subspace iteration in one
+//      block) and the 3-D projection of every point;
+//   4. a Morton-bucket counting sort of the projections (about four points per
+//      bucket), giving perm (sorted position -> original index): points close in
+//      space get close positions, so a query block finds its neighbours in the
+//      first candidate tiles it visits and its top-K threshold tightens at once;
 //   5. the screening layout in sorted order: centred FP32 rows xc (Dp-padded),
-//      their squared norms, fp16 hi/lo splits of 2^s * xc for the tensor screen,
-//      and the exact FP64 kernel diagonal k(i,i) (original order) for the re-rank.
+//      their squared norms (float-float accumulated), fp16 hi/lo splits of
+//      2^s * xc and the norm column for the tensor screen, and R = max |xc|.
 // The ordering only affects speed: the re-rank and certification make the
 // final neighbour sets independent of it.
 #include <cuda_fp16.h>
@@ -20,6 +21,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "ff.cuh"
 #include "tk_internal.h"
 
 namespace tk {
@@ -27,17 +29,14 @@ namespace {
 
 constexpr int SKETCH = 16;
 
+__device__ __forceinline__ float ldx_f(const void* X, int dtype, int64_t off)
+{
+    return dtype == TK_F64 ? (float)reinterpret_cast<const double*>(X)[off] : reinterpret_cast<const float*>(X)[off];
+}
+
 __device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
 {
     return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
-}
-
-__device__ __forceinline__ double warp_sum_d(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
 }
 
 __device__ __forceinline__ float warp_sum_f(float v)
@@ -82,14 +81,14 @@ __global__ void k_colsum_partial(const void* X, int dtype, int64_t N, int D, int
     }
 }
 
-__global__ void k_colsum_final(const double* partial, int nblk, int D, int64_t N, double* mean)
+__global__ void k_colsum_final(const double* partial, int nblk, int D, int64_t N, float* meanf)
 {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < D; c += gridDim.x * blockDim.x)
     {
         double s = 0.0;
         for (int b = 0; b < nblk; ++b)
             s += partial[(int64_t)b * D + c];
-        mean[c] = s / (double)N;
+        meanf[c] = (float)(s / (double)N);
     }
 }
 
@@ -111,14 +110,14 @@ __global__ void k_gen_sketch(int D, float* G)
         G[t] = sketch_g(t / SKETCH, t % SKETCH);
 }
 
-// 2. sketch covariance partials per warp + R = max |x - mu|.
-__global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx, const double* mean,
-                         const float* G, double* cov_partial /* nwarps x 136 */, unsigned* rmax_ord)
+// 2. sketch covariance per block + max |x - mu| estimate (FP32; only the order
+// of the points and the fp16 scale depend on it).
+__global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx, const float* meanf, const float* G,
+                         float* cov_partial /* blocks x 136 */, unsigned* rmax_ord)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    // upper-triangle pairs (a<=b) of the 16x16 covariance owned by this lane: p = lane + 32 m
     int pa[5], pb[5];
 #pragma unroll
     for (int m = 0; m < 5; ++m)
@@ -134,7 +133,7 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
         pa[m] = a;
         pb[m] = a + p;
     }
-    double acc[5] = {0, 0, 0, 0, 0};
+    float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     float rloc = 0.f;
     for (int64_t i = warp; i < N; i += nwarps)
     {
@@ -142,12 +141,11 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
 #pragma unroll
         for (int j = 0; j < SKETCH; ++j)
             s[j] = 0.f;
-        double r2 = 0.0;
+        float r2 = 0.f;
         for (int d = lane; d < D; d += 32)
         {
-            const double v = ldx_elem(X, dtype, i * ldx + d) - mean[d];
-            r2 += v * v;
-            const float vf = (float)v;
+            const float vf = ldx_f(X, dtype, i * ldx + d) - meanf[d];
+            r2 = fmaf(vf, vf, r2);
             const float4* g = reinterpret_cast<const float4*>(G + (size_t)d * SKETCH);
 #pragma unroll
             for (int q = 0; q < SKETCH / 4; ++q)
@@ -159,8 +157,8 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
                 s[4 * q + 3] = fmaf(gq.w, vf, s[4 * q + 3]);
             }
         }
-        r2 = warp_sum_d(r2);
-        rloc = fmaxf(rloc, (float)sqrt(r2));
+        r2 = warp_sum_f(r2);
+        rloc = fmaxf(rloc, sqrtf(r2));
 #pragma unroll
         for (int j = 0; j < SKETCH; ++j)
             s[j] = warp_sum_f(s[j]);
@@ -174,11 +172,10 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
                 sa = (j == pa[m]) ? s[j] : sa;
                 sb = (j == pb[m]) ? s[j] : sb;
             }
-            acc[m] += (double)sa * (double)sb;
+            acc[m] = fmaf(sa, sb, acc[m]);
         }
     }
-    // per-block partial (fixed order over the block's 8 warps)
-    __shared__ double red[8][160];
+    __shared__ float red[8][160];
     const int wib = threadIdx.x >> 5;
 #pragma unroll
     for (int m = 0; m < 5; ++m)
@@ -190,7 +187,7 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
     __syncthreads();
     for (int p = threadIdx.x; p < 136; p += blockDim.x)
     {
-        double sacc = 0.0;
+        float sacc = 0.f;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
             sacc += red[w][p];
         cov_partial[(int64_t)blockIdx.x * 136 + p] = sacc;
@@ -199,20 +196,19 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
         atomicMax(rmax_ord, f2ord(rloc));
 }
 
-// 3. top-3 principal directions of the 16x16 sketch covariance by subspace
-// iteration (one warp), then H = G V3 (D x 3) for the projection.
-__global__ void k_pca3(const double* cov_partial, int64_t nwarps, int D, float* H, const unsigned* rmax_ord,
-                       float* rmax)
+// 3. top-3 principal directions of the sketch covariance by subspace iteration
+// (one block, FP32), then H = G V3 (D x 3) for the projection.
+__global__ void k_pca3(const float* cov_partial, int nblk, int D, float* H)
 {
-    __shared__ double C[SKETCH][SKETCH];
-    __shared__ double V[SKETCH][3];
-    __shared__ double T[SKETCH][3];
+    __shared__ float C[SKETCH][SKETCH];
+    __shared__ float V[SKETCH][3];
+    __shared__ float T[SKETCH][3];
     const int t = threadIdx.x;
     for (int p = t; p < 136; p += blockDim.x)
     {
-        double s = 0.0;
-        for (int64_t w = 0; w < nwarps; ++w)
-            s += cov_partial[w * 136 + p];
+        float s = 0.f;
+        for (int w = 0; w < nblk; ++w)
+            s += cov_partial[(int64_t)w * 136 + p];
         int a = 0, rem = p;
         while (rem >= SKETCH - a)
         {
@@ -222,42 +218,43 @@ __global__ void k_pca3(const double* cov_partial, int64_t nwarps, int D, float* 
         C[a][a + rem] = s;
         C[a + rem][a] = s;
     }
-    if (t < SKETCH)
-        for (int c = 0; c < 3; ++c)
-            V[t][c] = (t % 3 == c) ? 1.0 : 0.01 * (t + 1) * (c + 1);
+    if (t < SKETCH * 3)
+        V[t / 3][t % 3] = ((t / 3) % 3 == t % 3) ? 1.f : 0.01f * (t / 3 + 1) * (t % 3 + 1);
     __syncthreads();
-    for (int it = 0; it < 30; ++it)
+    for (int it = 0; it < 24; ++it)
     {
-        if (t < SKETCH)
-            for (int c = 0; c < 3; ++c)
-            {
-                double s = 0.0;
-                for (int j = 0; j < SKETCH; ++j)
-                    s += C[t][j] * V[j][c];
-                T[t][c] = s;
-            }
+        if (t < SKETCH * 3)
+        {
+            const int i = t / 3, c = t % 3;
+            float s = 0.f;
+            for (int j = 0; j < SKETCH; ++j)
+                s = fmaf(C[i][j], V[j][c], s);
+            T[i][c] = s;
+        }
         __syncthreads();
         if (t == 0)
         {
-            // modified Gram-Schmidt on the 3 columns of T
             for (int c = 0; c < 3; ++c)
             {
                 for (int p = 0; p < c; ++p)
                 {
-                    double dot = 0.0;
+                    float dot = 0.f;
                     for (int j = 0; j < SKETCH; ++j)
-                        dot += T[j][c] * T[j][p];
+                        dot = fmaf(T[j][c], T[j][p], dot);
                     for (int j = 0; j < SKETCH; ++j)
-                        T[j][c] -= dot * T[j][p];
+                        T[j][c] = fmaf(-dot, T[j][p], T[j][c]);
                 }
-                double nrm = 0.0;
+                float nrm = 0.f;
                 for (int j = 0; j < SKETCH; ++j)
-                    nrm += T[j][c] * T[j][c];
-                nrm = sqrt(nrm);
+                    nrm = fmaf(T[j][c], T[j][c], nrm);
+                const float inv = nrm > 0.f ? rsqrtf(nrm) : 0.f;
                 for (int j = 0; j < SKETCH; ++j)
-                    V[j][c] = nrm > 0.0 ? T[j][c] / nrm : (j == c ? 1.0 : 0.0);
+                    T[j][c] = nrm > 0.f ? T[j][c] * inv : (j == c ? 1.f : 0.f);
             }
         }
+        __syncthreads();
+        if (t < SKETCH * 3)
+            V[t / 3][t % 3] = T[t / 3][t % 3];
         __syncthreads();
     }
     for (int d = t; d < D; d += blockDim.x)
@@ -265,15 +262,13 @@ __global__ void k_pca3(const double* cov_partial, int64_t nwarps, int D, float* 
         {
             float s = 0.f;
             for (int j = 0; j < SKETCH; ++j)
-                s = fmaf(sketch_g(d, j), (float)V[j][c], s);
+                s = fmaf(sketch_g(d, j), V[j][c], s);
             H[d * 3 + c] = s;
         }
-    if (t == 0)
-        *rmax = (*rmax_ord == 0u) ? 0.f : ord2f(*rmax_ord);
 }
 
 // projection p_i = H^T (x_i - mu) and its bounding box
-__global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ldx, const double* mean,
+__global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ldx, const float* meanf,
                           const float* H, float* proj, unsigned* bbox /* 6: min x3, max x3 */)
 {
     const int lane = threadIdx.x & 31;
@@ -285,7 +280,7 @@ __global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ld
         float p[3] = {0.f, 0.f, 0.f};
         for (int d = lane; d < D; d += 32)
         {
-            const float v = (float)(ldx_elem(X, dtype, i * ldx + d) - mean[d]);
+            const float v = ldx_f(X, dtype, i * ldx + d) - meanf[d];
             p[0] = fmaf(H[d * 3 + 0], v, p[0]);
             p[1] = fmaf(H[d * 3 + 1], v, p[1]);
             p[2] = fmaf(H[d * 3 + 2], v, p[2]);
@@ -379,34 +374,34 @@ __global__ void k_scatter(const unsigned* bucket, int64_t N, unsigned* offs, int
 
 // 5. screening layout in sorted order (one warp per row).
 __global__ void k_layout(const void* X, int dtype, int64_t N, int64_t Npad, int D, int Dp, int64_t ldx,
-                         const double* mean, const int32_t* perm, const float* rmax, float* xc, float* nrm,
-                         __half* xh, __half* xl, __half* xn, double* kdiag, float* scale_out)
+                         const float* meanf, const int32_t* perm, const unsigned* rest_ord, float* xc, float* nrm,
+                         __half* xh, __half* xl, __half* xn, unsigned* rmax_ord, float* scale_out)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    // xh/xl hold xc * 2^s with R * 2^s < 2^14 (fp16 max is 65504)
+    // xh/xl hold xc * 2^s with R * 2^s < 2^14 (fp16 max is 65504); the estimate
+    // of R gets a 1% margin
     int e = 0;
-    const float R = *rmax;
-    frexpf(R > 0.f ? R : 1.f, &e);
+    const float Rest = ord2f(*rest_ord) * 1.01f;
+    frexpf(Rest > 0.f ? Rest : 1.f, &e);
     const int s = 14 - e;
     const float scale = ldexpf(1.f, s);
     if (warp == 0 && lane == 0 && scale_out)
         *scale_out = (float)s;
+    float rloc = 0.f;
     for (int64_t p = warp; p < Npad; p += nwarps)
     {
         const bool valid = p < N;
         const int64_t i = valid ? perm[p] : 0;
-        double n2 = 0.0, k2 = 0.0;
+        ff n2 = ff_zero();
         for (int d = lane; d < Dp; d += 32)
         {
             float v = 0.f;
             if (valid && d < D)
             {
-                const double x = ldx_elem(X, dtype, i * ldx + d);
-                k2 += x * x;
-                v = (float)(x - mean[d]);
-                n2 += (double)v * (double)v;
+                v = ldx_f(X, dtype, i * ldx + d) - meanf[d];
+                n2 = ff_add(n2, two_prod(v, v));
             }
             xc[p * Dp + d] = v;
             if (xh)
@@ -418,14 +413,14 @@ __global__ void k_layout(const void* X, int dtype, int64_t N, int64_t Npad, int 
                 xl[p * Dp + d] = l;
             }
         }
-        n2 = warp_sum_d(n2);
-        k2 = warp_sum_d(k2);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            n2 = ff_add(n2, ff_shfl_xor(n2, o));
+        const double n2d = ff_to_double(n2);
+        if (valid)
+            rloc = fmaxf(rloc, (float)sqrt(n2d) * 1.000001f);
         if (lane == 0)
-        {
-            nrm[p] = valid ? (float)n2 : __int_as_float(0x7f800000);
-            if (valid)
-                kdiag[i] = k2;
-        }
+            nrm[p] = valid ? (float)n2d : __int_as_float(0x7f800000);
         if (xn && lane < 16)
         {
             // -|2^s xc|^2 / 2^14 as fp16 hi + lo: the tensor screen adds 2^13 (h + l)
@@ -434,13 +429,21 @@ __global__ void k_layout(const void* X, int dtype, int64_t N, int64_t Npad, int 
             __half v = __float2half_rn(0.f);
             if (valid && lane < 2)
             {
-                const double t = -n2 * ldexp(1.0, 2 * s) * (1.0 / 16384.0);
-                const __half h = __double2half(t);
-                v = (lane == 0) ? h : __double2half(t - (double)__half2float(h));
+                const float f = ldexpf(1.f, 2 * s - 14);
+                const float t_hi = -n2.hi * f, t_lo = -n2.lo * f;
+                const __half h = __float2half_rn(t_hi);
+                v = (lane == 0) ? h : __float2half_rn((t_hi - __half2float(h)) + t_lo);
             }
             xn[p * 16 + lane] = v;
         }
     }
+    if (lane == 0 && rloc > 0.f)
+        atomicMax(rmax_ord, f2ord(rloc));
+}
+
+__global__ void k_finalize_r(const unsigned* rmax_ord, float* rmax)
+{
+    rmax[0] = (*rmax_ord == 0u) ? 0.f : ord2f(*rmax_ord);
 }
 
 } // namespace
@@ -459,17 +462,17 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     const int nblk = (int)std::min<int64_t>(4 * sms, std::max<int64_t>(1, (N + 63) / 64));
     const int64_t rpb = (N + nblk - 1) / nblk;
     double* partial = (double*)ctx->scratch.get("prep.partial", sizeof(double) * (size_t)nblk * D);
-    double* mean = (double*)ctx->scratch.get("prep.mean", sizeof(double) * D);
+    float* meanf = (float*)ctx->scratch.get("prep.mean", sizeof(float) * D);
     k_colsum_partial<<<nblk, 256, 0, st>>>(X, dtype, N, D, ldx, rpb, partial);
     TK_CHECK_LAUNCH();
-    k_colsum_final<<<(D + 255) / 256, 256, 0, st>>>(partial, nblk, D, N, mean);
+    k_colsum_final<<<(D + 255) / 256, 256, 0, st>>>(partial, nblk, D, N, meanf);
     TK_CHECK_LAUNCH();
 
-    // 2. sketch covariance and R
+    // 2. sketch covariance and the R estimate
     const int sk_blocks = 2 * sms;
-    double* covp = (double*)ctx->scratch.get("prep.covp", sizeof(double) * sk_blocks * 136);
+    float* covp = (float*)ctx->scratch.get("prep.covp", sizeof(float) * sk_blocks * 136);
+    // small[0] = R estimate (ordered), small[1] = R (ordered), small[8..13] = bbox
     unsigned* small = (unsigned*)ctx->scratch.get("prep.small", 64 * sizeof(unsigned));
-    // small[0] = rmax ord, small[8..13] = bbox
     float* rmax = (float*)ctx->scratch.get("prep.rmax", 2 * sizeof(float));
     unsigned init[16];
     for (int c = 0; c < 16; ++c)
@@ -479,20 +482,20 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     float* G = (float*)ctx->scratch.get("prep.G", sizeof(float) * SKETCH * (size_t)D);
     k_gen_sketch<<<(D * SKETCH + 255) / 256, 256, 0, st>>>(D, G);
     TK_CHECK_LAUNCH();
-    k_sketch<<<sk_blocks, 256, 0, st>>>(X, dtype, N, D, ldx, mean, G, covp, small);
+    k_sketch<<<sk_blocks, 256, 0, st>>>(X, dtype, N, D, ldx, meanf, G, covp, small);
     TK_CHECK_LAUNCH();
 
     // 3. principal directions and projection
     float* H = (float*)ctx->scratch.get("prep.H", sizeof(float) * 3 * (size_t)D);
-    k_pca3<<<1, 256, 0, st>>>(covp, sk_blocks, D, H, small, rmax);
+    k_pca3<<<1, 64, 0, st>>>(covp, sk_blocks, D, H);
     TK_CHECK_LAUNCH();
     float* proj = (float*)ctx->scratch.get("prep.proj", sizeof(float) * 3 * (size_t)N);
-    k_project<<<2 * sms, 256, 0, st>>>(X, dtype, N, D, ldx, mean, H, proj, small + 8);
+    k_project<<<2 * sms, 256, 0, st>>>(X, dtype, N, D, ldx, meanf, H, proj, small + 8);
     TK_CHECK_LAUNCH();
 
-    // 4. Morton-bucket counting sort (about one point per bucket)
+    // 4. Morton-bucket counting sort (about four points per bucket)
     int bits = 10;
-    while (bits < 24 && ((int64_t)1 << bits) < N)
+    while (bits < 24 && ((int64_t)1 << (bits + 2)) < N)
         ++bits;
     const int nb = 1 << bits;
     const int shift = 30 - bits;
@@ -510,7 +513,6 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     // 5. layout
     P.xc = (float*)ctx->scratch.get("prep.xc", sizeof(float) * (size_t)P.Npad * P.Dp);
     P.nrm = (float*)ctx->scratch.get("prep.nrm", sizeof(float) * (size_t)P.Npad);
-    P.kdiag = (double*)ctx->scratch.get("prep.kdiag", sizeof(double) * (size_t)N);
     if (tensor)
     {
         P.xh = (uint16_t*)ctx->scratch.get("prep.xh", sizeof(uint16_t) * (size_t)P.Npad * P.Dp);
@@ -522,8 +524,10 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
         P.xh = P.xl = P.xn = nullptr;
     }
     P.rmax = rmax;
-    k_layout<<<4 * sms, 256, 0, st>>>(X, dtype, N, P.Npad, D, P.Dp, ldx, mean, P.perm, rmax, P.xc, P.nrm,
-                                      (__half*)P.xh, (__half*)P.xl, (__half*)P.xn, P.kdiag, rmax + 1);
+    k_layout<<<4 * sms, 256, 0, st>>>(X, dtype, N, P.Npad, D, P.Dp, ldx, meanf, P.perm, small, P.xc, P.nrm,
+                                      (__half*)P.xh, (__half*)P.xl, (__half*)P.xn, small + 1, rmax + 1);
+    TK_CHECK_LAUNCH();
+    k_finalize_r<<<1, 1, 0, st>>>(small + 1, rmax);
     TK_CHECK_LAUNCH();
 }
 

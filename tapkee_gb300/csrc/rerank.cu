@@ -73,14 +73,25 @@ __device__ __forceinline__ double exact_d2(const void* X, int dtype, int64_t ldx
     return ff_to_double(acc) + (double)cross;
 }
 
+constexpr int RR_CHUNK = 64;  // dimensions staged per pass
+constexpr int RR_WARPS = 4;  // 4 x 8.6 KB static shared memory per block
+
+struct RerankSmem
+{
+    float q[RR_CHUNK];
+    float rows[32][RR_CHUNK + 1];
+};
+
 template <int KC>
-__global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k, const int32_t* perm,
-                         const double* kdiag, const float* nrm, const float* rmax, const int32_t* cand_idx,
-                         const float* cand_val, float c1, float c2, int32_t* idx_out, double* d2_out,
-                         int32_t* failed, double* failed_ub, unsigned* nfailed)
+__global__ void __launch_bounds__(RR_WARPS * 32)
+    k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k, const int32_t* perm, const float* nrm,
+             const float* rmax, const int32_t* cand_idx, const float* cand_val, float c1, float c2,
+             int32_t* idx_out, double* d2_out, int32_t* failed, double* failed_ub, unsigned* nfailed)
 {
     constexpr int PER = (KC + 31) / 32;
+    __shared__ RerankSmem smem[RR_WARPS];
     const int lane = threadIdx.x & 31;
+    RerankSmem& S = smem[threadIdx.x >> 5];
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const double R = (double)*rmax;
@@ -95,18 +106,55 @@ __global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N
             const int slot = lane + 32 * s;
             d[s] = __longlong_as_double(0x7ff0000000000000LL);  // +inf
             j[s] = 0x7fffffff - slot;                          // distinct, ranks last
+            int64_t jj = -1;
             if (slot < KC)
             {
                 const int c = cand_idx[p * KC + slot];
                 if (c >= 0 && c < N)
                 {
-                    const int64_t jj = perm[c];
-                    if (jj != i)
-                    {
-                        d[s] = exact_d2(X, dtype, ldx, D, i, jj);
-                        j[s] = (int)jj;
-                    }
+                    jj = perm[c];
+                    if (jj == i)
+                        jj = -1;
                 }
+            }
+            if (dtype == TK_F64)
+            {
+                if (jj >= 0)
+                {
+                    d[s] = exact_d2(X, dtype, ldx, D, i, jj);
+                    j[s] = (int)jj;
+                }
+                continue;
+            }
+            // float32: stage the 32 candidate rows through shared memory with
+            // coalesced loads, then each lane sums its own row in float-float
+            const float* Xf = reinterpret_cast<const float*>(X);
+            ff acc = ff_zero();
+            float cross = 0.f;
+            for (int d0 = 0; d0 < D; d0 += RR_CHUNK)
+            {
+                const int dn = min(RR_CHUNK, D - d0);
+                for (int t = lane; t < RR_CHUNK; t += 32)
+                    S.q[t] = (t < dn) ? Xf[i * ldx + d0 + t] : 0.f;
+                for (int r = 0; r < 32; ++r)
+                {
+                    const int64_t row = __shfl_sync(0xffffffffu, jj, r);
+                    for (int t = lane; t < RR_CHUNK; t += 32)
+                        S.rows[r][t] = (row >= 0 && t < dn) ? Xf[row * ldx + d0 + t] : 0.f;
+                }
+                __syncwarp();
+                for (int dd = 0; dd < dn; ++dd)
+                {
+                    const ff z = two_sum(S.rows[lane][dd], -S.q[dd]);
+                    acc = ff_add(acc, two_prod(z.hi, z.hi));
+                    cross = fmaf(2.f * z.hi, z.lo, cross);
+                }
+                __syncwarp();
+            }
+            if (jj >= 0)
+            {
+                d[s] = ff_to_double(acc) + (double)cross;
+                j[s] = (int)jj;
             }
         }
         // rank of every element among the KC (d, j) keys
@@ -160,7 +208,7 @@ __global__ void k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N
 
 // Exact fallback: one CTA per failed row (persistent over the failed list).
 __global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k,
-                                                  const int32_t* perm, const double* kdiag, const int32_t* failed,
+                                                  const int32_t* perm, const int32_t* failed,
                                                   const double* failed_ub, const unsigned* nfailed,
                                                   int32_t* idx_out, double* d2_out, unsigned* err)
 {
@@ -173,11 +221,9 @@ __global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int6
         const int64_t p = failed[f];
         const int64_t i = perm[p];
         const double ub = failed_ub[f];
-        const double kii = kdiag[i];
         // FP32 direct-difference filter with a relative slack covering its error
         const double slack = (double)(D + 8) * 1.1920928955078125e-07;
         const float thr = (float)(ub * (1.0 + slack)) * 1.0000005f + 1e-30f;
-        (void)kii;
         if (threadIdx.x == 0)
             cnt = 0;
         __syncthreads();
@@ -267,7 +313,7 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
     TK_CUDA(cudaMemsetAsync(nfailed, 0, 16, st));
     const int blocks = 8 * ctx->num_sms;
 #define TK_RERANK(KCV)                                                                                         \
-    k_rerank<KCV><<<blocks, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, P.nrm, P.rmax, cand_idx,    \
+    k_rerank<KCV><<<blocks, RR_WARPS * 32, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.nrm, P.rmax, cand_idx,    \
                                           cand_val, eps_c1, eps_c2, idx_out, d2_out, failed, failed_ub, nfailed)
     if (kc == 32)
         TK_RERANK(32);
@@ -280,7 +326,7 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
     else
         throw Error(TK_ERR_INTERNAL, "rerank: unsupported candidate count");
     TK_CHECK_LAUNCH();
-    k_fallback<<<ctx->num_sms, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.kdiag, failed, failed_ub, nfailed,
+    k_fallback<<<ctx->num_sms, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, failed, failed_ub, nfailed,
                                              idx_out, d2_out, ctx->dev_err);
     TK_CHECK_LAUNCH();
     TK_CUDA(cudaMemcpyAsync(ctx->host_i64, nfailed, sizeof(unsigned), cudaMemcpyDeviceToHost, st));

@@ -78,8 +78,7 @@ struct Prepared
     uint16_t* xl = nullptr;     // Npad x Dp fp16 low parts
     uint16_t* xn = nullptr;     // Npad x 16 fp16: hi/lo of -|2^s xc|^2 / 2^14 (cols 0,1), tensor screen
     int32_t* perm = nullptr;    // sorted position -> original index
-    double* kdiag = nullptr;    // N exact k(i,i) in FP64, original order
-    float* rmax = nullptr;      // device scalar: max |xc|
+    float* rmax = nullptr;      // device scalars: [0] R = max |xc|, [1] fp16 scale exponent s
     float scale_log2 = 0.f;     // xh/xl hold xc * 2^scale_log2
 };
 
