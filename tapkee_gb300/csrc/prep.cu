@@ -2,11 +2,11 @@
 //
 // Steps (all on the context stream, no host synchronisation):
 //   1. column mean mu (FP64, deterministic two-level reduction);
-//   2. a 16-dimensional random sketch s_i = G^T (x_i - mu) of every point (FP32),
-//      its 16x16 covariance (deterministic per-block partials) and an estimate of
-//      max |x_i - mu| that sets the fp16 scale of the tensor screen;
+//   2. a 16-dimensional random sketch s_i = G^T (x_i - mu) of a subsample of the
+//      points (FP32) and its 16x16 covariance (deterministic per-block partials);
 //   3. the 3 leading principal directions of the sketch (subspace iteration in one
-//      block) and the 3-D projection of every point;
+//      block), the 3-D projection of every point and an estimate of
+//      max |x_i - mu| that sets the fp16 scale of the tensor screen;
 //   4. a Morton-bucket counting sort of the projections (about four points per
 //      bucket), giving perm (sorted position -> original index): points close in
 //      space get close positions, so a query block finds its neighbours in the
@@ -110,10 +110,10 @@ __global__ void k_gen_sketch(int D, float* G)
         G[t] = sketch_g(t / SKETCH, t % SKETCH);
 }
 
-// 2. sketch covariance per block + max |x - mu| estimate (FP32; only the order
-// of the points and the fp16 scale depend on it).
-__global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx, const float* meanf, const float* G,
-                         float* cov_partial /* blocks x 136 */, unsigned* rmax_ord)
+// 2. sketch covariance of a subsample (every stride-th point), per block (FP32;
+// only the order of the points depends on it).
+__global__ void k_sketch(const void* X, int dtype, int64_t N, int64_t stride, int D, int64_t ldx, const float* meanf,
+                         const float* G, float* cov_partial /* blocks x 136 */)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -134,18 +134,15 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
         pb[m] = a + p;
     }
     float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    float rloc = 0.f;
-    for (int64_t i = warp; i < N; i += nwarps)
+    for (int64_t i = warp * stride; i < N; i += nwarps * stride)
     {
         float s[SKETCH];
 #pragma unroll
         for (int j = 0; j < SKETCH; ++j)
             s[j] = 0.f;
-        float r2 = 0.f;
         for (int d = lane; d < D; d += 32)
         {
             const float vf = ldx_f(X, dtype, i * ldx + d) - meanf[d];
-            r2 = fmaf(vf, vf, r2);
             const float4* g = reinterpret_cast<const float4*>(G + (size_t)d * SKETCH);
 #pragma unroll
             for (int q = 0; q < SKETCH / 4; ++q)
@@ -157,8 +154,6 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
                 s[4 * q + 3] = fmaf(gq.w, vf, s[4 * q + 3]);
             }
         }
-        r2 = warp_sum_f(r2);
-        rloc = fmaxf(rloc, sqrtf(r2));
 #pragma unroll
         for (int j = 0; j < SKETCH; ++j)
             s[j] = warp_sum_f(s[j]);
@@ -192,8 +187,6 @@ __global__ void k_sketch(const void* X, int dtype, int64_t N, int D, int64_t ldx
             sacc += red[w][p];
         cov_partial[(int64_t)blockIdx.x * 136 + p] = sacc;
     }
-    if (rloc > 0.f)
-        atomicMax(rmax_ord, f2ord(rloc));
 }
 
 // 3. top-3 principal directions of the sketch covariance by subspace iteration
@@ -269,8 +262,9 @@ __global__ void k_pca3(const float* cov_partial, int nblk, int D, float* H)
 
 // projection p_i = H^T (x_i - mu) and its bounding box
 __global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ldx, const float* meanf,
-                          const float* H, float* proj, unsigned* bbox /* 6: min x3, max x3 */)
+                          const float* H, float* proj, unsigned* bbox /* 6: min x3, max x3 */, unsigned* rest_ord)
 {
+    float rloc = 0.f;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -278,9 +272,11 @@ __global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ld
     for (int64_t i = warp; i < N; i += nwarps)
     {
         float p[3] = {0.f, 0.f, 0.f};
+        float r2 = 0.f;
         for (int d = lane; d < D; d += 32)
         {
             const float v = ldx_f(X, dtype, i * ldx + d) - meanf[d];
+            r2 = fmaf(v, v, r2);
             p[0] = fmaf(H[d * 3 + 0], v, p[0]);
             p[1] = fmaf(H[d * 3 + 1], v, p[1]);
             p[2] = fmaf(H[d * 3 + 2], v, p[2]);
@@ -294,7 +290,10 @@ __global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ld
         }
         if (lane < 3)
             proj[i * 3 + lane] = lane == 0 ? p[0] : (lane == 1 ? p[1] : p[2]);
+        rloc = fmaxf(rloc, sqrtf(warp_sum_f(r2)));
     }
+    if (lane == 0 && rloc > 0.f)
+        atomicMax(rest_ord, f2ord(rloc));
     if (lane == 0 && mn[0] <= mx[0])
         for (int c = 0; c < 3; ++c)
         {
@@ -468,8 +467,8 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     k_colsum_final<<<(D + 255) / 256, 256, 0, st>>>(partial, nblk, D, N, meanf);
     TK_CHECK_LAUNCH();
 
-    // 2. sketch covariance and the R estimate
-    const int sk_blocks = 2 * sms;
+    // 2. sketch covariance (subsample)
+    const int sk_blocks = sms;
     float* covp = (float*)ctx->scratch.get("prep.covp", sizeof(float) * sk_blocks * 136);
     // small[0] = R estimate (ordered), small[1] = R (ordered), small[8..13] = bbox
     unsigned* small = (unsigned*)ctx->scratch.get("prep.small", 64 * sizeof(unsigned));
@@ -482,7 +481,8 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     float* G = (float*)ctx->scratch.get("prep.G", sizeof(float) * SKETCH * (size_t)D);
     k_gen_sketch<<<(D * SKETCH + 255) / 256, 256, 0, st>>>(D, G);
     TK_CHECK_LAUNCH();
-    k_sketch<<<sk_blocks, 256, 0, st>>>(X, dtype, N, D, ldx, meanf, G, covp, small);
+    const int64_t stride = std::max<int64_t>(1, N / 16384);
+    k_sketch<<<sk_blocks, 256, 0, st>>>(X, dtype, N, stride, D, ldx, meanf, G, covp);
     TK_CHECK_LAUNCH();
 
     // 3. principal directions and projection
@@ -490,7 +490,7 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     k_pca3<<<1, 64, 0, st>>>(covp, sk_blocks, D, H);
     TK_CHECK_LAUNCH();
     float* proj = (float*)ctx->scratch.get("prep.proj", sizeof(float) * 3 * (size_t)N);
-    k_project<<<2 * sms, 256, 0, st>>>(X, dtype, N, D, ldx, meanf, H, proj, small + 8);
+    k_project<<<2 * sms, 256, 0, st>>>(X, dtype, N, D, ldx, meanf, H, proj, small + 8, small);
     TK_CHECK_LAUNCH();
 
     // 4. Morton-bucket counting sort (about four points per bucket)

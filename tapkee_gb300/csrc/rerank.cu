@@ -24,6 +24,7 @@
 // survivors in FP64.
 #include <cfloat>
 #include <cmath>
+#include <cstdint>
 
 #include "ff.cuh"
 #include "tk_internal.h"
@@ -74,12 +75,11 @@ __device__ __forceinline__ double exact_d2(const void* X, int dtype, int64_t ldx
 }
 
 constexpr int RR_CHUNK = 64;  // dimensions staged per pass
-constexpr int RR_WARPS = 4;  // 4 x 8.6 KB static shared memory per block
+constexpr int RR_WARPS = 8;
 
 struct RerankSmem
 {
     float q[RR_CHUNK];
-    float rows[32][RR_CHUNK + 1];
 };
 
 template <int KC>
@@ -126,30 +126,50 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                 }
                 continue;
             }
-            // float32: stage the 32 candidate rows through shared memory with
-            // coalesced loads, then each lane sums its own row in float-float
+            // float32: every lane streams its own candidate row with independent
+            // (vectorised when aligned) loads; the query chunk is a shared-memory
+            // broadcast; squares accumulate in float-float
             const float* Xf = reinterpret_cast<const float*>(X);
+            const bool vec = ((reinterpret_cast<uintptr_t>(X) & 15u) == 0u) && ((ldx & 3) == 0);
             ff acc = ff_zero();
             float cross = 0.f;
             for (int d0 = 0; d0 < D; d0 += RR_CHUNK)
             {
                 const int dn = min(RR_CHUNK, D - d0);
+                __syncwarp();
                 for (int t = lane; t < RR_CHUNK; t += 32)
                     S.q[t] = (t < dn) ? Xf[i * ldx + d0 + t] : 0.f;
-                for (int r = 0; r < 32; ++r)
-                {
-                    const int64_t row = __shfl_sync(0xffffffffu, jj, r);
-                    for (int t = lane; t < RR_CHUNK; t += 32)
-                        S.rows[r][t] = (row >= 0 && t < dn) ? Xf[row * ldx + d0 + t] : 0.f;
-                }
                 __syncwarp();
-                for (int dd = 0; dd < dn; ++dd)
+                if (jj >= 0)
                 {
-                    const ff z = two_sum(S.rows[lane][dd], -S.q[dd]);
-                    acc = ff_add(acc, two_prod(z.hi, z.hi));
-                    cross = fmaf(2.f * z.hi, z.lo, cross);
+                    const float* row = Xf + jj * ldx + d0;
+                    float y[RR_CHUNK];
+                    if (vec && dn == RR_CHUNK)
+                    {
+#pragma unroll
+                        for (int q4 = 0; q4 < RR_CHUNK / 4; ++q4)
+                        {
+                            const float4 v4 = __ldg(reinterpret_cast<const float4*>(row) + q4);
+                            y[4 * q4 + 0] = v4.x;
+                            y[4 * q4 + 1] = v4.y;
+                            y[4 * q4 + 2] = v4.z;
+                            y[4 * q4 + 3] = v4.w;
+                        }
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int t = 0; t < RR_CHUNK; ++t)
+                            y[t] = (t < dn) ? __ldg(row + t) : 0.f;
+                    }
+#pragma unroll
+                    for (int t = 0; t < RR_CHUNK; ++t)
+                    {
+                        const ff z = two_sum(y[t], -S.q[t]);  // 0 - 0 for padding
+                        acc = ff_add(acc, two_prod(z.hi, z.hi));
+                        cross = fmaf(2.f * z.hi, z.lo, cross);
+                    }
                 }
-                __syncwarp();
             }
             if (jj >= 0)
             {
