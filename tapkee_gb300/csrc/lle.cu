@@ -276,64 +276,140 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         const int iters = (k > D) ? 2 : 1;
         for (int itr = 0; itr < iters; ++itr)
         {
-            ff sa[NPL], ta[NPL];
+            if (KP <= 32)
+            {
+                // lanes own dimensions: z_a(d) = hi + lo exactly, v(d) = sum_b w_b z_b(d),
+                // and lane-local partials of (C w)_a = sum_d z_a(d) v(d) and of
+                // trace = sum_a |z_a|^2; one reduce-scatter gathers (C w)_a.
+                constexpr int KR = (KP <= 32) ? KP : 32;
+                ff part[KR];
+                ff trp = ff_zero();
 #pragma unroll
-            for (int s = 0; s < NPL; ++s)
-            {
-                sa[s] = ff_zero();
-                ta[s] = ff_zero();
-            }
-            for (int d0 = 0; d0 < D; d0 += 32)
-            {
-                const int d = d0 + lane;
-                for (int a = 0; a < KP; ++a)
+                for (int a = 0; a < KR; ++a)
+                    part[a] = ff_zero();
+                for (int d0 = 0; d0 < D; d0 += 32)
                 {
-                    const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
-                    ff z = ff_zero();
-                    if (a < k && d < D)
-                        z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
-                    S.Zh[a][lane] = z.hi;
-                    S.Zl[a][lane] = z.lo;
+                    const int d = d0 + lane;
+                    float zh[KR], zl[KR];
+#pragma unroll
+                    for (int a = 0; a < KR; ++a)
+                    {
+                        const int nba = __shfl_sync(0xffffffffu, nb[0], a & 31);
+                        ff z = ff_zero();
+                        if (a < k && d < D)
+                            z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
+                        zh[a] = z.hi;
+                        zl[a] = z.lo;
+                    }
+                    // two independent chains for v
+                    ff v0 = ff_zero(), v1 = ff_zero();
+#pragma unroll
+                    for (int b = 0; b < KR; b += 2)
+                    {
+                        v0 = ff_fma(v0, S.w[b], 0.f, zh[b], zl[b]);
+                        if (b + 1 < KR)
+                            v1 = ff_fma(v1, S.w[b + 1], 0.f, zh[b + 1], zl[b + 1]);
+                    }
+                    const ff v = ff_add(v0, v1);
+#pragma unroll
+                    for (int a = 0; a < KR; ++a)
+                    {
+                        part[a] = ff_fma(part[a], zh[a], zl[a], v.hi, v.lo);
+                        trp = ff_fma(trp, zh[a], zl[a], zh[a], zl[a]);
+                    }
                 }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    trp = ff_add(trp, ff_shfl_xor(trp, o));
+                // reduce-scatter of the KR partials (KR = 16 or 32 values)
+#pragma unroll
+                for (int lvl = 0; lvl < 5; ++lvl)
+                {
+                    const int o = 16 >> lvl;
+                    const int half = (KR >> (lvl + 1)) > 0 ? (KR >> (lvl + 1)) : 0;
+                    if (half > 0)
+                    {
+                        const bool upper = (lane & o) != 0;
+#pragma unroll
+                        for (int q = 0; q < half; ++q)
+                        {
+                            const ff send = upper ? part[q] : part[q + half];
+                            const ff keep = upper ? part[q + half] : part[q];
+                            part[q] = ff_add(keep, ff_shfl_xor(send, o));
+                        }
+                    }
+                    else
+                        part[0] = ff_add(part[0], ff_shfl_xor(part[0], o));  // pairs hold the same index
+                }
+                // part[0] of lane l is (C w)_a for a = KR == 32 ? l : (l >> 1)
+                const int a_own = (KR == 32) ? lane : (lane >> 1);
+                const double shift_true = klle_shift * ff_to_double(trp);
+                if ((KR == 32 || (lane & 1) == 0) && a_own < KP)
+                    S.r[a_own] = (a_own < k) ? (float)(1.0 - ff_to_double(part[0]) - shift_true * (double)S.w[a_own])
+                                             : 0.f;
                 __syncwarp();
-                // v_d = sum_b w_b z_bd for d = d0 + lane
-                ff v = ff_zero();
-                for (int b = 0; b < k; ++b)
-                    v = ff_fma(v, S.w[b], 0.f, S.Zh[b][lane], S.Zl[b][lane]);
-                S.vh[lane] = v.hi;
-                S.vl[lane] = v.lo;
-                __syncwarp();
+            }
+            else
+            {
+                ff sa[NPL], ta[NPL];
+#pragma unroll
+                for (int s = 0; s < NPL; ++s)
+                {
+                    sa[s] = ff_zero();
+                    ta[s] = ff_zero();
+                }
+                for (int d0 = 0; d0 < D; d0 += 32)
+                {
+                    const int d = d0 + lane;
+                    for (int a = 0; a < KP; ++a)
+                    {
+                        const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
+                        ff z = ff_zero();
+                        if (a < k && d < D)
+                            z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
+                        S.Zh[a][lane] = z.hi;
+                        S.Zl[a][lane] = z.lo;
+                    }
+                    __syncwarp();
+                    // v_d = sum_b w_b z_bd for d = d0 + lane
+                    ff v = ff_zero();
+                    for (int b = 0; b < k; ++b)
+                        v = ff_fma(v, S.w[b], 0.f, S.Zh[b][lane], S.Zl[b][lane]);
+                    S.vh[lane] = v.hi;
+                    S.vl[lane] = v.lo;
+                    __syncwarp();
+#pragma unroll
+                    for (int s = 0; s < NPL; ++s)
+                    {
+                        const int a = lane + 32 * s;
+                        if (a < k)
+                            for (int dd = 0; dd < 32; ++dd)
+                            {
+                                const float zh = S.Zh[a][dd], zl = S.Zl[a][dd];
+                                sa[s] = ff_fma(sa[s], zh, zl, S.vh[dd], S.vl[dd]);
+                                ta[s] = ff_fma(ta[s], zh, zl, zh, zl);
+                            }
+                    }
+                    __syncwarp();
+                }
+                // exact trace = sum_a |z_a|^2
+                ff tr = ff_zero();
+#pragma unroll
+                for (int s = 0; s < NPL; ++s)
+                    tr = ff_add(tr, ta[s]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    tr = ff_add(tr, ff_shfl_xor(tr, o));
+                const double shift_true = klle_shift * ff_to_double(tr);
 #pragma unroll
                 for (int s = 0; s < NPL; ++s)
                 {
                     const int a = lane + 32 * s;
-                    if (a < k)
-                        for (int dd = 0; dd < 32; ++dd)
-                        {
-                            const float zh = S.Zh[a][dd], zl = S.Zl[a][dd];
-                            sa[s] = ff_fma(sa[s], zh, zl, S.vh[dd], S.vl[dd]);
-                            ta[s] = ff_fma(ta[s], zh, zl, zh, zl);
-                        }
+                    if (a < KP)
+                        S.r[a] = (a < k) ? (float)(1.0 - ff_to_double(sa[s]) - shift_true * (double)S.w[a]) : 0.f;
                 }
                 __syncwarp();
             }
-            // exact trace = sum_a |z_a|^2
-            ff tr = ff_zero();
-#pragma unroll
-            for (int s = 0; s < NPL; ++s)
-                tr = ff_add(tr, ta[s]);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                tr = ff_add(tr, ff_shfl_xor(tr, o));
-            const double shift_true = klle_shift * ff_to_double(tr);
-#pragma unroll
-            for (int s = 0; s < NPL; ++s)
-            {
-                const int a = lane + 32 * s;
-                if (a < KP)
-                    S.r[a] = (a < k) ? (float)(1.0 - ff_to_double(sa[s]) - shift_true * (double)S.w[a]) : 0.f;
-            }
-            __syncwarp();
             chol_solve<KP>(S, lane);
             for (int a = lane; a < k; a += 32)
                 S.w[a] += S.r[a];

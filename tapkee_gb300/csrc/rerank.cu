@@ -126,51 +126,47 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                 }
                 continue;
             }
-            // float32: every lane streams its own candidate row with independent
-            // (vectorised when aligned) loads; the query chunk is a shared-memory
-            // broadcast; squares accumulate in float-float
+            // float32: lanes own dimensions (coalesced row loads); each lane keeps
+            // float-float partial sums for all 32 candidates of the group, and a
+            // warp reduce-scatter leaves candidate l's total in lane l
             const float* Xf = reinterpret_cast<const float*>(X);
-            const bool vec = ((reinterpret_cast<uintptr_t>(X) & 15u) == 0u) && ((ldx & 3) == 0);
-            ff acc = ff_zero();
-            float cross = 0.f;
-            for (int d0 = 0; d0 < D; d0 += RR_CHUNK)
+            ff part[32];
+#pragma unroll
+            for (int r = 0; r < 32; ++r)
+                part[r] = ff_zero();
+            for (int d0 = 0; d0 < D; d0 += 32)
             {
-                const int dn = min(RR_CHUNK, D - d0);
-                __syncwarp();
-                for (int t = lane; t < RR_CHUNK; t += 32)
-                    S.q[t] = (t < dn) ? Xf[i * ldx + d0 + t] : 0.f;
-                __syncwarp();
-                if (jj >= 0)
+                const int d = d0 + lane;
+                const float xq = (d < D) ? Xf[i * ldx + d] : 0.f;
+#pragma unroll
+                for (int r = 0; r < 32; ++r)
                 {
-                    const float* row = Xf + jj * ldx + d0;
-                    float y[RR_CHUNK];
-                    if (vec && dn == RR_CHUNK)
-                    {
-#pragma unroll
-                        for (int q4 = 0; q4 < RR_CHUNK / 4; ++q4)
-                        {
-                            const float4 v4 = __ldg(reinterpret_cast<const float4*>(row) + q4);
-                            y[4 * q4 + 0] = v4.x;
-                            y[4 * q4 + 1] = v4.y;
-                            y[4 * q4 + 2] = v4.z;
-                            y[4 * q4 + 3] = v4.w;
-                        }
-                    }
-                    else
-                    {
-#pragma unroll
-                        for (int t = 0; t < RR_CHUNK; ++t)
-                            y[t] = (t < dn) ? __ldg(row + t) : 0.f;
-                    }
-#pragma unroll
-                    for (int t = 0; t < RR_CHUNK; ++t)
-                    {
-                        const ff z = two_sum(y[t], -S.q[t]);  // 0 - 0 for padding
-                        acc = ff_add(acc, two_prod(z.hi, z.hi));
-                        cross = fmaf(2.f * z.hi, z.lo, cross);
-                    }
+                    const int64_t row = __shfl_sync(0xffffffffu, jj, r);
+                    const float y = (row >= 0 && d < D) ? Xf[row * ldx + d] : 0.f;
+                    const ff z = two_sum(y, -xq);  // exact difference
+                    ff sq = two_prod(z.hi, z.hi);
+                    sq.lo = fmaf(2.f * z.hi, z.lo, sq.lo);
+                    part[r] = ff_add(part[r], sq);
                 }
             }
+            // reduce-scatter: after the level with offset o, a lane keeps the half of
+            // its candidates whose index bit matches its own lane bit
+#pragma unroll
+            for (int lvl = 0; lvl < 5; ++lvl)
+            {
+                const int o = 16 >> lvl;
+                const int half = o;  // values kept after this level: 2 * half -> half
+                const bool upper = (lane & o) != 0;
+#pragma unroll
+                for (int q = 0; q < half; ++q)
+                {
+                    const ff send = upper ? part[q] : part[q + half];
+                    const ff keep = upper ? part[q + half] : part[q];
+                    part[q] = ff_add(keep, ff_shfl_xor(send, o));
+                }
+            }
+            const ff acc = part[0];
+            const float cross = 0.f;
             if (jj >= 0)
             {
                 d[s] = ff_to_double(acc) + (double)cross;
