@@ -220,7 +220,7 @@ __device__ __forceinline__ void reg_insert(float (&L)[KC], int32_t (&I)[KC], flo
 
 struct TcBarriers
 {
-    uint64_t full[4], empty[4], tfull[2], tempty[2], afull, fin;
+    uint64_t full[4], empty[4], tfull[2][2], tempty[2][2], afull, fin;  // t* : [buffer][query block]
     uint32_t tmem_base;
     int abort;
 };
@@ -258,8 +258,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         for (int b = 0; b < 2; ++b)
         {
-            mbar_init(smem_u32(&Bar.tfull[b]), 1);
-            mbar_init(smem_u32(&Bar.tempty[b]), C::EPI_WARPS);
+            for (int qt = 0; qt < 2; ++qt)
+            {
+                mbar_init(smem_u32(&Bar.tfull[b][qt]), 1);
+                mbar_init(smem_u32(&Bar.tempty[b][qt]), 4);  // the 4 epilogue warps of a query block
+            }
         }
         mbar_init(smem_u32(&Bar.afull), 1);
         mbar_init(smem_u32(&Bar.fin), 1);
@@ -359,13 +362,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t bph = (uint32_t)(it >> 1) & 1u;
                 if (!mbar_wait(smem_u32(&Bar.full[slot]), ph, abort, err))
                     break;
-                if (!mbar_wait(smem_u32(&Bar.tempty[buf]), bph ^ 1u, abort, err))
-                    break;
-                tc_fence_after();
                 const uint64_t soff = (uint64_t)((slot * C::B_STAGE_BYTES) >> 4);
+                bool ok_q = true;
+                // each query block's accumulator half has its own handoff, so its
+                // epilogue warps start as soon as its 13 MMAs are done
 #pragma unroll
                 for (int qt = 0; qt < C::QT; ++qt)
                 {
+                    if (!mbar_wait(smem_u32(&Bar.tempty[buf][qt]), bph ^ 1u, abort, err))
+                    {
+                        ok_q = false;
+                        break;
+                    }
+                    tc_fence_after();
                     const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
                     // norm step first: D = 2^13 (h + l) of -|2^s y|^2 / 2^14
                     umma_f16(d, axd, bx0 + soff, 0u);
@@ -378,10 +387,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         for (int kk = 0; kk < DP / 16; ++kk)
                             umma_f16(d, adesc[qt][apart][kk], bdesc0[bpart][kk] + soff, 1u);
                     }
+                    umma_commit(smem_u32(&Bar.tfull[buf][qt]));
+                    issued_any = 1;
                 }
+                if (!ok_q)
+                    break;
                 umma_commit(smem_u32(&Bar.empty[slot]));
-                umma_commit(smem_u32(&Bar.tfull[buf]));
-                issued_any = 1;
             }
             if (issued_any)
             {
@@ -422,7 +433,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int buf = it & 1;
             const uint32_t bph = (uint32_t)(it >> 1) & 1u;
             // tcgen05.ld is warp-collective: leave the loop as a whole warp
-            const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf]), bph, abort, err);
+            const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf][qt]), bph, abort, err);
             if (!__all_sync(0xffffffffu, ok))
                 break;
             tc_fence_after();
@@ -438,6 +449,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (CPW == 64)
                     tmem_ld32_nowait(tacc + h * CPW + 32, v + 32);
                 tmem_wait_ld();
+                if (h == TC_N / CPW - 1)
+                {
+                    // the last columns are in registers: hand the buffer back now
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0)
+                        mbar_arrive(smem_u32(&Bar.tempty[buf][qt]));
+                }
 #pragma unroll
                 for (int s32 = 0; s32 < CPW / 32; ++s32)
                 {
@@ -476,10 +495,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     }
                 }
             }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0)
-                mbar_arrive(smem_u32(&Bar.tempty[buf]));
         }
 #pragma unroll
         for (int s = 0; s < KC; ++s)
