@@ -25,6 +25,7 @@
 #ifndef TAPKEE_GB300_H
 #define TAPKEE_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -219,6 +220,32 @@ int tk_operator_get_info(const tk_ctx* ctx, tk_operator_info* info);
 
 /* Waits for all work queued on the context's stream. */
 int tk_ctx_synchronize(tk_ctx* ctx);
+
+/* ---- allocation-free entry point --------------------------------------------- */
+
+/* Largest graph tk_check_connected_noalloc accepts, and the size of the static
+ * device scratch that holds its BFS state (one instance per device). */
+#define TK_NOALLOC_MAX_POINTS 2097152
+#define TK_NOALLOC_SCRATCH_BYTES 17039616
+
+/* Same result as tk_check_connected, without a context and without allocating
+ * host or device memory. It has no counterpart in the reference: it exists for
+ * callers that cannot allocate device memory at the point of the call (a process
+ * whose free HBM is held by a caching allocator) or cannot accept the
+ * device-wide synchronisation of a scratch buffer being freed and regrown.
+ *   - idx (N x k) must already be device or managed memory of `device`;
+ *     nothing is copied. stream is a cudaStream_t of `device` (NULL = default
+ *     stream). The call waits for its own result on that stream.
+ *   - N must not exceed TK_NOALLOC_MAX_POINTS; larger N returns
+ *     TK_ERR_INVALID_ARG with a message naming the limit.
+ *   - The first call on a device does the set-up (resolves the device address of
+ *     the scratch array and loads the kernel): make it before any stream capture.
+ *   - Every call on a device shares the one scratch array: calls that overlap in
+ *     time on that device (other threads, other streams) race and must be
+ *     serialised by the caller.
+ *   - msg (msg_len bytes, may be NULL) receives the error message, "" on success. */
+int tk_check_connected_noalloc(int device, void* stream, int64_t N, int k, const int32_t* idx, int* connected,
+                               char* msg, size_t msg_len);
 
 #ifdef __cplusplus
 }

@@ -24,6 +24,7 @@ TK_ERR_NO_DEVICE = 9
 TK_ERR_INTERNAL = 10
 
 TK_F32, TK_F64 = 0, 1
+TK_NOALLOC_MAX_POINTS = 2097152
 TK_METHOD_KLLE, TK_METHOD_KLTSA = 0, 1
 TK_SCREEN_TENSOR, TK_SCREEN_FP32 = 0, 1
 
@@ -87,6 +88,8 @@ SIGNATURES = {
                                       ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "tk_operator_get_info": (_I, [_P, ctypes.POINTER(tk_operator_info)]),
     "tk_ctx_synchronize": (_I, [_P]),
+    "tk_check_connected_noalloc": (_I, [_I, _P, _I64, _I, _P, ctypes.POINTER(_I), ctypes.c_char_p,
+                                        ctypes.c_size_t]),
 }
 
 _lib = None
