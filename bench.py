@@ -132,14 +132,14 @@ def cpu_baseline(X, k, sample, threads):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_DEF)
     ap.add_argument("--d", type=int, default=D_DEF)
     ap.add_argument("--k", type=int, default=K_DEF)
     ap.add_argument("--fp32-steps", type=int, default=2)
-    ap.add_argument("--cpu-sample", type=int, default=2000)
+    ap.add_argument("--cpu-sample", type=int, default=16000)
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--check-connectivity", type=int, default=0)
     args = ap.parse_args()
