@@ -141,6 +141,7 @@ def main():
     ap.add_argument("--fp32-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=16000)
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-ltsa", action="store_true")
     ap.add_argument("--check-connectivity", type=int, default=0)
     args = ap.parse_args()
 
@@ -258,6 +259,34 @@ def main():
                 "screen_kernel_ms": float(np.mean([i.stage_ms[5] for i in inf_f])),
                 "tc_over_fp32": ms_f / ms_step}
 
+    # LTSA workload (lifted S-curve N=50000 D=32 k=20 td=2, float32): same timing
+    # rules, reported beside the headline
+    ltsa = None
+    if not args.no_ltsa:
+        Xl = torch.from_numpy(datasets.lifted_s_curve(50_000, 32, seed=3, noise=0.02)).cuda()
+        for _ in range(3):
+            ctx.local_operator(Xl, "ltsa", num_neighbors=20, target_dimension=2, check_connectivity=False,
+                               copy_out=False)
+        lt, linf = [], []
+        for _ in range(5):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            linf.append(ctx.local_operator(Xl, "ltsa", num_neighbors=20, target_dimension=2,
+                                           check_connectivity=False, copy_out=False))
+            e1.record(stream)
+            e1.synchronize()
+            lt.append(e0.elapsed_time(e1))
+        lms = float(np.mean(lt))
+        ltsa = {"workload": "LTSA lifted S-curve N=50000 D=32 k=20 td=2 float32", "ms_per_step": lms,
+                "points_per_s": 50_000 / (lms / 1000.0),
+                "stage_ms": {"knn": float(np.mean([i.stage_ms[0] for i in linf])),
+                             "tangent_bases": float(np.mean([i.stage_ms[2] for i in linf])),
+                             "assembly": float(np.mean([i.stage_ms[3] for i in linf]))},
+                "nnz": int(linf[-1].nnz)}
+        del Xl
+
     # end to end through the public API with pinned host buffers
     Xh = torch.from_numpy(X).pin_memory()
     nnz = int(info.nnz)
@@ -303,7 +332,7 @@ def main():
             "vs_baseline": None, "dtype": "fp16x3-split screen / f64 re-rank / f32+ff weights",
             "data": "synthetic (seeded lifted Swiss roll)", "config": workload, "stage_ms": stage,
             "rows_uncertified": int(info.rows_uncertified), "nnz": nnz, "k_used": kk,
-            "fp32_path": fp32, "roofline": roofline,
+            "fp32_path": fp32, "ltsa": ltsa, "roofline": roofline,
             "e2e": {"value": args.n / (e2e_ms / 1000.0), "unit": "points/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clocks, "gpu_launches": int(launches)}

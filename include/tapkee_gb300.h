@@ -173,6 +173,18 @@ int tk_check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx, int* c
 int tk_lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
                    int k, double klle_shift, double* W_out);
 
+/* Reverse-mode derivative of tk_lle_weights with the neighbour sets held fixed:
+ * given the weights W (N x k, from tk_lle_weights on the same X, idx, klle_shift)
+ * and an upstream gradient dW = dL/dW (N x k), writes dX_out = dL/dX (N x D FP64,
+ * row stride D). Per point it solves (C + klle_shift tr(C) I) mu = dW_i - (dW_i.w_i) 1
+ * with the forward's solver and scatters -mu_a p - w_a q - 2 klle_shift (mu.w) z_a
+ * (p = sum w_b z_b, q = sum mu_b z_b, z_a = x_{n_a} - x_i) to the neighbours and its
+ * negated sum to the point. No counterpart in the reference (which does not
+ * differentiate); it is the adjoint of the solve in linear_weight_matrix
+ * (routines/locally_linear.hpp:117-131). */
+int tk_lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                        int k, double klle_shift, const double* W, const double* dW, double* dX_out);
+
 /* LTSA tangent basis: per point, the eigenvectors of the td largest eigenvalues
  * of the double-centred neighbour Gram. V_out is N x k x td (sign of each vector
  * is arbitrary); the alignment block is P = (1/k) 1 1^T + V V^T.

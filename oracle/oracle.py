@@ -135,13 +135,15 @@ def lle_weights_rows(X, rows, idx_rows, klle_shift=1e-3, nthreads=None):
 
 
 def ltsa_basis(X, idx, td=2, nthreads=None, return_evals=False):
+    """Tangent bases of the neighbourhoods idx (one row per neighbourhood; the
+    rows may be any subset of the points, since LTSA's Gram uses neighbours only)."""
     X = _X64(X)
-    N, D = X.shape
+    D = X.shape[1]
     idx = np.ascontiguousarray(idx, dtype=np.int32)
-    k = idx.shape[1]
-    V = np.zeros((N, k, td), np.float64)
-    ev = np.zeros((N, k), np.float64)
-    lib().oracle_ltsa_basis(X.ctypes.data, N, D, idx.ctypes.data, k, td, V.ctypes.data, ev.ctypes.data,
+    rows, k = idx.shape
+    V = np.zeros((rows, k, td), np.float64)
+    ev = np.zeros((rows, k), np.float64)
+    lib().oracle_ltsa_basis(X.ctypes.data, rows, D, idx.ctypes.data, k, td, V.ctypes.data, ev.ctypes.data,
                             _threads(nthreads))
     return (V, ev) if return_evals else V
 

@@ -79,6 +79,7 @@ SIGNATURES = {
     "tk_knn_brute": (_I, [_P, _P, _I, _I64, _I, _I64, _I, _I, _P, _P, ctypes.POINTER(tk_knn_stats)]),
     "tk_check_connected": (_I, [_P, _I64, _I, _P, ctypes.POINTER(_I)]),
     "tk_lle_weights": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P]),
+    "tk_lle_weights_grad": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P, _P, _P]),
     "tk_ltsa_basis": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _I, _P]),
     "tk_assemble": (_I, [_P, _I, _I64, _I, _I, _P, _P, _D, _P, _P, _P, ctypes.POINTER(_I64)]),
     "tk_local_operator": (_I, [_P, ctypes.POINTER(tk_params), _P, _I, _I64, _I, _I64,

@@ -454,6 +454,30 @@ int tk_lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int6
     });
 }
 
+int tk_lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                        int k, double klle_shift, const double* W, const double* dW, double* dX_out)
+{
+    return guarded(ctx, [&] {
+        validate_points(X, dtype, N, D, ldx);
+        if (k < 1 || !idx || !W || !dW || !dX_out)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        if (k > 128)
+            throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 128 neighbours");
+        int64_t ldd;
+        const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "io.X");
+        const int32_t* idx_d = device_array(ctx, idx, (size_t)N * k, "io.idx_in");
+        const double* W_d = device_array(ctx, W, (size_t)N * k, "io.W_in");
+        const double* G_d = device_array(ctx, dW, (size_t)N * k, "io.dW_in");
+        bool gh;
+        double* gX_d = device_out(ctx, dX_out, (size_t)N * D, "io.dX", &gh);
+        lle_weights_grad(ctx, Xd, dtype, N, D, ldd, idx_d, k, klle_shift, W_d, G_d, gX_d);
+        check_device_errors(ctx);
+        if (gh)
+            copy_back(ctx, dX_out, gX_d, (size_t)N * D);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 int tk_ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
                   int td, double* V_out)
 {

@@ -78,6 +78,7 @@ __device__ __forceinline__ void chol_solve(LleSmem<KP>& S, int lane)
 template <int KP, int WARPS, bool BLOCKED = (KP <= 64)>
 __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, int64_t N, int D, int64_t ldx,
                                                     const int32_t* __restrict__ idx, int k, double klle_shift,
+                                                    const double* __restrict__ rhs, int normalize,
                                                     double* __restrict__ W, unsigned* err)
 {
     constexpr int NB4 = KP / 4;
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
                 S.C[a][a] += shift;
             else
                 S.C[a][a] = 1.f;  // padding rows/columns are zero: identity block
-            S.r[a] = (a < k) ? 1.f : 0.f;
+            S.r[a] = (a < k) ? (rhs ? (float)rhs[i * k + a] : 1.f) : 0.f;
         }
         __syncwarp();
 
@@ -345,7 +346,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
                 const int a_own = (KR == 32) ? lane : (lane >> 1);
                 const double shift_true = klle_shift * ff_to_double(trp);
                 if ((KR == 32 || (lane & 1) == 0) && a_own < KP)
-                    S.r[a_own] = (a_own < k) ? (float)(1.0 - ff_to_double(part[0]) - shift_true * (double)S.w[a_own])
+                    S.r[a_own] = (a_own < k) ? (float)((rhs ? rhs[i * k + a_own] : 1.0) - ff_to_double(part[0]) -
+                                                       shift_true * (double)S.w[a_own])
                                              : 0.f;
                 __syncwarp();
             }
@@ -406,7 +408,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
                 {
                     const int a = lane + 32 * s;
                     if (a < KP)
-                        S.r[a] = (a < k) ? (float)(1.0 - ff_to_double(sa[s]) - shift_true * (double)S.w[a]) : 0.f;
+                        S.r[a] = (a < k) ? (float)((rhs ? rhs[i * k + a] : 1.0) - ff_to_double(sa[s]) -
+                                                   shift_true * (double)S.w[a])
+                                         : 0.f;
                 }
                 __syncwarp();
             }
@@ -416,7 +420,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
             __syncwarp();
         }
 
-        // ---- normalise and store ----
+        // ---- normalise (weights) or store the raw solution (adjoint solve) ----
+        if (!normalize)
+        {
+            for (int a = lane; a < k; a += 32)
+                W[i * k + a] = (double)S.w[a];
+            __syncwarp();
+            continue;
+        }
         double sum = 0.0;
         for (int a = lane; a < k; a += 32)
             sum += (double)S.w[a];
@@ -431,32 +442,39 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
 
 template <int KP, int WARPS>
 void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
-            double klle_shift, double* W)
+            double klle_shift, const double* rhs, int normalize, double* W)
 {
     const size_t smem = sizeof(LleSmem<KP>) * WARPS;
     TK_CUDA(cudaFuncSetAttribute(k_lle<KP, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t want = (N + WARPS - 1) / WARPS;
     const int grid = (int)std::min<int64_t>(want, (int64_t)ctx->num_sms * 16);
-    k_lle<KP, WARPS><<<grid, WARPS * 32, smem, ctx->stream>>>(X, dtype, N, D, ldx, idx, k, klle_shift, W,
-                                                               ctx->dev_err);
+    k_lle<KP, WARPS><<<grid, WARPS * 32, smem, ctx->stream>>>(X, dtype, N, D, ldx, idx, k, klle_shift, rhs,
+                                                               normalize, W, ctx->dev_err);
     TK_CHECK_LAUNCH();
 }
 
 } // namespace
 
+void lle_solve(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+               double klle_shift, const double* rhs, bool normalize, double* W)
+{
+    const int nm = normalize ? 1 : 0;
+    if (k <= 16)
+        launch<16, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
+    else if (k <= 32)
+        launch<32, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
+    else if (k <= 64)
+        launch<64, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
+    else if (k <= 128)
+        launch<128, 1>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
+    else
+        throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 128 neighbours");
+}
+
 void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
                  double klle_shift, double* W)
 {
-    if (k <= 16)
-        launch<16, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
-    else if (k <= 32)
-        launch<32, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
-    else if (k <= 64)
-        launch<64, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
-    else if (k <= 128)
-        launch<128, 1>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, W);
-    else
-        throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 128 neighbours");
+    lle_solve(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, nullptr, true, W);
 }
 
 } // namespace tk

@@ -132,6 +132,13 @@ bool check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx);
 // lle.cu
 void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
                  int k, double klle_shift, double* W);
+// The same regularised solve with a per-point right-hand side rhs (N x k; NULL =
+// ones) and, when normalize is false, the raw solution instead of weights.
+void lle_solve(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+               double klle_shift, const double* rhs, bool normalize, double* W);
+// dL/dX (N x D, FP64, row stride D) of the weights W for upstream dL/dW = G.
+void lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+                      double klle_shift, const double* W, const double* G, double* gX);
 
 // ltsa.cu
 void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
