@@ -66,7 +66,10 @@ __device__ void warp_jacobi(JacobiSmem<M, T>& S, int lane, int max_sweeps)
             off += __shfl_xor_sync(0xffffffffu, off, o);
             dia += __shfl_xor_sync(0xffffffffu, dia, o);
         }
-        const T tol = sizeof(T) == 8 ? T(1e-30) : T(1e-14);
+        // stop when the off-diagonal mass is at the working precision's level:
+        // FP32 -> rms off-diagonal ~1e-6 of the diagonal, enough for the
+        // float-float refinement that follows; FP64 -> ~1e-13
+        const T tol = sizeof(T) == 8 ? T(1e-26) : T(1e-12);
         if (off <= tol * dia || dia == T(0))
             break;
         for (int round = 0; round < M - 1; ++round)
@@ -178,10 +181,12 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
         S.Vt[a][t] = (a < k) ? (double)S.V[a][top[t]] : 0.0;
     }
     __syncwarp();
-    ff acc[8];
-    for (int t = 0; t < 8; ++t)
-        acc[t] = ff_zero();
-    const int a_own = lane;  // this lane accumulates (G V)[a_own][:]
+    constexpr int RPL = (M + 31) / 32;  // basis rows per lane: a = lane + 32 r
+    ff acc[RPL][8];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+        for (int t = 0; t < 8; ++t)
+            acc[r][t] = ff_zero();
     for (int d0 = 0; d0 < D; d0 += 32)
     {
         const int d = d0 + lane;
@@ -213,19 +218,29 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
             S.tl[lane][t] = s.lo;
         }
         __syncwarp();
-        // (G V)_a += sum_d z_ad t_d   (lane = a)
-        if (a_own < k)
-            for (int dd = 0; dd < 32; ++dd)
-            {
-                const float zh = S.Z[a_own][dd], zl = S.Zl[a_own][dd];
-                for (int t = 0; t < td; ++t)
-                    acc[t] = ff_fma(acc[t], zh, zl, S.th[dd][t], S.tl[dd][t]);
-            }
+        // (G V)_a += sum_d z_ad t_d   (a = lane + 32 r)
+#pragma unroll
+        for (int r = 0; r < RPL; ++r)
+        {
+            const int a = lane + 32 * r;
+            if (a < k)
+                for (int dd = 0; dd < 32; ++dd)
+                {
+                    const float zh = S.Z[a][dd], zl = S.Zl[a][dd];
+                    for (int t = 0; t < td; ++t)
+                        acc[r][t] = ff_fma(acc[r][t], zh, zl, S.th[dd][t], S.tl[dd][t]);
+                }
+        }
         __syncwarp();
     }
-    if (a_own < M)
-        for (int t = 0; t < td; ++t)
-            S.GV[a_own][t] = (a_own < k) ? ff_to_double(acc[t]) : 0.0;
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+    {
+        const int a = lane + 32 * r;
+        if (a < M)
+            for (int t = 0; t < td; ++t)
+                S.GV[a][t] = (a < k) ? ff_to_double(acc[r][t]) : 0.0;
+    }
     __syncwarp();
     // Rayleigh quotient Lambda = V^T G V (td x td) and residual R = G V - V Lambda
     __shared__ double Lam_s[4][8][8];  // up to 4 warps per block
@@ -239,10 +254,12 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
         Lam[i * 8 + j] = s;
     }
     __syncwarp();
-    // corrections (lane = row a of the basis)
-    double corr[8];
-    for (int t = 0; t < td; ++t)
-        corr[t] = 0.0;
+    // corrections (rows a = lane + 32 r of the basis)
+    double corr[RPL][8];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+        for (int t = 0; t < td; ++t)
+            corr[r][t] = 0.0;
     for (int j = 0; j < k; ++j)
     {
         bool is_top = false;
@@ -263,14 +280,24 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
                 ur += (double)S.V[a][j] * r;
             }
             const double gap = Lam[t * 8 + t] - lj;
-            if (lane < k && gap != 0.0)
-                corr[t] += (double)S.V[lane][j] * ur / gap;
+#pragma unroll
+            for (int r = 0; r < RPL; ++r)
+            {
+                const int a = lane + 32 * r;
+                if (a < k && gap != 0.0)
+                    corr[r][t] += (double)S.V[a][j] * ur / gap;
+            }
         }
     }
     __syncwarp();
-    if (lane < k)
-        for (int t = 0; t < td; ++t)
-            S.Vt[lane][t] += corr[t];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+    {
+        const int a = lane + 32 * r;
+        if (a < k)
+            for (int t = 0; t < td; ++t)
+                S.Vt[a][t] += corr[r][t];
+    }
     __syncwarp();
     // modified Gram-Schmidt (FP64) on the td columns
     for (int t = 0; t < td; ++t)
@@ -281,16 +308,16 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
             for (int a = 0; a < k; ++a)
                 dot += S.Vt[a][t] * S.Vt[a][q];
             __syncwarp();
-            if (lane < k)
-                S.Vt[lane][t] -= dot * S.Vt[lane][q];
+            for (int a = lane; a < k; a += 32)
+                S.Vt[a][t] -= dot * S.Vt[a][q];
             __syncwarp();
         }
         double nrm = 0.0;
         for (int a = 0; a < k; ++a)
             nrm += S.Vt[a][t] * S.Vt[a][t];
         __syncwarp();
-        if (lane < k)
-            S.Vt[lane][t] /= sqrt(nrm);
+        for (int a = lane; a < k; a += 32)
+            S.Vt[a][t] /= sqrt(nrm);
         __syncwarp();
     }
 }
@@ -312,7 +339,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, i
         __syncwarp();
         centred_gram<M, float>(S, lane, X, dtype, ldx, D, nb_s[wib], k);
         warp_jacobi<M, float>(S, lane, 30);
-        // order eigenvalues (lane 0, M <= 32): top td indices
+        // order eigenvalues (lane 0): top td indices and the next one
         __shared__ int top_s[WARPS][8];
         if (lane == 0)
         {
@@ -437,10 +464,20 @@ void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t
 {
     if (td < 1 || td > 8 || td >= k)
         throw Error(TK_ERR_INVALID_ARG, "LTSA needs 1 <= target_dimension <= 8 and target_dimension < k");
-    if (k <= 16)
+    // the Jacobi works on the zero-padded M x M Gram (M even): pick M close to k,
+    // since a sweep costs ~M^3
+    if (k <= 12)
+        launch<12>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
+    else if (k <= 16)
         launch<16>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
+    else if (k <= 20)
+        launch<20>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
+    else if (k <= 24)
+        launch<24>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
     else if (k <= 32)
         launch<32>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
+    else if (k <= 48)
+        launch<48>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
     else if (k <= 64)
         launch<64>(ctx, X, dtype, N, D, ldx, idx, k, td, V);
     else

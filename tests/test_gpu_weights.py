@@ -37,7 +37,8 @@ def _P(V, k):
     return np.einsum("nat,nbt->nab", V, V) + 1.0 / k
 
 
-@pytest.mark.parametrize("n,d,k,td", [(1500, 8, 12, 2), (3000, 32, 20, 2), (2000, 16, 10, 3), (1000, 64, 30, 2)])
+@pytest.mark.parametrize("n,d,k,td", [(1500, 8, 12, 2), (3000, 32, 20, 2), (2000, 16, 10, 3), (1000, 64, 30, 2),
+                                      (1500, 16, 40, 2), (1200, 8, 64, 3), (1500, 32, 22, 2)])
 def test_ltsa_basis(ctx, n, d, k, td):
     X = datasets.lifted_s_curve(n, d, seed=n, noise=0.02)
     idx, _, _ = oracle.knn_brute(X, k)
