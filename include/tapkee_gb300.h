@@ -233,6 +233,55 @@ int tk_operator_get_info(const tk_ctx* ctx, tk_operator_info* info);
 /* Waits for all work queued on the context's stream. */
 int tk_ctx_synchronize(tk_ctx* ctx);
 
+/* ---- batches of independent problems ------------------------------------------ */
+
+/* Many independent KLLE stages (the part of embed() that tk_local_operator runs,
+ * without the connectivity retry) of uneven N, D and k, planned once and replayed
+ * as one CUDA graph: one persistent tensor-core screen launch per group of
+ * problems with the same padded dimension and candidate-list length, one launch
+ * per stage for the rest. No counterpart in the reference, which embeds one data
+ * set per call; each problem's result equals tk_local_operator's on it (the same
+ * neighbours, weights within 1e-5, the same M structure). */
+typedef struct tk_batch tk_batch;
+
+typedef struct tk_batch_problem
+{
+    const void* X; /* device memory, points-major N x D, row stride ldx     */
+    int dtype;     /* TK_F32 or TK_F64                                      */
+    int64_t N;
+    int D;         /* 1..128                                                */
+    int64_t ldx;
+    int k;         /* 1..min(56, N-1)                                       */
+} tk_batch_problem;
+
+/* Tile shapes of a batch (picked by the autotuner, tapkee_gb300/autotune.py). */
+typedef struct tk_batch_tuning
+{
+    int screen_qt[2]; /* query blocks of 128 rows per screen work item for padded
+                         dimension 64 (1 or 2) and 128 (1)                       */
+    int lle_warps;    /* problems per block of the weight solve: 4 or 8 warps    */
+    int wide_lists;   /* 1: 64 screened candidates per row for every k, else the
+                         smallest list >= k + 8 (32 or 64)                        */
+} tk_batch_tuning;
+
+void tk_batch_tuning_default(tk_batch_tuning* tuning);
+
+/* Plans the batch on ctx's device and stream, runs it once and captures it as a
+ * CUDA graph. The X buffers must stay valid (their contents may change) for the
+ * life of the batch. tuning may be NULL (defaults). */
+int tk_batch_create(tk_ctx* ctx, const tk_batch_problem* problems, int count, double klle_shift,
+                    double nullspace_shift, const tk_batch_tuning* tuning, tk_batch** out);
+/* Replays the graph and waits for it; ms_out (may be NULL) = device time. */
+int tk_batch_run(tk_batch* batch, float* ms_out);
+int tk_batch_count(const tk_batch* batch);
+/* n, k, nnz of problem p (caller numbering); rows_uncertified counts its screen group. */
+int tk_batch_get_info(tk_batch* batch, int p, tk_operator_info* info);
+/* Problem p's neighbours (N x k), weights (N x k), and M in CSR (N+1, nnz, nnz),
+ * numbered within the problem. Host or device buffers; any may be NULL. */
+int tk_batch_copy(tk_batch* batch, int p, int32_t* idx, double* weights, int64_t* row_ptr, int32_t* col_idx,
+                  double* vals);
+int tk_batch_destroy(tk_batch* batch);
+
 /* ---- allocation-free entry point --------------------------------------------- */
 
 /* Largest graph tk_check_connected_noalloc accepts, and the size of the static

@@ -49,6 +49,15 @@ class tk_knn_stats(ctypes.Structure):
     _fields_ = [("rows_uncertified", ctypes.c_int64), ("candidates", ctypes.c_int32), ("screen", ctypes.c_int32)]
 
 
+class tk_batch_problem(ctypes.Structure):
+    _fields_ = [("X", ctypes.c_void_p), ("dtype", ctypes.c_int), ("N", ctypes.c_int64), ("D", ctypes.c_int),
+                ("ldx", ctypes.c_int64), ("k", ctypes.c_int)]
+
+
+class tk_batch_tuning(ctypes.Structure):
+    _fields_ = [("screen_qt", ctypes.c_int * 2), ("lle_warps", ctypes.c_int), ("wide_lists", ctypes.c_int)]
+
+
 class tk_operator_info(ctypes.Structure):
     _fields_ = [
         ("n", ctypes.c_int64),
@@ -89,6 +98,14 @@ SIGNATURES = {
                                       ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "tk_operator_get_info": (_I, [_P, ctypes.POINTER(tk_operator_info)]),
     "tk_ctx_synchronize": (_I, [_P]),
+    "tk_batch_tuning_default": (None, [ctypes.POINTER(tk_batch_tuning)]),
+    "tk_batch_create": (_I, [_P, ctypes.POINTER(tk_batch_problem), _I, _D, _D, ctypes.POINTER(tk_batch_tuning),
+                             ctypes.POINTER(_P)]),
+    "tk_batch_run": (_I, [_P, ctypes.POINTER(ctypes.c_float)]),
+    "tk_batch_count": (_I, [_P]),
+    "tk_batch_get_info": (_I, [_P, _I, ctypes.POINTER(tk_operator_info)]),
+    "tk_batch_copy": (_I, [_P, _I, _P, _P, _P, _P, _P]),
+    "tk_batch_destroy": (_I, [_P]),
     "tk_check_connected_noalloc": (_I, [_I, _P, _I64, _I, _P, ctypes.POINTER(_I), ctypes.c_char_p,
                                         ctypes.c_size_t]),
 }

@@ -524,7 +524,8 @@ int rows_grid(tk_ctx* ctx, int64_t N)
 }
 } // namespace
 
-int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, int64_t* row_ptr)
+void assemble_symbolic_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
+                              int64_t* row_ptr)
 {
     cudaStream_t st = ctx->stream;
     const int64_t nk = N * (int64_t)k;
@@ -555,8 +556,13 @@ int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, con
                                                                            ctx->dev_err);
     TK_CHECK_LAUNCH();
     scan_to_offsets(ctx, a.row_nnz, N, row_ptr);
-    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    TK_CUDA(cudaStreamSynchronize(st));
+}
+
+int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, int64_t* row_ptr)
+{
+    assemble_symbolic_device(ctx, method, N, k, td, idx, row_ptr);
+    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    TK_CUDA(cudaStreamSynchronize(ctx->stream));
     return ctx->host_i64[0];
 }
 

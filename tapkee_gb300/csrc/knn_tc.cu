@@ -40,17 +40,23 @@ constexpr int TC_M = 128;      // queries per A tile (MMA M)
 constexpr int TC_THREADS = 320;
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per single wait
 
-template <int DP>
+// QT query blocks of 128 rows share each candidate tile (QT = 2 only for DP = 64:
+// two 128-column accumulators double-buffered fill the 512 TMEM columns).
+template <int DP, int QT_ = (DP <= 64) ? 2 : 1>
 struct TcCfg
 {
-    static constexpr int QT = (DP <= 64) ? 2 : 1;  // A tiles (query blocks) per CTA
+    static constexpr int QT = QT_;                 // A tiles (query blocks) per work item
     static constexpr int KATOMS = DP / 64;         // 128-byte swizzle atoms along K
     static constexpr int ATOM_BYTES = 128 * 128;   // 128 rows x 128 B (SW128)
     static constexpr int EXTRA_BYTES = 128 * 32;   // 128 rows x 32 B (SW32): the norm column slice
     static constexpr int A_BYTES = QT * 2 * KATOMS * ATOM_BYTES;
-    static constexpr int STAGES = (DP <= 64) ? 4 : 2;
     static constexpr int B_OPER_BYTES = 2 * KATOMS * ATOM_BYTES;        // hi + lo
     static constexpr int B_STAGE_BYTES = B_OPER_BYTES + EXTRA_BYTES;    // + norm column
+    // as many candidate stages as fit in 227 KB next to the A tiles, the norm
+    // slice, the barriers and the stash (at most 6)
+    static constexpr int FIXED_BYTES = EXTRA_BYTES + 256 + 8 * 32 * (8 + 1) * 4 + 1024;
+    static constexpr int STAGES_FIT = (227 * 1024 - A_BYTES - FIXED_BYTES) / B_STAGE_BYTES;
+    static constexpr int STAGES = STAGES_FIT > 6 ? 6 : STAGES_FIT;
     static constexpr int ACC_COLS = QT * TC_N;
     static constexpr int TMEM_COLS = 2 * ACC_COLS;  // 512 or 256, power of two
     static constexpr int EPI_WARPS = 4 * QT;
@@ -59,6 +65,7 @@ struct TcCfg
     static constexpr size_t OFF_BAR = OFF_AX + EXTRA_BYTES;
     static constexpr size_t OFF_STASH = OFF_BAR + 256;
     static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 1024 /*align*/;
+    static_assert(STAGES >= 2, "at least two candidate stages");
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -220,19 +227,66 @@ __device__ __forceinline__ void reg_insert(float (&L)[KC], int32_t (&I)[KC], flo
 
 struct TcBarriers
 {
-    uint64_t full[4], empty[4], tfull[2][2], tempty[2][2], afull, fin;  // t* : [buffer][query block]
+    uint64_t full[6], empty[6], tfull[2][2], tempty[2][2], afull, aempty, fin;  // t* : [buffer][query block]
     uint32_t tmem_base;
     int abort;
 };
 
-template <int DP, int KC>
+// One unit of screening work: QT query blocks starting at stacked row q0, against
+// the ntiles candidate tiles of one problem, which start at stacked tile t0.
+struct Item
+{
+    int64_t q0;
+    int t0, ntiles;
+    int64_t n;  // points of the problem (candidate ids >= n are padding)
+    float s;    // scale exponent of the problem's fp16 split
+};
+
+// Work of one launch. Single problem: items == nullptr and CTA b owns the query
+// rows [b QT 128, (b + 1) QT 128). Batch: a persistent grid walks the items
+// (stacked row q0, first tile, tiles, problem) in steps of gridDim.x; every warp
+// role walks the same sequence, so the pipeline phases stay in step.
+struct ScreenWork
+{
+    const int4* items;
+    int nitems;
+    const int64_t* prob_n;
+    const float* prob_scale;
+};
+
+template <int QROWS, bool BATCH>
+__device__ __forceinline__ Item fetch_item(const ScreenWork& W, int j, int64_t N, int ntiles, const float* scale)
+{
+    Item it;
+    if constexpr (!BATCH)
+    {
+        it.q0 = (int64_t)j * QROWS;
+        it.t0 = 0;
+        it.ntiles = ntiles;
+        it.n = N;
+        it.s = scale[0];
+    }
+    else
+    {
+        const int4 v = W.items[j];
+        it.q0 = (int64_t)v.x * QROWS;
+        it.t0 = v.y;
+        it.ntiles = v.z;
+        it.n = W.prob_n[v.w];
+        it.s = W.prob_scale[v.w];
+    }
+    return it;
+}
+
+template <int DP, int KC, int QT, bool BATCH>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_screen_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
                 const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
-                int64_t Npad, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
+                int64_t Npad, ScreenWork work, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
                 const float* __restrict__ nrm, unsigned* err)
 {
-    using C = TcCfg<DP>;
+    using C = TcCfg<DP, QT>;
+    constexpr int QROWS = C::QT * TC_M;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned operand region
     const uint32_t raw = smem_u32(smem_raw);
@@ -246,8 +300,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     volatile int* abort = &Bar.abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ntiles = (int)(Npad / TC_N);
-    const int64_t q0 = (int64_t)blockIdx.x * (C::QT * TC_M);
+    const int ntiles1 = (int)(Npad / TC_N);
+    // single problem: exactly one item, this CTA's; batch: a strided walk
+    const int j_first = (int)blockIdx.x;
+    const int j_end = BATCH ? work.nitems : j_first + 1;
+    const int j_step = BATCH ? (int)gridDim.x : 1;
 
     if (threadIdx.x == 0)
     {
@@ -265,6 +322,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
         mbar_init(smem_u32(&Bar.afull), 1);
+        mbar_init(smem_u32(&Bar.aempty), 1);
         mbar_init(smem_u32(&Bar.fin), 1);
         Bar.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -291,38 +349,52 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (lane == 0)
         {
             const uint32_t afull = smem_u32(&Bar.afull);
-            mbar_expect_tx(afull, C::A_BYTES);
-            for (int qt = 0; qt < C::QT; ++qt)
-                for (int part = 0; part < 2; ++part)
-                    for (int ka = 0; ka < C::KATOMS; ++ka)
-                        tma_load_2d(A_s + ((qt * 2 + part) * C::KATOMS + ka) * C::ATOM_BYTES, part ? &tm_lo : &tm_hi,
-                                    ka * 64, (int)(q0 + qt * TC_M), afull);
-            ZigZag zz((int)blockIdx.x * C::QT, ntiles);
-            int issued = 0;
-            for (int it = 0; it < ntiles; ++it)
+            int gi = 0;      // candidate tiles issued so far (all items)
+            int na = 0;      // A loads issued
+            bool ok = true;
+            for (int j = j_first; ok && j < j_end; j += j_step)
             {
-                const int tile = zz.next();
-                const int slot = it % C::STAGES;
-                const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
-                if (!mbar_wait(smem_u32(&Bar.empty[slot]), ph ^ 1u, abort, err))
+                const Item I = fetch_item<QROWS, BATCH>(work, j, N, ntiles1, scale_log2);
+                // the previous item's MMAs must be done reading the A tiles
+                if (na > 0 && !mbar_wait(smem_u32(&Bar.aempty), (uint32_t)(na - 1) & 1u, abort, err))
                     break;
-                const uint32_t fb = smem_u32(&Bar.full[slot]);
-                const uint32_t bst = B_s + slot * C::B_STAGE_BYTES;
-                mbar_expect_tx(fb, C::B_STAGE_BYTES);
-                for (int part = 0; part < 2; ++part)
-                    for (int ka = 0; ka < C::KATOMS; ++ka)
-                        tma_load_2d(bst + (part * C::KATOMS + ka) * C::ATOM_BYTES, part ? &tm_lo : &tm_hi, ka * 64,
-                                    tile * TC_N, fb);
-                tma_load_2d(bst + C::B_OPER_BYTES, &tm_nrm, 0, tile * TC_N, fb);
-                issued = it + 1;
+                mbar_expect_tx(afull, C::A_BYTES);
+                for (int qt = 0; qt < C::QT; ++qt)
+                    for (int part = 0; part < 2; ++part)
+                        for (int ka = 0; ka < C::KATOMS; ++ka)
+                            tma_load_2d(A_s + ((qt * 2 + part) * C::KATOMS + ka) * C::ATOM_BYTES,
+                                        part ? &tm_lo : &tm_hi, ka * 64, (int)(I.q0 + qt * TC_M), afull);
+                ++na;
+                ZigZag zz((int)(I.q0 / TC_N) - I.t0, I.ntiles);
+                for (int it = 0; it < I.ntiles; ++it)
+                {
+                    const int tile = I.t0 + zz.next();
+                    const int slot = gi % C::STAGES;
+                    const uint32_t ph = (uint32_t)(gi / C::STAGES) & 1u;
+                    if (!mbar_wait(smem_u32(&Bar.empty[slot]), ph ^ 1u, abort, err))
+                    {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t fb = smem_u32(&Bar.full[slot]);
+                    const uint32_t bst = B_s + slot * C::B_STAGE_BYTES;
+                    mbar_expect_tx(fb, C::B_STAGE_BYTES);
+                    for (int part = 0; part < 2; ++part)
+                        for (int ka = 0; ka < C::KATOMS; ++ka)
+                            tma_load_2d(bst + (part * C::KATOMS + ka) * C::ATOM_BYTES, part ? &tm_lo : &tm_hi,
+                                        ka * 64, tile * TC_N, fb);
+                    tma_load_2d(bst + C::B_OPER_BYTES, &tm_nrm, 0, tile * TC_N, fb);
+                    ++gi;
+                }
             }
             if (*abort)
             {
                 // drain the loads still in flight (bounded)
                 volatile int no_abort = 0;
-                mbar_wait(afull, 0u, &no_abort, err);
-                for (int j = (issued > C::STAGES ? issued - C::STAGES : 0); j < issued; ++j)
-                    mbar_wait(smem_u32(&Bar.full[j % C::STAGES]), (uint32_t)(j / C::STAGES) & 1u, &no_abort, err);
+                if (na > 0)
+                    mbar_wait(afull, (uint32_t)(na - 1) & 1u, &no_abort, err);
+                for (int g = (gi > C::STAGES ? gi - C::STAGES : 0); g < gi; ++g)
+                    mbar_wait(smem_u32(&Bar.full[g % C::STAGES]), (uint32_t)(g / C::STAGES) & 1u, &no_abort, err);
             }
         }
     }
@@ -331,8 +403,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ------------------------------------------------------------ MMA issuer
         if (lane == 0)
         {
-            bool ok = mbar_wait(smem_u32(&Bar.afull), 0u, abort, err);
-            tc_fence_after();
             int issued_any = 0;
             const uint64_t axd = umma_desc_sw32(AX_s);
             // descriptors of every A slice (constant) and of stage 0's B slices;
@@ -354,45 +424,61 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     bdesc0[part][kk] =
                         umma_desc(B_s + (part * C::KATOMS + (kk >> 2)) * C::ATOM_BYTES + (uint32_t)(kk & 3) * 32u);
             const uint64_t bx0 = umma_desc_sw32(B_s + C::B_OPER_BYTES);
-            for (int it = 0; ok && it < ntiles; ++it)
+            int gi = 0, na = 0;
+            bool ok = true;
+            for (int j = j_first; ok && j < j_end; j += j_step)
             {
-                const int slot = it % C::STAGES;
-                const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
-                const int buf = it & 1;
-                const uint32_t bph = (uint32_t)(it >> 1) & 1u;
-                if (!mbar_wait(smem_u32(&Bar.full[slot]), ph, abort, err))
+                const Item I = fetch_item<QROWS, BATCH>(work, j, N, ntiles1, scale_log2);
+                if (!mbar_wait(smem_u32(&Bar.afull), (uint32_t)na & 1u, abort, err))
                     break;
-                const uint64_t soff = (uint64_t)((slot * C::B_STAGE_BYTES) >> 4);
-                bool ok_q = true;
-                // each query block's accumulator half has its own handoff, so its
-                // epilogue warps start as soon as its 13 MMAs are done
-#pragma unroll
-                for (int qt = 0; qt < C::QT; ++qt)
+                ++na;
+                tc_fence_after();
+                for (int it = 0; it < I.ntiles; ++it)
                 {
-                    if (!mbar_wait(smem_u32(&Bar.tempty[buf][qt]), bph ^ 1u, abort, err))
+                    const int slot = gi % C::STAGES;
+                    const uint32_t ph = (uint32_t)(gi / C::STAGES) & 1u;
+                    const int buf = gi & 1;
+                    const uint32_t bph = (uint32_t)(gi >> 1) & 1u;
+                    if (!mbar_wait(smem_u32(&Bar.full[slot]), ph, abort, err))
                     {
-                        ok_q = false;
+                        ok = false;
                         break;
                     }
-                    tc_fence_after();
-                    const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
-                    // norm step first: D = 2^13 (h + l) of -|2^s y|^2 / 2^14
-                    umma_f16(d, axd, bx0 + soff, 0u);
+                    const uint64_t soff = (uint64_t)((slot * C::B_STAGE_BYTES) >> 4);
+                    // each query block's accumulator half has its own handoff, so its
+                    // epilogue warps start as soon as its 13 MMAs are done
 #pragma unroll
-                    for (int prod = 0; prod < 3; ++prod)
+                    for (int qt = 0; qt < C::QT; ++qt)
                     {
-                        const int apart = (prod == 2) ? 1 : 0;  // l_x . h_y
-                        const int bpart = (prod == 1) ? 1 : 0;  // h_x . l_y
+                        if (!mbar_wait(smem_u32(&Bar.tempty[buf][qt]), bph ^ 1u, abort, err))
+                        {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
+                        // norm step first: D = 2^13 (h + l) of -|2^s y|^2 / 2^14
+                        umma_f16(d, axd, bx0 + soff, 0u);
 #pragma unroll
-                        for (int kk = 0; kk < DP / 16; ++kk)
-                            umma_f16(d, adesc[qt][apart][kk], bdesc0[bpart][kk] + soff, 1u);
+                        for (int prod = 0; prod < 3; ++prod)
+                        {
+                            const int apart = (prod == 2) ? 1 : 0;  // l_x . h_y
+                            const int bpart = (prod == 1) ? 1 : 0;  // h_x . l_y
+#pragma unroll
+                            for (int kk = 0; kk < DP / 16; ++kk)
+                                umma_f16(d, adesc[qt][apart][kk], bdesc0[bpart][kk] + soff, 1u);
+                        }
+                        umma_commit(smem_u32(&Bar.tfull[buf][qt]));
+                        issued_any = 1;
                     }
-                    umma_commit(smem_u32(&Bar.tfull[buf][qt]));
-                    issued_any = 1;
+                    if (!ok)
+                        break;
+                    umma_commit(smem_u32(&Bar.empty[slot]));
+                    ++gi;
                 }
-                if (!ok_q)
-                    break;
-                umma_commit(smem_u32(&Bar.empty[slot]));
+                // the A tiles are free once this item's MMAs complete
+                if (ok)
+                    umma_commit(smem_u32(&Bar.aempty));
             }
             if (issued_any)
             {
@@ -410,84 +496,94 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int quad = warp & 3;
         const int qt = warp >> 2;
         const int row = quad * 32 + lane;
-        const int64_t q = q0 + qt * TC_M + row;
-        const float nq = nrm[q];
-        // |y|^2 - 2 x.y = m2 * acc, m2 = -2^(1-2s) (exact power of two)
-        const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);
-        const float inv_m2 = 1.0f / m2;
         float* stash = stash_all + (warp * 32 + lane) * (C::STASH + 1);
-        float L[KC];
-        int32_t I[KC];
+        int gi = 0;
+        bool alive = true;
+        for (int j = j_first; alive && j < j_end; j += j_step)
+        {
+            const Item I = fetch_item<QROWS, BATCH>(work, j, N, ntiles1, scale_log2);
+            const int64_t q = I.q0 + qt * TC_M + row;
+            const float nq = nrm[q];
+            // |y|^2 - 2 x.y = m2 * acc, m2 = -2^(1-2s) (exact power of two)
+            const float m2 = -exp2f(1.0f - 2.0f * I.s);
+            const float inv_m2 = 1.0f / m2;
+            float L[KC];
+            int32_t Ix[KC];
 #pragma unroll
-        for (int s = 0; s < KC; ++s)
-        {
-            L[s] = FLT_MAX;
-            I[s] = -1;
-        }
-        float cmp = FLT_MAX;
-        float thr = -__int_as_float(0x7f800000);  // accept everything until the list fills
-        ZigZag zz((int)blockIdx.x * C::QT, ntiles);
-        for (int it = 0; it < ntiles; ++it)
-        {
-            const int tile = zz.next();
-            const int buf = it & 1;
-            const uint32_t bph = (uint32_t)(it >> 1) & 1u;
-            // tcgen05.ld is warp-collective: leave the loop as a whole warp
-            const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf][qt]), bph, abort, err);
-            if (!__all_sync(0xffffffffu, ok))
-                break;
-            tc_fence_after();
-            const int64_t c0 = (int64_t)tile * TC_N;
-            const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
-            // columns per TMEM wait: 64 with 32-entry lists, 32 with 64-entry lists
-            constexpr int CPW = (KC <= 32) ? 64 : 32;
-#pragma unroll 1
-            for (int h = 0; h < TC_N / CPW; ++h)
+            for (int s = 0; s < KC; ++s)
             {
-                float v[CPW];
-                tmem_ld32_nowait(tacc + h * CPW, v);
-                if (CPW == 64)
-                    tmem_ld32_nowait(tacc + h * CPW + 32, v + 32);
-                tmem_wait_ld();
-                if (h == TC_N / CPW - 1)
+                L[s] = FLT_MAX;
+                Ix[s] = -1;
+            }
+            float cmp = FLT_MAX;
+            float thr = -__int_as_float(0x7f800000);  // accept everything until the list fills
+            ZigZag zz((int)(I.q0 / TC_N) - I.t0, I.ntiles);
+            for (int it = 0; it < I.ntiles; ++it)
+            {
+                const int tile = zz.next();  // local to the problem
+                const int buf = gi & 1;
+                const uint32_t bph = (uint32_t)(gi >> 1) & 1u;
+                ++gi;
+                // tcgen05.ld is warp-collective: leave the loop as a whole warp
+                const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf][qt]), bph, abort, err);
+                if (!__all_sync(0xffffffffu, ok))
                 {
-                    // the last columns are in registers: hand the buffer back now
-                    tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0)
-                        mbar_arrive(smem_u32(&Bar.tempty[buf][qt]));
+                    alive = false;
+                    break;
                 }
-#pragma unroll
-                for (int s32 = 0; s32 < CPW / 32; ++s32)
+                tc_fence_after();
+                const int64_t c0 = (int64_t)tile * TC_N;
+                const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
+                // columns per TMEM wait: 64 with 32-entry lists, 32 with 64-entry lists
+                constexpr int CPW = (KC <= 32) ? 64 : 32;
+#pragma unroll 1
+                for (int h = 0; h < TC_N / CPW; ++h)
                 {
-                    float gm[4];
-#pragma unroll
-                    for (int g = 0; g < 4; ++g)
+                    float v[CPW];
+                    tmem_ld32_nowait(tacc + h * CPW, v);
+                    if (CPW == 64)
+                        tmem_ld32_nowait(tacc + h * CPW + 32, v + 32);
+                    tmem_wait_ld();
+                    if (h == TC_N / CPW - 1)
                     {
-                        const float* w = v + s32 * 32 + g * 8;
-                        gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
-                                      fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
+                        // the last columns are in registers: hand the buffer back now
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0)
+                            mbar_arrive(smem_u32(&Bar.tempty[buf][qt]));
                     }
-                    if (fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3])) > thr)
+#pragma unroll
+                    for (int s32 = 0; s32 < CPW / 32; ++s32)
                     {
+                        float gm[4];
 #pragma unroll
                         for (int g = 0; g < 4; ++g)
                         {
-                            if (gm[g] > thr)
-                            {
+                            const float* w = v + s32 * 32 + g * 8;
+                            gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
+                                          fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
+                        }
+                        if (fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3])) > thr)
+                        {
 #pragma unroll
-                                for (int e = 0; e < 8; ++e)
-                                    stash[e] = v[s32 * 32 + g * 8 + e];
-                                const int64_t cb = c0 + h * CPW + s32 * 32 + g * 8;
-#pragma unroll 1
-                                for (int e = 0; e < 8; ++e)
+                            for (int g = 0; g < 4; ++g)
+                            {
+                                if (gm[g] > thr)
                                 {
-                                    const float t = m2 * stash[e];
-                                    if (t < cmp && cb + e < N)
+#pragma unroll
+                                    for (int e = 0; e < 8; ++e)
+                                        stash[e] = v[s32 * 32 + g * 8 + e];
+                                    const int64_t cb = c0 + h * CPW + s32 * 32 + g * 8;
+#pragma unroll 1
+                                    for (int e = 0; e < 8; ++e)
                                     {
-                                        reg_insert<KC>(L, I, t, (int32_t)(cb + e));
-                                        cmp = L[KC - 1];
-                                        thr = cmp * inv_m2;
+                                        const float t = m2 * stash[e];
+                                        if (t < cmp && cb + e < I.n)
+                                        {
+                                            reg_insert<KC>(L, Ix, t, (int32_t)(cb + e));
+                                            cmp = L[KC - 1];
+                                            thr = cmp * inv_m2;
+                                        }
                                     }
                                 }
                             }
@@ -495,12 +591,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     }
                 }
             }
-        }
+            if (!alive)
+                break;
 #pragma unroll
-        for (int s = 0; s < KC; ++s)
-        {
-            cand_idx[q * KC + s] = I[s];
-            cand_val[q * KC + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+            for (int s = 0; s < KC; ++s)
+            {
+                cand_idx[q * KC + s] = Ix[s];
+                cand_val[q * KC + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+            }
         }
     }
 
@@ -541,20 +639,30 @@ void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int 
         throw Error(TK_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
 }
 
-template <int DP, int KC>
-void launch(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
+template <int DP, int KC, int QT = TcCfg<DP>::QT, bool BATCH = false>
+void launch(tk_ctx* ctx, const uint16_t* xh, const uint16_t* xl, const uint16_t* xn, const float* nrm,
+            int64_t rows, const float* scale, int64_t N, const ScreenWork& work, int grid, int32_t* cand_idx,
+            float* cand_val)
 {
-    using C = TcCfg<DP>;
+    using C = TcCfg<DP, QT>;
     static_assert(C::SMEM <= 227 * 1024, "shared memory budget");
     CUtensorMap mh, ml, mn;
-    make_map(&mh, P.xh, P.Npad, P.Dp, 64, CU_TENSOR_MAP_SWIZZLE_128B);
-    make_map(&ml, P.xl, P.Npad, P.Dp, 64, CU_TENSOR_MAP_SWIZZLE_128B);
-    make_map(&mn, P.xn, P.Npad, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B);
-    TK_CUDA(cudaFuncSetAttribute(k_screen_tc<DP, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
-    const int grid = (int)(P.Npad / (C::QT * TC_M));
-    k_screen_tc<DP, KC><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, mn, P.rmax + 1, P.N, P.Npad, cand_idx,
-                                                                    cand_val, P.nrm, ctx->dev_err);
+    make_map(&mh, xh, rows, DP, 64, CU_TENSOR_MAP_SWIZZLE_128B);
+    make_map(&ml, xl, rows, DP, 64, CU_TENSOR_MAP_SWIZZLE_128B);
+    make_map(&mn, xn, rows, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B);
+    TK_CUDA(cudaFuncSetAttribute(k_screen_tc<DP, KC, QT, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)C::SMEM));
+    k_screen_tc<DP, KC, QT, BATCH><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, mn, scale, N, rows, work, cand_idx,
+                                                                        cand_val, nrm, ctx->dev_err);
     TK_CHECK_LAUNCH();
+}
+
+template <int DP, int KC>
+void launch_single(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
+{
+    const ScreenWork single{nullptr, 0, nullptr, nullptr};
+    const int grid = (int)(P.Npad / (TcCfg<DP>::QT * TC_M));
+    launch<DP, KC>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single, grid, cand_idx, cand_val);
 }
 
 } // namespace
@@ -568,21 +676,46 @@ void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, fl
     if (P.Dp == 64)
     {
         if (kc == 32)
-            launch<64, 32>(ctx, P, cand_idx, cand_val);
+            launch_single<64, 32>(ctx, P, cand_idx, cand_val);
         else
-            launch<64, 64>(ctx, P, cand_idx, cand_val);
+            launch_single<64, 64>(ctx, P, cand_idx, cand_val);
     }
     else if (P.Dp == 128)
     {
         if (kc == 32)
-            launch<128, 32>(ctx, P, cand_idx, cand_val);
+            launch_single<128, 32>(ctx, P, cand_idx, cand_val);
         else
-            launch<128, 64>(ctx, P, cand_idx, cand_val);
+            launch_single<128, 64>(ctx, P, cand_idx, cand_val);
     }
     else
         throw Error(TK_ERR_UNSUPPORTED, "the tensor-core screen supports D <= 128 (padded to 64 or 128); use the "
                                         "FP32 screen for D = " +
                                             std::to_string(P.D));
+}
+
+void screen_tensor_batch(tk_ctx* ctx, const StackedScreen& S, int32_t* cand_idx, float* cand_val)
+{
+    const ScreenWork work{S.items, S.nitems, S.prob_n, S.prob_scale};
+    const int grid = std::min(S.nitems, ctx->num_sms);
+    if (grid <= 0)
+        return;
+#define TK_SCREEN_BATCH(DPV, KCV, QTV)                                                                            \
+    launch<DPV, KCV, QTV, true>(ctx, S.xh, S.xl, S.xn, S.nrm, S.rows, nullptr, 0, work, grid, cand_idx, cand_val)
+    if (S.Dp == 64 && S.kc == 32 && S.qt == 2)
+        TK_SCREEN_BATCH(64, 32, 2);
+    else if (S.Dp == 64 && S.kc == 32 && S.qt == 1)
+        TK_SCREEN_BATCH(64, 32, 1);
+    else if (S.Dp == 64 && S.kc == 64 && S.qt == 2)
+        TK_SCREEN_BATCH(64, 64, 2);
+    else if (S.Dp == 64 && S.kc == 64 && S.qt == 1)
+        TK_SCREEN_BATCH(64, 64, 1);
+    else if (S.Dp == 128 && S.kc == 32)
+        TK_SCREEN_BATCH(128, 32, 1);
+    else if (S.Dp == 128 && S.kc == 64)
+        TK_SCREEN_BATCH(128, 64, 1);
+    else
+        throw Error(TK_ERR_UNSUPPORTED, "batched tensor screen: unsupported (Dp, KC, QT)");
+#undef TK_SCREEN_BATCH
 }
 
 } // namespace tk

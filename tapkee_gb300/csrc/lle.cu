@@ -75,11 +75,27 @@ __device__ __forceinline__ void chol_solve(LleSmem<KP>& S, int lane)
     __syncwarp();
 }
 
-template <int KP, int WARPS, bool BLOCKED = (KP <= 64)>
-__global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, int64_t N, int D, int64_t ldx,
-                                                    const int32_t* __restrict__ idx, int k, double klle_shift,
-                                                    const double* __restrict__ rhs, int normalize,
-                                                    double* __restrict__ W, unsigned* err)
+// Rows of one launch: the points of one problem (row_prob == NULL; row g is
+// point g), or the rows of a batch's k-group (row g belongs to problem
+// row_prob[g], at point out_row0 + g - probs[.].out_row0 of it). idx, W and rhs
+// are indexed by row.
+struct LleRows
+{
+    const void* X;
+    int dtype;
+    int64_t N;
+    int D;
+    int64_t ldx;
+    int64_t rows;
+    const int32_t* row_prob;
+    const BatchProb* probs;
+    int64_t out_row0;
+};
+
+template <int KP, int WARPS, bool BATCH, bool BLOCKED = (KP <= 64)>
+__global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int32_t* __restrict__ idx, int k,
+                                                    double klle_shift, const double* __restrict__ rhs,
+                                                    int normalize, double* __restrict__ W, unsigned* err)
 {
     constexpr int NB4 = KP / 4;
     constexpr int NBLK = BLOCKED ? NB4 * (NB4 + 1) / 2 : 1;
@@ -113,14 +129,30 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         bG[m] = (itm < ITEMS) ? itm / NBLK : 0;
     }
 
-    for (int64_t i = warp; i < N; i += nwarps)
+    for (int64_t g = warp; g < RW.rows; g += nwarps)
     {
+        const void* X = RW.X;
+        int dtype = RW.dtype;
+        int64_t N = RW.N;
+        int D = RW.D;
+        int64_t ldx = RW.ldx;
+        int64_t i = g;
+        if constexpr (BATCH)
+        {
+            const BatchProb& P = RW.probs[RW.row_prob[g]];
+            X = P.X;
+            dtype = P.dtype;
+            N = P.N;
+            D = P.D;
+            ldx = P.ldx;
+            i = RW.out_row0 + g - P.out_row0;
+        }
         int nb[NPL];
 #pragma unroll
         for (int s = 0; s < NPL; ++s)
         {
             const int a = lane + 32 * s;
-            nb[s] = (a < k) ? idx[i * k + a] : 0;
+            nb[s] = (a < k) ? idx[g * k + a] : 0;
             if (a < k && (nb[s] < 0 || nb[s] >= N))
             {
                 atomicOr(err, DEV_ERR_BOUNDS);
@@ -246,7 +278,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
                 S.C[a][a] += shift;
             else
                 S.C[a][a] = 1.f;  // padding rows/columns are zero: identity block
-            S.r[a] = (a < k) ? (rhs ? (float)rhs[i * k + a] : 1.f) : 0.f;
+            S.r[a] = (a < k) ? (rhs ? (float)rhs[g * k + a] : 1.f) : 0.f;
         }
         __syncwarp();
 
@@ -346,7 +378,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
                 const int a_own = (KR == 32) ? lane : (lane >> 1);
                 const double shift_true = klle_shift * ff_to_double(trp);
                 if ((KR == 32 || (lane & 1) == 0) && a_own < KP)
-                    S.r[a_own] = (a_own < k) ? (float)((rhs ? rhs[i * k + a_own] : 1.0) - ff_to_double(part[0]) -
+                    S.r[a_own] = (a_own < k) ? (float)((rhs ? rhs[g * k + a_own] : 1.0) - ff_to_double(part[0]) -
                                                        shift_true * (double)S.w[a_own])
                                              : 0.f;
                 __syncwarp();
@@ -408,7 +440,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
                 {
                     const int a = lane + 32 * s;
                     if (a < KP)
-                        S.r[a] = (a < k) ? (float)((rhs ? rhs[i * k + a] : 1.0) - ff_to_double(sa[s]) -
+                        S.r[a] = (a < k) ? (float)((rhs ? rhs[g * k + a] : 1.0) - ff_to_double(sa[s]) -
                                                    shift_true * (double)S.w[a])
                                          : 0.f;
                 }
@@ -424,7 +456,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         if (!normalize)
         {
             for (int a = lane; a < k; a += 32)
-                W[i * k + a] = (double)S.w[a];
+                W[g * k + a] = (double)S.w[a];
             __syncwarp();
             continue;
         }
@@ -435,22 +467,43 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const void* X, int dtype, in
         for (int o = 16; o > 0; o >>= 1)
             sum += __shfl_xor_sync(0xffffffffu, sum, o);
         for (int a = lane; a < k; a += 32)
-            W[i * k + a] = (double)S.w[a] / sum;
+            W[g * k + a] = (double)S.w[a] / sum;
         __syncwarp();
     }
 }
 
-template <int KP, int WARPS>
-void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
-            double klle_shift, const double* rhs, int normalize, double* W)
+template <int KP, int WARPS, bool BATCH>
+void launch(tk_ctx* ctx, const LleRows& RW, const int32_t* idx, int k, double klle_shift, const double* rhs,
+            int normalize, double* W)
 {
     const size_t smem = sizeof(LleSmem<KP>) * WARPS;
-    TK_CUDA(cudaFuncSetAttribute(k_lle<KP, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t want = (N + WARPS - 1) / WARPS;
-    const int grid = (int)std::min<int64_t>(want, (int64_t)ctx->num_sms * 16);
-    k_lle<KP, WARPS><<<grid, WARPS * 32, smem, ctx->stream>>>(X, dtype, N, D, ldx, idx, k, klle_shift, rhs,
-                                                               normalize, W, ctx->dev_err);
+    TK_CUDA(cudaFuncSetAttribute(k_lle<KP, WARPS, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t want = (RW.rows + WARPS - 1) / WARPS;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 16));
+    k_lle<KP, WARPS, BATCH><<<grid, WARPS * 32, smem, ctx->stream>>>(RW, idx, k, klle_shift, rhs, normalize, W,
+                                                               ctx->dev_err);
     TK_CHECK_LAUNCH();
+}
+
+template <bool BATCH>
+void dispatch(tk_ctx* ctx, const LleRows& RW, const int32_t* idx, int k, double klle_shift, const double* rhs,
+              bool normalize, double* W, int warps)
+{
+    const int nm = normalize ? 1 : 0;
+    if (k <= 16 && warps == 4)
+        launch<16, 4, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
+    else if (k <= 16)
+        launch<16, 8, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
+    else if (k <= 32 && warps == 4)
+        launch<32, 4, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
+    else if (k <= 32)
+        launch<32, 8, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
+    else if (k <= 64)
+        launch<64, 4, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
+    else if (!BATCH && k <= 128)
+        launch<128, 1, false>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
+    else
+        throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 128 neighbours (64 in a batch)");
 }
 
 } // namespace
@@ -458,17 +511,15 @@ void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx
 void lle_solve(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
                double klle_shift, const double* rhs, bool normalize, double* W)
 {
-    const int nm = normalize ? 1 : 0;
-    if (k <= 16)
-        launch<16, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
-    else if (k <= 32)
-        launch<32, 8>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
-    else if (k <= 64)
-        launch<64, 4>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
-    else if (k <= 128)
-        launch<128, 1>(ctx, X, dtype, N, D, ldx, idx, k, klle_shift, rhs, nm, W);
-    else
-        throw Error(TK_ERR_UNSUPPORTED, "LLE weights support up to 128 neighbours");
+    const LleRows RW{X, dtype, N, D, ldx, N, nullptr, nullptr, 0};
+    dispatch<false>(ctx, RW, idx, k, klle_shift, rhs, normalize, W, 8);
+}
+
+void lle_weights_batch(tk_ctx* ctx, const BatchProb* probs, const int32_t* row_prob, int64_t out_row0, int64_t rows,
+                       const int32_t* idx, int k, double klle_shift, double* W, int warps)
+{
+    const LleRows RW{nullptr, 0, 0, 0, 0, rows, row_prob, probs, out_row0};
+    dispatch<true>(ctx, RW, idx, k, klle_shift, nullptr, true, W, warps);
 }
 
 void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,

@@ -74,30 +74,65 @@ __device__ __forceinline__ double exact_d2(const void* X, int dtype, int64_t ldx
     return ff_to_double(acc) + (double)cross;
 }
 
-constexpr int RR_CHUNK = 64;  // dimensions staged per pass
-constexpr int RR_WARPS = 8;
-
-struct RerankSmem
+// The problem a screened row belongs to, and the row's original index in it.
+struct RowView
 {
-    float q[RR_CHUNK];
+    const void* X;
+    int dtype;
+    int64_t ldx;
+    int D;
+    int64_t N;
+    int k;
+    int64_t i;
+    float R;
+    const int32_t* perm;  // candidate id -> original index (NULL: identity)
+    int32_t* idx_out;
+    double* d2_out;
 };
 
-template <int KC>
+template <bool BATCH>
+__device__ __forceinline__ bool row_view(const RowSpace& S, int64_t p, RowView& v)
+{
+    if constexpr (!BATCH)
+    {
+        v = RowView{S.X, S.dtype, S.ldx, S.D, S.N, S.k, (int64_t)S.perm[p], *S.R, S.perm, S.idx_out, S.d2_out};
+        return true;
+    }
+    const int b = S.row_prob[p];
+    if (b < 0)
+        return false;
+    const BatchProb& P = S.probs[b];
+    const int64_t i = p - P.row0;
+    if (i < 0 || i >= P.N)
+        return false;
+    v = RowView{P.X, P.dtype, P.ldx, P.D, P.N, P.k, i, S.prob_R[b], nullptr, S.idx_all + P.idx_off, nullptr};
+    return true;
+}
+
+constexpr int RR_WARPS = 8;
+
+template <int KC, bool BATCH>
 __global__ void __launch_bounds__(RR_WARPS * 32)
-    k_rerank(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k, const int32_t* perm, const float* nrm,
-             const float* rmax, const int32_t* cand_idx, const float* cand_val, float c1, float c2,
-             int32_t* idx_out, double* d2_out, int32_t* failed, double* failed_ub, unsigned* nfailed)
+    k_rerank(const RowSpace RS, int64_t rows, const float* nrm, const int32_t* cand_idx, const float* cand_val,
+             float c1, float c2, int32_t* failed, double* failed_ub, unsigned* nfailed)
 {
     constexpr int PER = (KC + 31) / 32;
-    __shared__ RerankSmem smem[RR_WARPS];
     const int lane = threadIdx.x & 31;
-    RerankSmem& S = smem[threadIdx.x >> 5];
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const double R = (double)*rmax;
-    for (int64_t p = warp; p < N; p += nwarps)
+    for (int64_t p = warp; p < rows; p += nwarps)
     {
-        const int64_t i = perm[p];
+        RowView V;
+        if (!row_view<BATCH>(RS, p, V))
+            continue;
+        const void* X = V.X;
+        const int dtype = V.dtype;
+        const int64_t ldx = V.ldx;
+        const int D = V.D;
+        const int64_t N = V.N;
+        const int k = V.k;
+        const int64_t i = V.i;
+        const double R = (double)V.R;
         double d[PER];
         int j[PER];
 #pragma unroll
@@ -112,7 +147,7 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                 const int c = cand_idx[p * KC + slot];
                 if (c >= 0 && c < N)
                 {
-                    jj = perm[c];
+                    jj = V.perm ? V.perm[c] : c;
                     if (jj == i)
                         jj = -1;
                 }
@@ -208,9 +243,9 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
             for (int s = 0; s < PER; ++s)
                 if (rank[s] < k)
                 {
-                    idx_out[i * k + rank[s]] = j[s];
-                    if (d2_out)
-                        d2_out[i * k + rank[s]] = d[s];
+                    V.idx_out[i * k + rank[s]] = j[s];
+                    if (V.d2_out)
+                        V.d2_out[i * k + rank[s]] = d[s];
                 }
         }
         else if (lane == 0)
@@ -223,10 +258,9 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
 }
 
 // Exact fallback: one CTA per failed row (persistent over the failed list).
-__global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int64_t ldx, int D, int64_t N, int k,
-                                                  const int32_t* perm, const int32_t* failed,
-                                                  const double* failed_ub, const unsigned* nfailed,
-                                                  int32_t* idx_out, double* d2_out, unsigned* err)
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_fallback(const RowSpace RS, const int32_t* failed,
+                                                  const double* failed_ub, const unsigned* nfailed, unsigned* err)
 {
     __shared__ int32_t sj[FB_CAP];
     __shared__ double sd[FB_CAP];
@@ -235,7 +269,18 @@ __global__ void __launch_bounds__(256) k_fallback(const void* X, int dtype, int6
     for (unsigned f = blockIdx.x; f < nf; f += gridDim.x)
     {
         const int64_t p = failed[f];
-        const int64_t i = perm[p];
+        RowView V;
+        if (!row_view<BATCH>(RS, p, V))
+            continue;
+        const void* X = V.X;
+        const int dtype = V.dtype;
+        const int64_t ldx = V.ldx;
+        const int D = V.D;
+        const int64_t N = V.N;
+        const int k = V.k;
+        const int64_t i = V.i;
+        int32_t* idx_out = V.idx_out;
+        double* d2_out = V.d2_out;
         const double ub = failed_ub[f];
         // FP32 direct-difference filter with a relative slack covering its error
         const double slack = (double)(D + 8) * 1.1920928955078125e-07;
@@ -317,20 +362,19 @@ void screen_error_model(int screen, int Dp, float* c1, float* c2)
     }
 }
 
-int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t ldx, int k, int kc,
-               const int32_t* cand_idx, const float* cand_val, float eps_c1, float eps_c2, int32_t* idx_out,
-               double* d2_out)
+namespace {
+
+template <bool BATCH>
+void launch_rerank(tk_ctx* ctx, const RowSpace& S, int64_t rows, int kc, const int32_t* cand_idx,
+                   const float* cand_val, const float* nrm, float eps_c1, float eps_c2, int32_t* failed,
+                   double* failed_ub, unsigned* nfailed)
 {
     cudaStream_t st = ctx->stream;
-    const int64_t N = P.N;
-    int32_t* failed = (int32_t*)ctx->scratch.get("rerank.failed", sizeof(int32_t) * (size_t)N);
-    double* failed_ub = (double*)ctx->scratch.get("rerank.failed_ub", sizeof(double) * (size_t)N);
-    unsigned* nfailed = (unsigned*)ctx->scratch.get("rerank.nfailed", 16);
-    TK_CUDA(cudaMemsetAsync(nfailed, 0, 16, st));
+    TK_CUDA(cudaMemsetAsync(nfailed, 0, sizeof(unsigned), st));
     const int blocks = 8 * ctx->num_sms;
 #define TK_RERANK(KCV)                                                                                         \
-    k_rerank<KCV><<<blocks, RR_WARPS * 32, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, P.nrm, P.rmax, cand_idx,    \
-                                          cand_val, eps_c1, eps_c2, idx_out, d2_out, failed, failed_ub, nfailed)
+    k_rerank<KCV, BATCH><<<blocks, RR_WARPS * 32, 0, st>>>(S, rows, nrm, cand_idx, cand_val, eps_c1, eps_c2, failed,    \
+                                                    failed_ub, nfailed)
     if (kc == 32)
         TK_RERANK(32);
     else if (kc == 64)
@@ -341,13 +385,46 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
         TK_RERANK(256);
     else
         throw Error(TK_ERR_INTERNAL, "rerank: unsupported candidate count");
+#undef TK_RERANK
     TK_CHECK_LAUNCH();
-    k_fallback<<<ctx->num_sms, 256, 0, st>>>(X, dtype, ldx, P.D, N, k, P.perm, failed, failed_ub, nfailed,
-                                             idx_out, d2_out, ctx->dev_err);
+    k_fallback<BATCH><<<ctx->num_sms, 256, 0, st>>>(S, failed, failed_ub, nfailed, ctx->dev_err);
     TK_CHECK_LAUNCH();
+}
+
+} // namespace
+
+int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t ldx, int k, int kc,
+               const int32_t* cand_idx, const float* cand_val, float eps_c1, float eps_c2, int32_t* idx_out,
+               double* d2_out)
+{
+    cudaStream_t st = ctx->stream;
+    const int64_t N = P.N;
+    int32_t* failed = (int32_t*)ctx->scratch.get("rerank.failed", sizeof(int32_t) * (size_t)N);
+    double* failed_ub = (double*)ctx->scratch.get("rerank.failed_ub", sizeof(double) * (size_t)N);
+    unsigned* nfailed = (unsigned*)ctx->scratch.get("rerank.nfailed", 16);
+    RowSpace S;
+    S.X = X;
+    S.dtype = dtype;
+    S.ldx = ldx;
+    S.D = P.D;
+    S.N = N;
+    S.k = k;
+    S.perm = P.perm;
+    S.R = P.rmax;
+    S.idx_out = idx_out;
+    S.d2_out = d2_out;
+    launch_rerank<false>(ctx, S, N, kc, cand_idx, cand_val, P.nrm, eps_c1, eps_c2, failed, failed_ub, nfailed);
     TK_CUDA(cudaMemcpyAsync(ctx->host_i64, nfailed, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     TK_CUDA(cudaStreamSynchronize(st));
     return (int64_t) * reinterpret_cast<unsigned*>(ctx->host_i64);
+}
+
+void rerank_batch(tk_ctx* ctx, const RowSpace& S, int64_t rows, int kc, const int32_t* cand_idx,
+                  const float* cand_val, const float* nrm, float eps_c1, float eps_c2, unsigned* nfailed_out)
+{
+    int32_t* failed = (int32_t*)ctx->scratch.get("rerank.failed", sizeof(int32_t) * (size_t)rows);
+    double* failed_ub = (double*)ctx->scratch.get("rerank.failed_ub", sizeof(double) * (size_t)rows);
+    launch_rerank<true>(ctx, S, rows, kc, cand_idx, cand_val, nrm, eps_c1, eps_c2, failed, failed_ub, nfailed_out);
 }
 
 } // namespace tk

@@ -118,6 +118,68 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
 constexpr int KCAND_MAX = 64;
 void screen_fp32(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
 void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
+
+// ---- batches of independent problems -----------------------------------------
+
+// One problem of a batch as the kernels see it.
+struct BatchProb
+{
+    const void* X;     // device points, row stride ldx
+    int dtype;
+    int D;
+    int64_t ldx;
+    int64_t N;
+    int k;
+    int group;         // screen group
+    int64_t row0;      // first stacked row in its screen group (multiple of 256)
+    int64_t idx_off;   // element offset of its rows in the neighbour and weight tables
+    int64_t out_row0;  // first row in the batch's output row space (problems ordered by k)
+};
+
+// Problems stacked for one batched screen launch (same Dp and KC).
+struct StackedScreen
+{
+    int Dp = 0, kc = 0, qt = 1;
+    int64_t rows = 0;                 // stacked rows (multiple of 256)
+    const uint16_t* xh = nullptr;     // rows x Dp fp16 hi / lo of 2^s (x - mean)
+    const uint16_t* xl = nullptr;
+    const uint16_t* xn = nullptr;     // rows x 16 fp16 norm column
+    const float* nrm = nullptr;       // rows squared norms (+inf for padding)
+    const int4* items = nullptr;      // (q0 / (qt 128), first tile, tiles, problem)
+    int nitems = 0;
+    const int64_t* prob_n = nullptr;  // per problem (batch numbering)
+    const float* prob_scale = nullptr;
+};
+void screen_tensor_batch(tk_ctx* ctx, const StackedScreen& S, int32_t* cand_idx, float* cand_val);
+
+// Where the rows handled by the re-rank live: one problem (rows in sorted order,
+// perm maps them back) or a batch (stacked rows; row_prob gives each row's problem
+// or -1 for padding).
+struct RowSpace
+{
+    const void* X = nullptr;
+    int dtype = 0;
+    int64_t ldx = 0;
+    int D = 0;
+    int64_t N = 0;
+    int k = 0;
+    const int32_t* perm = nullptr;
+    const float* R = nullptr;
+    int32_t* idx_out = nullptr;
+    double* d2_out = nullptr;
+    const int32_t* row_prob = nullptr;  // batch only
+    const BatchProb* probs = nullptr;
+    const float* prob_R = nullptr;
+    int32_t* idx_all = nullptr;
+};
+// Re-rank + certification + exact fallback of a batch group; the fallback reads
+// its row count on the device (no host synchronisation).
+// LLE weights of the rows of one k-group of a batch (uniform k; row g belongs to
+// problem row_prob[g]); warps = warps per block of the solve kernel (4 or 8).
+void lle_weights_batch(tk_ctx* ctx, const BatchProb* probs, const int32_t* row_prob, int64_t out_row0, int64_t rows,
+                       const int32_t* idx, int k, double klle_shift, double* W, int warps);
+void rerank_batch(tk_ctx* ctx, const RowSpace& S, int64_t rows, int kc, const int32_t* cand_idx,
+                  const float* cand_val, const float* nrm, float eps_c1, float eps_c2, unsigned* nfailed_out);
 bool tensor_screen_supported(int Dp);
 
 // rerank.cu: exact FP64 re-rank, certification and exact fallback.
@@ -147,6 +209,9 @@ void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t
 // assemble.cu: symbolic phase (reverse adjacency, row counts, row_ptr) returns
 // nnz; the numeric phase then fills col_idx/vals (device pointers) using the
 // symbolic state kept in the context's scratch.
+// The same without reading nnz back (row_ptr[N] holds it on the device).
+void assemble_symbolic_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
+                              int64_t* row_ptr);
 int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
                           int64_t* row_ptr);
 void assemble_numeric(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
