@@ -142,6 +142,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16000)
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-ltsa", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--check-connectivity", type=int, default=0)
     args = ap.parse_args()
 
@@ -197,7 +199,9 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library's kernels and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = tk.Context(local_rank, stream=stream.cuda_stream)
     Xd = torch.from_numpy(X).cuda()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -287,6 +291,40 @@ def main():
                 "nnz": int(linf[-1].nnz)}
         del Xl
 
+    # batched uneven problems: one captured CUDA graph vs one launch sequence per
+    # problem through the single-problem entry point (same GPU, same screen)
+    batch = None
+    if not args.no_batch:
+        from tapkee_gb300.batch import Batch
+        specs = datasets.batch_problems(args.batch_count, seed=7)
+        Xb = [torch.from_numpy(datasets.batch_problem_data(n, d, sd)).cuda() for n, d, _, sd in specs]
+        ks = [k for _, _, k, _ in specs]
+        points = int(sum(n for n, _, _, _ in specs))
+        bt = Batch(Xb, ks, context=ctx)
+        for _ in range(2):
+            bt.run()
+        graph_ms = [bt.run() for _ in range(3)]
+        tuning = bt.tuning
+        bt.close()
+        for p in range(min(4, len(specs))):
+            ctx.local_operator(Xb[p], "lle", num_neighbors=ks[p], klle_shift=1e-3, check_connectivity=False,
+                               copy_out=False)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for p in range(len(specs)):
+            ctx.local_operator(Xb[p], "lle", num_neighbors=ks[p], klle_shift=1e-3, check_connectivity=False,
+                               copy_out=False)
+        e1.record(stream)
+        e1.synchronize()
+        seq_ms = e0.elapsed_time(e1)
+        gms = float(statistics.median(graph_ms))
+        batch = {"workload": f"{len(specs)} LLE problems, N~U[500,20000], D in {{3,16,64,128}}, "
+                             f"k in {{8,12,16,24,32}}, seeded lifted Swiss rolls, float32 (inputs > L2)",
+                 "points": points, "graph_ms": gms, "points_per_s": points / (gms / 1000.0),
+                 "per_problem_sequence_ms": seq_ms, "graph_speedup": seq_ms / gms, "tuning": tuning}
+        del Xb
+
     # end to end through the public API with pinned host buffers
     Xh = torch.from_numpy(X).pin_memory()
     nnz = int(info.nnz)
@@ -332,7 +370,7 @@ def main():
             "vs_baseline": None, "dtype": "fp16x3-split screen / f64 re-rank / f32+ff weights",
             "data": "synthetic (seeded lifted Swiss roll)", "config": workload, "stage_ms": stage,
             "rows_uncertified": int(info.rows_uncertified), "nnz": nnz, "k_used": kk,
-            "fp32_path": fp32, "ltsa": ltsa, "roofline": roofline,
+            "fp32_path": fp32, "ltsa": ltsa, "batch": batch, "roofline": roofline,
             "e2e": {"value": args.n / (e2e_ms / 1000.0), "unit": "points/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clocks, "gpu_launches": int(launches)}

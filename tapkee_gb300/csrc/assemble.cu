@@ -134,6 +134,8 @@ __global__ void k_seg_scan(const int* in, int64_t n, const int64_t* seg, int64_t
     }
 }
 
+} // namespace
+
 void scan_to_offsets(tk_ctx* ctx, const int* in, int64_t n, int64_t* out)
 {
     const int nseg = (int)((n + SCAN_SEG - 1) / SCAN_SEG);
@@ -145,6 +147,8 @@ void scan_to_offsets(tk_ctx* ctx, const int* in, int64_t n, int64_t* out)
     k_seg_scan<<<nseg, 256, 0, ctx->stream>>>(in, n, seg, out);
     TK_CHECK_LAUNCH();
 }
+
+namespace {
 
 __global__ void k_fill_rev(const int32_t* __restrict__ idx, int64_t nk, const int64_t* rptr, int* fillc,
                            int32_t* rev)

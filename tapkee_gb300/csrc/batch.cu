@@ -15,9 +15,10 @@
 //     the alignment matrices are assembled as one block-diagonal CSR (capacity
 //     sized by the triplet count, so no host read-back is needed).
 // The whole sequence is captured once into a CUDA graph and replayed by
-// tk_batch_run. Differences from the single-problem path: points keep their
-// input order (no spatial sort), and connectivity is not checked (callers that
-// want the reference's 2k retry run tk_check_connected per problem).
+// tk_batch_run. Differences from the single-problem path:
+// connectivity is not checked (callers that want the reference's 2k retry run
+// tk_check_connected per problem), and the spatial order comes from a random
+// 16-direction sketch of each problem's covariance.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -56,25 +57,33 @@ __device__ __forceinline__ ff centred_norm2(const BatchProb& P, int64_t i, const
     return n2;
 }
 
-// Per problem (one CTA each): column means (FP64 partial sums combined in a
-// fixed order), the radius R = max |x - mean| and the fp16 split exponent s with
-// R 2^s < 2^14.
-__global__ void __launch_bounds__(256) k_b_stats(const BatchProb* __restrict__ probs, const int32_t* grp_probs,
-                                                 float* means, float* prob_R, float* prob_scale)
+// ---- batched preparation --------------------------------------------------
+// Stacked slots of a group come in blocks of 256 that belong to one problem
+// (each problem starts on a 256-slot boundary). In input order, slot q of
+// problem b holds point q - row0_b (valid while < N_b). The spatial order
+// replaces this by the Morton order of each problem's top-3 principal
+// coordinates, as the single-problem path does.
+
+// 1. column sums of one 256-slot chunk (FP64, fixed order)
+__global__ void __launch_bounds__(256) k_b_colsum(const BatchProb* __restrict__ probs,
+                                                  const int32_t* __restrict__ row_prob, double* partial)
 {
     __shared__ double part[256];
-    __shared__ float mean_s[B_DMAX];
-    __shared__ float wmax[8];
-    const int b = grp_probs[blockIdx.x];
+    const int64_t c0 = (int64_t)blockIdx.x * 256;
+    const int b = row_prob[c0];
     const BatchProb P = probs[b];
     const int t = threadIdx.x;
-    const int per = 256 / P.D;  // threads per column
+    const int per = 256 / P.D;
     double s = 0.0;
     if (t < per * P.D)
     {
         const int d = t % P.D;
-        for (int64_t r = t / P.D; r < P.N; r += per)
-            s += (double)xf(P.X, P.dtype, r * P.ldx + d);
+        for (int j = t / P.D; j < 256; j += per)
+        {
+            const int64_t i = c0 + j - P.row0;
+            if (i < P.N)
+                s += (double)xf(P.X, P.dtype, i * P.ldx + d);
+        }
     }
     part[t] = s;
     __syncthreads();
@@ -83,26 +92,245 @@ __global__ void __launch_bounds__(256) k_b_stats(const BatchProb* __restrict__ p
         double tot = 0.0;
         for (int q = 0; q < per; ++q)
             tot += part[q * P.D + t];
-        const float m = (float)(tot / (double)P.N);
-        mean_s[t] = m;
-        means[(int64_t)b * B_DMAX + t] = m;
+        partial[(int64_t)blockIdx.x * B_DMAX + t] = tot;
     }
-    __syncthreads();
-    const int lane = t & 31, w = t >> 5;
-    float rloc = 0.f;
-    for (int64_t i = w; i < P.N; i += 8)
+}
+
+constexpr int PCA_SAMPLES = 1024;  // rows of the covariance sketch per problem
+constexpr int B_SKETCH = 16;       // random directions of the sketch
+
+// deterministic pseudo-random sketch entry in [-1, 1)
+__device__ __forceinline__ float b_sketch_g(int d, int j)
+{
+    unsigned h = (unsigned)d * 0x9E3779B1u + (unsigned)j * 0x85EBCA77u + 0x165667B1u;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return (float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f;
+}
+
+// 2. per problem (one CTA): the mean, then the top-3 principal directions of a
+// randomly sketched covariance (x -> G^T x, G: D x 16) of up to 1024 rows, by
+// subspace iteration, mapped back as H = G V (D x 3). FP32: they only order points.
+__global__ void __launch_bounds__(256) k_b_mean_pca(const BatchProb* __restrict__ probs, const int32_t* grp_probs,
+                                                    const double* partial, float* means, float* H)
+{
+    __shared__ float mean_s[B_DMAX];
+    __shared__ float G[B_DMAX][B_SKETCH];
+    __shared__ float red[8][136];
+    __shared__ float C[B_SKETCH][B_SKETCH];
+    __shared__ float V[B_SKETCH][3], T[B_SKETCH][3];
+    const int b = grp_probs[blockIdx.x];
+    const BatchProb P = probs[b];
+    const int D = P.D, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int64_t c_first = P.row0 / 256, c_count = (P.N + 255) / 256;
+    for (int d = t; d < D; d += 256)
     {
-        const ff n2 = centred_norm2(P, i, mean_s, lane);
+        double tot = 0.0;
+        for (int64_t c = 0; c < c_count; ++c)
+            tot += partial[(c_first + c) * B_DMAX + d];
+        const float m = (float)(tot / (double)P.N);
+        mean_s[d] = m;
+        means[(int64_t)b * B_DMAX + d] = m;
+    }
+    for (int e = t; e < D * B_SKETCH; e += 256)
+        G[e / B_SKETCH][e % B_SKETCH] = b_sketch_g(e / B_SKETCH, e % B_SKETCH);
+    __syncthreads();
+    // upper-triangle pair (pa, pb) of the 136 entries owned by each lane
+    int pa[5], pb[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+    {
+        int q = lane + 32 * m, a = 0;
+        if (q >= 136)
+            q = 0;
+        while (q >= B_SKETCH - a)
+        {
+            q -= B_SKETCH - a;
+            ++a;
+        }
+        pa[m] = a;
+        pb[m] = a + q;
+    }
+    float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int64_t stride = P.N > PCA_SAMPLES ? P.N / PCA_SAMPLES : 1;
+    for (int64_t i = (int64_t)w * stride; i < P.N; i += 8 * stride)
+    {
+        float sk[B_SKETCH];
+#pragma unroll
+        for (int j = 0; j < B_SKETCH; ++j)
+            sk[j] = 0.f;
+        for (int d = lane; d < D; d += 32)
+        {
+            const float v = xf(P.X, P.dtype, i * P.ldx + d) - mean_s[d];
+#pragma unroll
+            for (int j = 0; j < B_SKETCH; ++j)
+                sk[j] = fmaf(G[d][j], v, sk[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < B_SKETCH; ++j)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                sk[j] += __shfl_xor_sync(0xffffffffu, sk[j], o);
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+        {
+            float sa = 0.f, sb = 0.f;
+#pragma unroll
+            for (int j = 0; j < B_SKETCH; ++j)
+            {
+                sa = (j == pa[m]) ? sk[j] : sa;
+                sb = (j == pb[m]) ? sk[j] : sb;
+            }
+            acc[m] = fmaf(sa, sb, acc[m]);
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 5; ++m)
+        if (lane + 32 * m < 136)
+            red[w][lane + 32 * m] = acc[m];
+    __syncthreads();
+    if (t < 136)
+    {
+        float sacc = 0.f;
+        for (int q = 0; q < 8; ++q)
+            sacc += red[q][t];
+        int a = 0, rem = t;
+        while (rem >= B_SKETCH - a)
+        {
+            rem -= B_SKETCH - a;
+            ++a;
+        }
+        C[a][a + rem] = sacc;
+        C[a + rem][a] = sacc;
+    }
+    if (t < B_SKETCH * 3)
+        V[t / 3][t % 3] = ((t / 3) == (t % 3)) ? 1.f : 0.01f * (t / 3 + 1) * (t % 3 + 1);
+    __syncthreads();
+    for (int it = 0; it < 24; ++it)
+    {
+        if (t < B_SKETCH * 3)
+        {
+            const int i = t / 3, c = t % 3;
+            float sacc = 0.f;
+            for (int j = 0; j < B_SKETCH; ++j)
+                sacc = fmaf(C[i][j], V[j][c], sacc);
+            T[i][c] = sacc;
+        }
+        __syncthreads();
+        if (t == 0)
+        {
+            for (int c = 0; c < 3; ++c)
+            {
+                for (int q = 0; q < c; ++q)
+                {
+                    float dot = 0.f;
+                    for (int j = 0; j < B_SKETCH; ++j)
+                        dot = fmaf(T[j][c], T[j][q], dot);
+                    for (int j = 0; j < B_SKETCH; ++j)
+                        T[j][c] = fmaf(-dot, T[j][q], T[j][c]);
+                }
+                float nrm = 0.f;
+                for (int j = 0; j < B_SKETCH; ++j)
+                    nrm = fmaf(T[j][c], T[j][c], nrm);
+                const float inv = nrm > 0.f ? rsqrtf(nrm) : 0.f;
+                for (int j = 0; j < B_SKETCH; ++j)
+                    T[j][c] = nrm > 0.f ? T[j][c] * inv : (j == c ? 1.f : 0.f);
+            }
+        }
+        __syncthreads();
+        if (t < B_SKETCH * 3)
+            V[t / 3][t % 3] = T[t / 3][t % 3];
+        __syncthreads();
+    }
+    // H = G V, normalised per column so that |projection| <= |x - mean|
+    for (int e = t; e < 3 * D; e += 256)
+    {
+        const int d = e / 3, c = e % 3;
+        float sacc = 0.f;
+        for (int j = 0; j < B_SKETCH; ++j)
+            sacc = fmaf(G[d][j], V[j][c], sacc);
+        H[(int64_t)b * 3 * B_DMAX + e] = sacc;
+    }
+}
+
+// column norms of H (so the projections can be scaled into [-R, R])
+__global__ void k_b_hnorm(const int32_t* grp_probs, int count, const BatchProb* __restrict__ probs, float* H)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count * 3)
+        return;
+    const int b = grp_probs[q / 3], c = q % 3;
+    float* Hb = H + (int64_t)b * 3 * B_DMAX;
+    float n = 0.f;
+    for (int d = 0; d < probs[b].D; ++d)
+        n = fmaf(Hb[d * 3 + c], Hb[d * 3 + c], n);
+    const float inv = n > 0.f ? rsqrtf(n) : 0.f;
+    for (int d = 0; d < probs[b].D; ++d)
+        Hb[d * 3 + c] *= inv;
+}
+
+// 3. per slot (input order, one warp per row): radius (the same float-float norm
+// as the layout, so R bounds every stored norm) and the 3 principal coordinates
+__global__ void __launch_bounds__(256) k_b_project(const BatchProb* __restrict__ probs,
+                                                   const int32_t* __restrict__ row_prob, const float* means,
+                                                   const float* H, float* proj, unsigned* r_bits)
+{
+    __shared__ float wmax[8];
+    const int64_t c0 = (int64_t)blockIdx.x * 256;
+    const int b = row_prob[c0];
+    const BatchProb P = probs[b];
+    const float* mean = means + (int64_t)b * B_DMAX;
+    const float* Hb = H + (int64_t)b * 3 * B_DMAX;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float rloc = 0.f;
+    for (int j = w; j < 256; j += 8)
+    {
+        const int64_t i = c0 + j - P.row0;
+        if (i >= P.N)
+            break;
+        float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+        for (int d = lane; d < P.D; d += 32)
+        {
+            const float v = xf(P.X, P.dtype, i * P.ldx + d) - mean[d];
+            p0 = fmaf(Hb[d * 3 + 0], v, p0);
+            p1 = fmaf(Hb[d * 3 + 1], v, p1);
+            p2 = fmaf(Hb[d * 3 + 2], v, p2);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            p0 += __shfl_xor_sync(0xffffffffu, p0, o);
+            p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+            p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+        }
+        const ff n2 = centred_norm2(P, i, mean, lane);
         rloc = fmaxf(rloc, (float)sqrt(ff_to_double(n2)) * 1.000001f);
+        if (lane < 3)
+            proj[(c0 + j) * 3 + lane] = lane == 0 ? p0 : (lane == 1 ? p1 : p2);
     }
     if (lane == 0)
         wmax[w] = rloc;
     __syncthreads();
-    if (t == 0)
+    if (threadIdx.x == 0)
     {
         float R = 0.f;
         for (int q = 0; q < 8; ++q)
             R = fmaxf(R, wmax[q]);
+        atomicMax(&r_bits[b], __float_as_uint(R));  // R >= 0: bits order like values
+    }
+}
+
+// 4. radius and split exponent s (R 2^s < 2^14) per problem
+__global__ void k_b_scale(const int32_t* grp_probs, int count, const unsigned* r_bits, float* prob_R,
+                          float* prob_scale)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
+    {
+        const int b = grp_probs[q];
+        const float R = __uint_as_float(r_bits[b]);
         int e = 0;
         frexpf(R > 0.f ? R * 1.01f : 1.f, &e);
         prob_R[b] = R;
@@ -110,10 +338,63 @@ __global__ void __launch_bounds__(256) k_b_stats(const BatchProb* __restrict__ p
     }
 }
 
-// Stacked screening layout of one group, one warp per stacked row.
-__global__ void k_b_layout(const BatchProb* __restrict__ probs, const int32_t* __restrict__ row_prob, int64_t rows,
-                           int Dp, const float* means, const float* prob_scale, __half* xh, __half* xl, __half* xn,
-                           float* nrm)
+__device__ __forceinline__ unsigned b_spread3(unsigned v)  // 10 bits -> every third bit
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// 5. Morton bucket (about four points per bucket) of every valid slot
+__global__ void k_b_codes(const BatchProb* __restrict__ probs, const int32_t* __restrict__ row_prob, int64_t rows,
+                          const float* proj, const float* prob_R, int32_t* bucket, int* hist)
+{
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < rows; q += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int b = row_prob[q];
+        const BatchProb& P = probs[b];
+        if (q - P.row0 >= P.N)
+            continue;
+        const float R = prob_R[b];
+        unsigned u[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+        {
+            float tt = R > 0.f ? 0.5f * (proj[q * 3 + c] / R + 1.f) : 0.f;
+            tt = fminf(fmaxf(tt, 0.f), 1.f);
+            u[c] = min(1023u, (unsigned)(tt * 1024.f));
+        }
+        const unsigned code = (b_spread3(u[0]) << 2) | (b_spread3(u[1]) << 1) | b_spread3(u[2]);
+        const int32_t g = (int32_t)(P.hoff + (code >> (30 - P.hbits)));
+        bucket[q] = g;
+        atomicAdd(&hist[g], 1);
+    }
+}
+
+// 6. sorted position of every valid slot: perm_st[row0 + position] = point
+__global__ void k_b_scatter(const BatchProb* __restrict__ probs, const int32_t* __restrict__ row_prob, int64_t rows,
+                            const int32_t* bucket, const int64_t* offs, int* fillc, int32_t* perm_st)
+{
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < rows; q += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int b = row_prob[q];
+        const BatchProb& P = probs[b];
+        const int64_t i = q - P.row0;
+        if (i >= P.N)
+            continue;
+        const int32_t g = bucket[q];
+        const int64_t pos = offs[g] - offs[P.hoff] + atomicAdd(&fillc[g], 1);
+        perm_st[P.row0 + pos] = (int32_t)i;
+    }
+}
+
+// 7. stacked screening layout in sorted order, one warp per stacked row.
+__global__ void k_b_layout(const BatchProb* __restrict__ probs, const int32_t* __restrict__ row_prob,
+                           const int32_t* __restrict__ perm_st, int64_t rows, int Dp, const float* means,
+                           const float* prob_scale, __half* xh, __half* xl, __half* xn, float* nrm)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -121,16 +402,10 @@ __global__ void k_b_layout(const BatchProb* __restrict__ probs, const int32_t* _
     for (int64_t p = warp; p < rows; p += nwarps)
     {
         const int b = row_prob[p];
-        BatchProb P{};
-        int64_t i = 0;
-        bool valid = false;
-        if (b >= 0)
-        {
-            P = probs[b];
-            i = p - P.row0;
-            valid = i < P.N;
-        }
-        const float* mean = means + (int64_t)(b >= 0 ? b : 0) * B_DMAX;
+        const BatchProb P = probs[b];
+        const bool valid = p - P.row0 < P.N;
+        const int64_t i = valid ? perm_st[p] : 0;
+        const float* mean = means + (int64_t)b * B_DMAX;
         const int s = valid ? (int)prob_scale[b] : 0;
         const float scale = ldexpf(1.f, s);
         for (int d = lane; d < Dp; d += 32)
@@ -210,6 +485,14 @@ struct ScreenGroup
     float* nrm = nullptr;
     int32_t* row_prob = nullptr;  // device, per stacked row
     int32_t* grp_probs = nullptr; // device, the group's problems
+    int32_t* perm_st = nullptr;   // device, stacked sorted row -> point of its problem
+    double* partial = nullptr;    // column sums per 256-row chunk
+    float* proj = nullptr;        // 3 principal coordinates per input-order slot
+    int32_t* bucket = nullptr;    // Morton bucket per input-order slot
+    int* hist = nullptr;          // bucket counts, then fill counters
+    int* fillc = nullptr;
+    int64_t* offs = nullptr;      // exclusive scan of hist
+    int64_t nbuckets = 0;
     int4* items = nullptr;
     int nitems = 0;
     int32_t* cand_idx = nullptr;
@@ -247,7 +530,8 @@ struct tk_batch
     std::vector<int> kgroup_of;        // sorted position -> k-group
     BatchProb* probs = nullptr;
     int64_t* prob_n = nullptr;
-    float *prob_R = nullptr, *prob_scale = nullptr, *means = nullptr;
+    float *prob_R = nullptr, *prob_scale = nullptr, *means = nullptr, *H = nullptr;
+    unsigned* r_bits = nullptr;
     int32_t* row_prob_out = nullptr;
     int32_t* idx_all = nullptr;
     double* w_all = nullptr;
@@ -305,10 +589,29 @@ void enqueue(tk_batch* B)
     for (size_t g = 0; g < B->sg.size(); ++g)
     {
         ScreenGroup& S = B->sg[g];
-        k_b_stats<<<(int)S.probs.size(), 256, 0, st>>>(B->probs, S.grp_probs, B->means, B->prob_R, B->prob_scale);
+        const int nprob = (int)S.probs.size();
+        const int chunks = (int)(S.rows / 256);
+        k_b_colsum<<<chunks, 256, 0, st>>>(B->probs, S.row_prob, S.partial);
         TK_CHECK_LAUNCH();
-        k_b_layout<<<4 * sms, 256, 0, st>>>(B->probs, S.row_prob, S.rows, S.Dp, B->means, B->prob_scale, S.xh, S.xl,
-                                            S.xn, S.nrm);
+        k_b_mean_pca<<<nprob, 256, 0, st>>>(B->probs, S.grp_probs, S.partial, B->means, B->H);
+        TK_CHECK_LAUNCH();
+        k_b_hnorm<<<(3 * nprob + 127) / 128, 128, 0, st>>>(S.grp_probs, nprob, B->probs, B->H);
+        TK_CHECK_LAUNCH();
+        TK_CUDA(cudaMemsetAsync(B->r_bits, 0, sizeof(unsigned) * B->hp.size(), st));
+        k_b_project<<<chunks, 256, 0, st>>>(B->probs, S.row_prob, B->means, B->H, S.proj, B->r_bits);
+        TK_CHECK_LAUNCH();
+        k_b_scale<<<(nprob + 127) / 128, 128, 0, st>>>(S.grp_probs, nprob, B->r_bits, B->prob_R, B->prob_scale);
+        TK_CHECK_LAUNCH();
+        TK_CUDA(cudaMemsetAsync(S.hist, 0, sizeof(int) * (size_t)S.nbuckets, st));
+        TK_CUDA(cudaMemsetAsync(S.fillc, 0, sizeof(int) * (size_t)S.nbuckets, st));
+        k_b_codes<<<2 * sms, 256, 0, st>>>(B->probs, S.row_prob, S.rows, S.proj, B->prob_R, S.bucket, S.hist);
+        TK_CHECK_LAUNCH();
+        scan_to_offsets(ctx, S.hist, S.nbuckets, S.offs);
+        TK_CUDA(cudaMemsetAsync(S.perm_st, 0xff, sizeof(int32_t) * (size_t)S.rows, st));
+        k_b_scatter<<<2 * sms, 256, 0, st>>>(B->probs, S.row_prob, S.rows, S.bucket, S.offs, S.fillc, S.perm_st);
+        TK_CHECK_LAUNCH();
+        k_b_layout<<<4 * sms, 256, 0, st>>>(B->probs, S.row_prob, S.perm_st, S.rows, S.Dp, B->means, B->prob_scale,
+                                            S.xh, S.xl, S.xn, S.nrm);
         TK_CHECK_LAUNCH();
         StackedScreen SS;
         SS.Dp = S.Dp;
@@ -327,6 +630,7 @@ void enqueue(tk_batch* B)
         float c1, c2;
         screen_error_model(TK_SCREEN_TENSOR, S.Dp, &c1, &c2);
         RowSpace RS;
+        RS.perm = S.perm_st;
         RS.row_prob = S.row_prob;
         RS.probs = B->probs;
         RS.prob_R = B->prob_R;
@@ -459,6 +763,13 @@ void plan(tk_batch* B, const tk_batch_problem* problems, int count)
         h.row0 = g.rows;
         g.rows += ((q.N + 255) / 256) * 256;
         g.probs.push_back(s);
+        // Morton buckets: about four points each
+        int bits = 2;
+        while (bits < 24 && ((int64_t)1 << (bits + 2)) < q.N)
+            ++bits;
+        h.hbits = bits;
+        h.hoff = g.nbuckets;
+        g.nbuckets += (int64_t)1 << bits;
     }
     B->total_rows = out_row;
     B->total_idx = idx_off;
@@ -497,6 +808,8 @@ void plan(tk_batch* B, const tk_batch_problem* problems, int count)
     B->idx_all = dalloc<int32_t>(own, (size_t)B->total_idx);
     B->w_all = dalloc<double>(own, (size_t)B->total_idx);
     B->nfailed = dalloc<unsigned>(own, B->sg.size());
+    B->H = dalloc<float>(own, (size_t)P * 3 * B_DMAX);
+    B->r_bits = dalloc<unsigned>(own, P);
     upload(B->probs, B->hp, st);
     std::vector<int64_t> pn(P);
     std::vector<int32_t> rpo((size_t)B->total_rows);
@@ -516,6 +829,13 @@ void plan(tk_batch* B, const tk_batch_problem* problems, int count)
         g.cand_idx = dalloc<int32_t>(own, (size_t)g.rows * g.kc);
         g.cand_val = dalloc<float>(own, (size_t)g.rows * g.kc);
         g.row_prob = dalloc<int32_t>(own, (size_t)g.rows);
+        g.perm_st = dalloc<int32_t>(own, (size_t)g.rows);
+        g.partial = dalloc<double>(own, (size_t)(g.rows / 256) * B_DMAX);
+        g.proj = dalloc<float>(own, (size_t)g.rows * 3);
+        g.bucket = dalloc<int32_t>(own, (size_t)g.rows);
+        g.hist = dalloc<int>(own, (size_t)g.nbuckets);
+        g.fillc = dalloc<int>(own, (size_t)g.nbuckets);
+        g.offs = dalloc<int64_t>(own, (size_t)g.nbuckets + 1);
         g.grp_probs = dalloc<int32_t>(own, g.probs.size());
         std::vector<int32_t> rp((size_t)g.rows, -1);
         std::vector<int4> items;

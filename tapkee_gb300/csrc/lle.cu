@@ -129,23 +129,37 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         bG[m] = (itm < ITEMS) ? itm / NBLK : 0;
     }
 
-    for (int64_t g = warp; g < RW.rows; g += nwarps)
+    // batch: each warp takes a contiguous run of rows, so the problem
+    // description is reloaded only where the run crosses into the next problem
+    const int64_t run = BATCH ? (RW.rows + nwarps - 1) / nwarps : 0;
+    const int64_t g_begin = BATCH ? warp * run : warp;
+    const int64_t g_end = BATCH ? min(RW.rows, g_begin + run) : RW.rows;
+    const int64_t g_step = BATCH ? 1 : nwarps;
+    const void* X = RW.X;
+    int dtype = RW.dtype;
+    int64_t N = RW.N;
+    int D = RW.D;
+    int64_t ldx = RW.ldx;
+    int64_t prob_row0 = 0;  // batch: output row of the current problem's point 0
+    int cur = -1;
+    for (int64_t g = g_begin; g < g_end; g += g_step)
     {
-        const void* X = RW.X;
-        int dtype = RW.dtype;
-        int64_t N = RW.N;
-        int D = RW.D;
-        int64_t ldx = RW.ldx;
         int64_t i = g;
         if constexpr (BATCH)
         {
-            const BatchProb& P = RW.probs[RW.row_prob[g]];
-            X = P.X;
-            dtype = P.dtype;
-            N = P.N;
-            D = P.D;
-            ldx = P.ldx;
-            i = RW.out_row0 + g - P.out_row0;
+            const int b = RW.row_prob[g];
+            if (b != cur)
+            {
+                const BatchProb& P = RW.probs[b];
+                X = P.X;
+                dtype = P.dtype;
+                N = P.N;
+                D = P.D;
+                ldx = P.ldx;
+                prob_row0 = P.out_row0;
+                cur = b;
+            }
+            i = RW.out_row0 + g - prob_row0;
         }
         int nb[NPL];
 #pragma unroll

@@ -102,10 +102,10 @@ __device__ __forceinline__ bool row_view(const RowSpace& S, int64_t p, RowView& 
     if (b < 0)
         return false;
     const BatchProb& P = S.probs[b];
-    const int64_t i = p - P.row0;
-    if (i < 0 || i >= P.N)
+    if (p - P.row0 >= P.N)
         return false;
-    v = RowView{P.X, P.dtype, P.ldx, P.D, P.N, P.k, i, S.prob_R[b], nullptr, S.idx_all + P.idx_off, nullptr};
+    v = RowView{P.X,      P.dtype,          P.ldx,   P.D, P.N, P.k, (int64_t)S.perm[p], S.prob_R[b], S.perm + P.row0,
+                S.idx_all + P.idx_off, nullptr};
     return true;
 }
 

@@ -134,6 +134,8 @@ struct BatchProb
     int64_t row0;      // first stacked row in its screen group (multiple of 256)
     int64_t idx_off;   // element offset of its rows in the neighbour and weight tables
     int64_t out_row0;  // first row in the batch's output row space (problems ordered by k)
+    int64_t hoff;      // first Morton bucket of the problem in its group's histogram
+    int hbits;         // log2 of the problem's bucket count
 };
 
 // Problems stacked for one batched screen launch (same Dp and KC).
@@ -167,7 +169,7 @@ struct RowSpace
     const float* R = nullptr;
     int32_t* idx_out = nullptr;
     double* d2_out = nullptr;
-    const int32_t* row_prob = nullptr;  // batch only
+    const int32_t* row_prob = nullptr;  // batch only (perm then maps stacked rows to points)
     const BatchProb* probs = nullptr;
     const float* prob_R = nullptr;
     int32_t* idx_all = nullptr;
@@ -209,6 +211,8 @@ void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t
 // assemble.cu: symbolic phase (reverse adjacency, row counts, row_ptr) returns
 // nnz; the numeric phase then fills col_idx/vals (device pointers) using the
 // symbolic state kept in the context's scratch.
+// Exclusive scan of n int counters into n + 1 int64 offsets (deterministic).
+void scan_to_offsets(tk_ctx* ctx, const int* in, int64_t n, int64_t* out);
 // The same without reading nnz back (row_ptr[N] holds it on the device).
 void assemble_symbolic_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
                               int64_t* row_ptr);
