@@ -92,6 +92,72 @@ struct LleRows
     int64_t out_row0;
 };
 
+// Register-resident Cholesky for KP <= 32: lane a holds row a of the matrix
+// (L[c] = C_ac for c <= a) and ends with row a of the lower factor and invd =
+// 1 / L_aa. Column j's entries travel by shuffles, so no shared-memory round trip
+// sits on the factorisation's dependency chain. Reciprocal square roots replace
+// the divisions (the float-float refinement absorbs their last-bit errors).
+template <int KP>
+__device__ __forceinline__ void reg_cholesky(float (&L)[KP], float& invd, int lane)
+{
+    invd = 1.f;
+#pragma unroll
+    for (int j = 0; j < KP; ++j)
+    {
+        const float inv = rsqrtf(fmaxf(__shfl_sync(0xffffffffu, L[j], j), FLT_MIN));
+        if (lane == j)
+        {
+            L[j] = L[j] * inv;
+            invd = inv;
+        }
+        else if (lane > j)
+            L[j] = L[j] * inv;
+#pragma unroll
+        for (int c = 0; c < KP; ++c)  // constant trip count: fully unrolled, c > j folds
+        {
+            if (c > j)
+            {
+                const float lcj = __shfl_sync(0xffffffffu, L[j], c);
+                if (lane >= c)
+                    L[c] = fmaf(-L[j], lcj, L[c]);
+            }
+        }
+    }
+}
+
+// Solves L L^T x = r with the register factor; lane a holds r_a and gets x_a.
+template <int KP>
+__device__ __forceinline__ float reg_chol_solve(const float (&L)[KP], float invd, float r, int lane)
+{
+    float y = r;
+#pragma unroll
+    for (int j = 0; j < KP; ++j)
+    {
+        const float yj = __shfl_sync(0xffffffffu, y, j) * __shfl_sync(0xffffffffu, invd, j);
+        if (lane == j)
+            y = yj;
+        else if (lane > j)
+            y = fmaf(-L[j], yj, y);
+    }
+    float x = 0.f;
+#pragma unroll
+    for (int j = KP - 1; j >= 0; --j)
+    {
+        float s = (lane > j && lane < KP) ? L[j] * x : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == j)
+            x = (y - s) * invd;
+    }
+    return x;
+}
+
+__device__ __forceinline__ float ld_f(const void* X, int dtype, int64_t off)
+{
+    return dtype == TK_F64 ? (float)reinterpret_cast<const double*>(X)[off] : reinterpret_cast<const float*>(X)[off];
+}
+
 template <int KP, int WARPS, bool BATCH, bool BLOCKED = (KP <= 64)>
 __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int32_t* __restrict__ idx, int k,
                                                     double klle_shift, const double* __restrict__ rhs,
@@ -190,14 +256,32 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         for (int d0 = 0; d0 < D; d0 += 32)
         {
             const int d = d0 + lane;
-#pragma unroll 4
-            for (int a = 0; a < KP; ++a)
+            if (KP <= 32 && dtype == TK_F32)
             {
-                const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
-                float v = 0.f;
-                if (a < k && d < D)
-                    v = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d).hi;
-                S.Zh[a][lane] = v;
+                // every neighbour value of the chunk in flight at once
+                const float xi = (d < D) ? ld_f(X, dtype, i * ldx + d) : 0.f;
+                float v[KP <= 32 ? KP : 1];
+#pragma unroll
+                for (int a = 0; a < (KP <= 32 ? KP : 1); ++a)
+                {
+                    const int nba = __shfl_sync(0xffffffffu, nb[0], a & 31);
+                    v[a] = (a < k && d < D) ? ld_f(X, dtype, (int64_t)nba * ldx + d) : xi;
+                }
+#pragma unroll
+                for (int a = 0; a < (KP <= 32 ? KP : 1); ++a)
+                    S.Zh[a][lane] = v[a] - xi;
+            }
+            else
+            {
+#pragma unroll 4
+                for (int a = 0; a < KP; ++a)
+                {
+                    const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
+                    float v = 0.f;
+                    if (a < k && d < D)
+                        v = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d).hi;
+                    S.Zh[a][lane] = v;
+                }
             }
             __syncwarp();
             if (!BLOCKED)
@@ -296,7 +380,23 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         }
         __syncwarp();
 
-        // ---- FP32 Cholesky (lower, in place) ----
+        // ---- FP32 Cholesky (lower) ----
+        float Lr[KP <= 32 ? KP : 1];
+        float invd = 1.f;
+        if constexpr (KP <= 32)
+        {
+#pragma unroll
+            for (int c = 0; c < KP; ++c)
+                Lr[c] = (lane < KP && c <= lane) ? S.C[lane][c] : 0.f;
+            reg_cholesky<KP>(Lr, invd, lane);
+            const float x = reg_chol_solve<KP>(Lr, invd, lane < KP ? S.r[lane] : 0.f, lane);
+            __syncwarp();
+            if (lane < KP)
+                S.w[lane] = (lane < k) ? x : 0.f;
+            __syncwarp();
+        }
+        else
+        {
         for (int j = 0; j < KP; ++j)
         {
             const float ljj = sqrtf(fmaxf(S.C[j][j], FLT_MIN));
@@ -318,6 +418,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         for (int a = lane; a < KP; a += 32)
             S.w[a] = (a < k) ? S.r[a] : 0.f;
         __syncwarp();
+        }
 
         // ---- float-float residual refinement ----
         const int iters = (k > D) ? 2 : 1;
@@ -326,11 +427,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
             if (KP <= 32)
             {
                 // lanes own dimensions: z_a(d) = hi + lo exactly, v(d) = sum_b w_b z_b(d),
-                // and lane-local partials of (C w)_a = sum_d z_a(d) v(d) and of
-                // trace = sum_a |z_a|^2; one reduce-scatter gathers (C w)_a.
+                // and lane-local partials of (C w)_a = sum_d z_a(d) v(d); one
+                // reduce-scatter gathers (C w)_a. The shift uses the FP32 trace:
+                // its relative error (~D 2^-24) enters the residual scaled by
+                // klle_shift, far below the solve's own error.
                 constexpr int KR = (KP <= 32) ? KP : 32;
                 ff part[KR];
-                ff trp = ff_zero();
 #pragma unroll
                 for (int a = 0; a < KR; ++a)
                     part[a] = ff_zero();
@@ -360,14 +462,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
                     const ff v = ff_add(v0, v1);
 #pragma unroll
                     for (int a = 0; a < KR; ++a)
-                    {
                         part[a] = ff_fma(part[a], zh[a], zl[a], v.hi, v.lo);
-                        trp = ff_fma(trp, zh[a], zl[a], zh[a], zl[a]);
-                    }
                 }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    trp = ff_add(trp, ff_shfl_xor(trp, o));
                 // reduce-scatter of the KR partials (KR = 16 or 32 values)
 #pragma unroll
                 for (int lvl = 0; lvl < 5; ++lvl)
@@ -390,7 +486,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
                 }
                 // part[0] of lane l is (C w)_a for a = KR == 32 ? l : (l >> 1)
                 const int a_own = (KR == 32) ? lane : (lane >> 1);
-                const double shift_true = klle_shift * ff_to_double(trp);
+                const double shift_true = klle_shift * (double)trace;
                 if ((KR == 32 || (lane & 1) == 0) && a_own < KP)
                     S.r[a_own] = (a_own < k) ? (float)((rhs ? rhs[g * k + a_own] : 1.0) - ff_to_double(part[0]) -
                                                        shift_true * (double)S.w[a_own])
@@ -460,9 +556,19 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
                 }
                 __syncwarp();
             }
-            chol_solve<KP>(S, lane);
-            for (int a = lane; a < k; a += 32)
-                S.w[a] += S.r[a];
+            if constexpr (KP <= 32)
+            {
+                const float x = reg_chol_solve<KP>(Lr, invd, lane < KP ? S.r[lane] : 0.f, lane);
+                __syncwarp();
+                if (lane < k)
+                    S.w[lane] += x;
+            }
+            else
+            {
+                chol_solve<KP>(S, lane);
+                for (int a = lane; a < k; a += 32)
+                    S.w[a] += S.r[a];
+            }
             __syncwarp();
         }
 

@@ -74,6 +74,35 @@ __device__ __forceinline__ double exact_d2(const void* X, int dtype, int64_t ldx
     return ff_to_double(acc) + (double)cross;
 }
 
+// The exact distance as a normalised float pair (hi, lo): float-float for
+// float32 input, the FP64 value split for float64 input. Comparing (hi, lo)
+// lexicographically orders the values without FP64 arithmetic.
+__device__ __forceinline__ ff exact_key(const void* X, int dtype, int64_t ldx, int D, int64_t a, int64_t b)
+{
+    if (dtype == TK_F64)
+    {
+        const double v = exact_d2(X, dtype, ldx, D, a, b);
+        const float h = (float)v;
+        return ff{h, (float)(v - (double)h)};
+    }
+    const float* xa = reinterpret_cast<const float*>(X) + a * ldx;
+    const float* xb = reinterpret_cast<const float*>(X) + b * ldx;
+    ff acc = ff_zero();
+    float cross = 0.f;
+    for (int d = 0; d < D; ++d)
+    {
+        const ff z = two_sum(xa[d], -xb[d]);
+        acc = ff_add(acc, two_prod(z.hi, z.hi));
+        cross = fmaf(2.f * z.hi, z.lo, cross);
+    }
+    return ff_add(acc, ff{cross, 0.f});
+}
+
+__device__ __forceinline__ bool key_less_ff(float ha, float la, int ja, float hb, float lb, int jb)
+{
+    return ha < hb || (ha == hb && (la < lb || (la == lb && ja < jb)));
+}
+
 // The problem a screened row belongs to, and the row's original index in it.
 struct RowView
 {
@@ -111,13 +140,26 @@ __device__ __forceinline__ bool row_view(const RowSpace& S, int64_t p, RowView& 
 
 constexpr int RR_WARPS = 8;
 
+// One warp per query row; lane l owns candidates l, l + 32, ... (KC <= 256).
+// float32 input: every candidate gets an FP32 direct-difference distance f (any
+// summation order) with
+// |f - d2| <= gam f (gam = (D + 8) 2^-23). Since gam f is increasing in f, the
+// intervals [(1 - gam) f, (1 + gam) f] of candidates taken in f order are
+// ordered too wherever neighbours in that order do not overlap; so only the
+// candidates whose interval overlaps a rank neighbour among the first k + 1
+// need their exact (float-float) distance, and the ranking by (key, index) with
+// key = exact value where computed, else f, is the exact ranking. float64 input:
+// every candidate's distance in FP64.
 template <int KC, bool BATCH>
 __global__ void __launch_bounds__(RR_WARPS * 32)
     k_rerank(const RowSpace RS, int64_t rows, const float* nrm, const int32_t* cand_idx, const float* cand_val,
              float c1, float c2, int32_t* failed, double* failed_ub, unsigned* nfailed)
 {
     constexpr int PER = (KC + 31) / 32;
-    const int lane = threadIdx.x & 31;
+    constexpr int NONE = 0x7fffffff - 255;  // slots >= NONE hold no candidate
+    __shared__ float f_s[RR_WARPS][KC];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    float* fr = f_s[wib];
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t p = warp; p < rows; p += nwarps)
@@ -132,111 +174,178 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
         const int64_t N = V.N;
         const int k = V.k;
         const int64_t i = V.i;
-        const double R = (double)V.R;
-        double d[PER];
+        // relative error bound of the FP32 distances, plus the rounding of the
+        // float products that apply it
+        const float gam = (float)(D + 8) * 1.1920928955078125e-07f + 4.76837158203125e-07f;
+        float kh[PER], kl[PER];  // keys: exact (hi, lo) or the FP32 value (lo = 0)
         int j[PER];
+        bool exact[PER];
 #pragma unroll
         for (int s = 0; s < PER; ++s)
         {
             const int slot = lane + 32 * s;
-            d[s] = __longlong_as_double(0x7ff0000000000000LL);  // +inf
-            j[s] = 0x7fffffff - slot;                          // distinct, ranks last
-            int64_t jj = -1;
+            kh[s] = __int_as_float(0x7f800000);  // +inf
+            kl[s] = 0.f;
+            j[s] = 0x7fffffff - slot;            // distinct, ranks last
+            exact[s] = true;
             if (slot < KC)
             {
                 const int c = cand_idx[p * KC + slot];
                 if (c >= 0 && c < N)
                 {
-                    jj = V.perm ? V.perm[c] : c;
-                    if (jj == i)
-                        jj = -1;
+                    const int64_t jj = V.perm ? V.perm[c] : c;
+                    if (jj != i)
+                        j[s] = (int)jj;
                 }
-            }
-            if (dtype == TK_F64)
-            {
-                if (jj >= 0)
-                {
-                    d[s] = exact_d2(X, dtype, ldx, D, i, jj);
-                    j[s] = (int)jj;
-                }
-                continue;
-            }
-            // float32: lanes own dimensions (coalesced row loads); each lane keeps
-            // float-float partial sums for all 32 candidates of the group, and a
-            // warp reduce-scatter leaves candidate l's total in lane l
-            const float* Xf = reinterpret_cast<const float*>(X);
-            ff part[32];
-#pragma unroll
-            for (int r = 0; r < 32; ++r)
-                part[r] = ff_zero();
-            for (int d0 = 0; d0 < D; d0 += 32)
-            {
-                const int d = d0 + lane;
-                const float xq = (d < D) ? Xf[i * ldx + d] : 0.f;
-#pragma unroll
-                for (int r = 0; r < 32; ++r)
-                {
-                    const int64_t row = __shfl_sync(0xffffffffu, jj, r);
-                    const float y = (row >= 0 && d < D) ? Xf[row * ldx + d] : 0.f;
-                    const ff z = two_sum(y, -xq);  // exact difference
-                    ff sq = two_prod(z.hi, z.hi);
-                    sq.lo = fmaf(2.f * z.hi, z.lo, sq.lo);
-                    part[r] = ff_add(part[r], sq);
-                }
-            }
-            // reduce-scatter: after the level with offset o, a lane keeps the half of
-            // its candidates whose index bit matches its own lane bit
-#pragma unroll
-            for (int lvl = 0; lvl < 5; ++lvl)
-            {
-                const int o = 16 >> lvl;
-                const int half = o;  // values kept after this level: 2 * half -> half
-                const bool upper = (lane & o) != 0;
-#pragma unroll
-                for (int q = 0; q < half; ++q)
-                {
-                    const ff send = upper ? part[q] : part[q + half];
-                    const ff keep = upper ? part[q + half] : part[q];
-                    part[q] = ff_add(keep, ff_shfl_xor(send, o));
-                }
-            }
-            const ff acc = part[0];
-            const float cross = 0.f;
-            if (jj >= 0)
-            {
-                d[s] = ff_to_double(acc) + (double)cross;
-                j[s] = (int)jj;
             }
         }
-        // rank of every element among the KC (d, j) keys
-        int rank[PER];
+        if (dtype == TK_F64)
+        {
 #pragma unroll
-        for (int s = 0; s < PER; ++s)
-            rank[s] = 0;
+            for (int s = 0; s < PER; ++s)
+                if (j[s] < NONE)
+                {
+                    const ff e = exact_key(X, dtype, ldx, D, i, j[s]);
+                    kh[s] = e.hi;
+                    kl[s] = e.lo;
+                }
+        }
+        else
+        {
+            // FP32 screen of the candidates: lanes own dimensions, so every row
+            // load is one coalesced 128-byte segment; a warp reduce-scatter leaves
+            // candidate l's sum in lane l
+            const float* Xf = reinterpret_cast<const float*>(X);
 #pragma unroll
-        for (int so = 0; so < PER; ++so)
-            for (int m = 0; m < 32; ++m)
+            for (int s = 0; s < PER; ++s)
             {
-                const double dm = __shfl_sync(0xffffffffu, d[so], m);
-                const int jm = __shfl_sync(0xffffffffu, j[so], m);
+                float part[32];
+#pragma unroll
+                for (int r = 0; r < 32; ++r)
+                    part[r] = 0.f;
+                for (int d0 = 0; d0 < D; d0 += 32)
+                {
+                    const int d = d0 + lane;
+                    const float xq = (d < D) ? __ldg(Xf + i * ldx + d) : 0.f;
+#pragma unroll
+                    for (int r = 0; r < 32; ++r)
+                    {
+                        const int row = __shfl_sync(0xffffffffu, j[s], r);
+                        if (row < NONE && d < D)
+                        {
+                            const float z = __ldg(Xf + (int64_t)row * ldx + d) - xq;
+                            part[r] = fmaf(z, z, part[r]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int lvl = 0; lvl < 5; ++lvl)
+                {
+                    const int o = 16 >> lvl;
+                    const bool upper = (lane & o) != 0;
+#pragma unroll
+                    for (int q = 0; q < o; ++q)
+                    {
+                        const float send = upper ? part[q] : part[q + o];
+                        const float keep = upper ? part[q + o] : part[q];
+                        part[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                    }
+                }
+                if (j[s] < NONE)
+                {
+                    kh[s] = part[0];
+                    exact[s] = false;
+                }
+            }
+        }
+        // rank of every element among the KC (key, j) triples
+        int rank[PER];
+        auto rank_all = [&]() {
+#pragma unroll
+            for (int s = 0; s < PER; ++s)
+                rank[s] = 0;
+#pragma unroll
+            for (int so = 0; so < PER; ++so)
+                for (int m = 0; m < 32; ++m)
+                {
+                    const float hm = __shfl_sync(0xffffffffu, kh[so], m);
+                    const float lm = __shfl_sync(0xffffffffu, kl[so], m);
+                    const int jm = __shfl_sync(0xffffffffu, j[so], m);
+#pragma unroll
+                    for (int s = 0; s < PER; ++s)
+                        rank[s] += key_less_ff(hm, lm, jm, kh[s], kl[s], j[s]) ? 1 : 0;
+                }
+        };
+        rank_all();
+        if (dtype != TK_F64)
+        {
+            // overlap test of rank neighbours among ranks 0..k
+            __syncwarp();
+#pragma unroll
+            for (int s = 0; s < PER; ++s)
+                if (lane + 32 * s < KC)
+                    fr[rank[s]] = kh[s];
+            __syncwarp();
+            bool need[PER];
+            bool any = false;
+#pragma unroll
+            for (int s = 0; s < PER; ++s)
+            {
+                need[s] = false;
+                const int r = rank[s];
+                if (!exact[s] && r <= k)
+                {
+                    const float lo = kh[s] * (1.f - gam), hi = kh[s] * (1.f + gam);
+                    if (r < k && fr[r + 1] * (1.f - gam) <= hi)
+                        need[s] = true;
+                    if (r > 0 && fr[r - 1] * (1.f + gam) >= lo)
+                        need[s] = true;
+                    // distances returned to the caller are exact
+                    if (V.d2_out && r < k)
+                        need[s] = true;
+                }
+                any |= need[s];
+            }
+            if (__any_sync(0xffffffffu, any))
+            {
 #pragma unroll
                 for (int s = 0; s < PER; ++s)
-                    rank[s] += key_less(dm, jm, d[s], j[s]) ? 1 : 0;
+                    if (need[s])
+                    {
+                        const ff e = exact_key(X, dtype, ldx, D, i, j[s]);
+                        kh[s] = e.hi;
+                        kl[s] = e.lo;
+                        exact[s] = true;
+                    }
+                rank_all();
             }
-        // e_k = value of rank k-1
-        double ek = -1.0;
+        }
+        // e_k: an upper bound of the exact k-th distance, from the lane holding
+        // rank k-1
+        unsigned own = 0u;
+        double ek_own = 0.0;
 #pragma unroll
         for (int s = 0; s < PER; ++s)
             if (rank[s] == k - 1)
-                ek = d[s];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            ek = fmax(ek, __shfl_xor_sync(0xffffffffu, ek, o));
-        const float T = cand_val[p * KC + KC - 1];
-        const double nx = (double)nrm[p];
-        const double eps = (double)c1 * (nx + R * R) + (double)c2 * sqrt(nx) * R;
-        const bool full = T < FLT_MAX;  // list not full: every point was kept
-        const bool certified = !full || (ek < (double)T - eps);
+            {
+                own = 1u;
+                ek_own = exact[s] ? (double)kh[s] + (double)kl[s] : (double)kh[s] * (1.0 + (double)gam);
+            }
+        const unsigned holder = __ballot_sync(0xffffffffu, own != 0u);
+        const double ek = __shfl_sync(0xffffffffu, ek_own, holder ? __ffs(holder) - 1 : 0);
+        bool certified = true;
+        if (lane == 0)
+        {
+            const float T = cand_val[p * KC + KC - 1];
+            if (T < FLT_MAX)  // a full list: points outside it are bounded below
+            {
+                const double R = (double)V.R;
+                const double nx = (double)nrm[p];
+                const double eps = (double)c1 * (nx + R * R) + (double)c2 * sqrt(nx) * R;
+                certified = ek < (double)T - eps;
+            }
+        }
+        certified = __shfl_sync(0xffffffffu, certified, 0);
         if (certified)
         {
 #pragma unroll
@@ -245,14 +354,14 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                 {
                     V.idx_out[i * k + rank[s]] = j[s];
                     if (V.d2_out)
-                        V.d2_out[i * k + rank[s]] = d[s];
+                        V.d2_out[i * k + rank[s]] = (double)kh[s] + (double)kl[s];
                 }
         }
         else if (lane == 0)
         {
-            const unsigned f = atomicAdd(nfailed, 1u);
-            failed[f] = (int32_t)p;
-            failed_ub[f] = ek;
+            const unsigned fidx = atomicAdd(nfailed, 1u);
+            failed[fidx] = (int32_t)p;
+            failed_ub[fidx] = ek;
         }
     }
 }
