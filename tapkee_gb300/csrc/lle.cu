@@ -580,14 +580,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
             __syncwarp();
             continue;
         }
-        double sum = 0.0;
+        // w / sum(w) in float-float: the sum, its reciprocal refined by one Newton
+        // step (error ~2^-44), and the products, so that the weights sum to one
+        // to ~1e-13 without an FP64 division
+        ff sum = ff_zero();
         for (int a = lane; a < k; a += 32)
-            sum += (double)S.w[a];
+            sum = ff_add(sum, ff{S.w[a], 0.f});
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
-            sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            sum = ff_add(sum, ff_shfl_xor(sum, o));
+        const float y0 = 1.f / sum.hi;
+        const ff sy = two_prod(sum.hi, y0);
+        const float resid = ((1.f - sy.hi) - sy.lo) - sum.lo * y0;  // 1 - sum * y0
+        const float y1 = y0 * resid;                                 // y = y0 + y1
         for (int a = lane; a < k; a += 32)
-            W[g * k + a] = (double)S.w[a] / sum;
+        {
+            const ff q = two_prod(S.w[a], y0);
+            W[g * k + a] = (double)q.hi + (double)fmaf(S.w[a], y1, q.lo);
+        }
         __syncwarp();
     }
 }
