@@ -611,6 +611,333 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Wide screen for padded dimension 64 and 32-entry lists: one CTA per block of
+// 128 queries, candidate tiles of 256 rows, tcgen05.mma with N = 256 (half the
+// instructions of two N = 128 MMAs and half the shared-memory reads of the A
+// operand per output), two 256-column accumulators double-buffered in TMEM.
+// The epilogue splits each tile's 256 columns between warps 0-3 (columns
+// 0-127) and warps 4-7 (128-255); each keeps its own top-32 per row, and the
+// two lists of a row are merged before they are written. Both half lists hold
+// their half's 32 smallest values, so the merged list is the top 32 of the
+// union and its last value bounds every candidate outside it, as the
+// certification needs.
+constexpr int TW_N = 256;
+constexpr int TW_KC = 32;
+constexpr uint32_t IDESC_W = (1u << 4) | ((uint32_t)(TW_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+
+struct TwCfg
+{
+    static constexpr int A_ATOM = 128 * 128;                 // 128 rows x 128 B
+    static constexpr int B_ATOM = TW_N * 128;                // 256 rows x 128 B
+    static constexpr int A_BYTES = 2 * A_ATOM;               // hi + lo
+    static constexpr int AX_BYTES = 128 * 32;                // constant norm slice of A
+    static constexpr int BX_BYTES = TW_N * 32;               // norm column slice of B
+    static constexpr int B_STAGE = 2 * B_ATOM + BX_BYTES;    // 72 KB
+    static constexpr int STAGES = 2;
+    static constexpr int MERGE_BYTES = 4 * TW_KC * 32 * 8;   // warps 4-7 lists: value + id
+    static constexpr int STASH = 8;
+    static constexpr size_t OFF_B = A_BYTES;
+    static constexpr size_t OFF_AX = OFF_B + (size_t)STAGES * B_STAGE;
+    static constexpr size_t OFF_BAR = OFF_AX + AX_BYTES;
+    static constexpr size_t OFF_MERGE = OFF_BAR + 256;
+    static constexpr size_t OFF_STASH = OFF_MERGE + MERGE_BYTES;
+    static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 1024;
+    static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+struct TwBarriers
+{
+    uint64_t full[2], empty[2], tfull[2], tempty[2], afull, fin;
+    uint32_t tmem_base;
+    int abort;
+};
+
+__device__ __forceinline__ void umma_f16_w(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(IDESC_W), "r"(accumulate));
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_screen_tc_wide(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
+                     const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo,
+                     const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
+                     int64_t Npad, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
+                     const float* __restrict__ nrm, unsigned* err)
+{
+    using C = TwCfg;
+    constexpr int KC = TW_KC;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char* gbase = smem_raw + (base - raw);
+    const uint32_t A_s = base;
+    const uint32_t B_s = base + (uint32_t)C::OFF_B;
+    const uint32_t AX_s = base + (uint32_t)C::OFF_AX;
+    TwBarriers& Bar = *reinterpret_cast<TwBarriers*>(gbase + C::OFF_BAR);
+    float* merge_v = reinterpret_cast<float*>(gbase + C::OFF_MERGE);
+    int32_t* merge_i = reinterpret_cast<int32_t*>(gbase + C::OFF_MERGE + C::MERGE_BYTES / 2);
+    float* stash_all = reinterpret_cast<float*>(gbase + C::OFF_STASH);
+    volatile int* abort = &Bar.abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = (int)(Npad / TW_N);
+    const int64_t q0 = (int64_t)blockIdx.x * TC_M;
+
+    if (threadIdx.x == 0)
+    {
+        for (int st = 0; st < C::STAGES; ++st)
+        {
+            mbar_init(smem_u32(&Bar.full[st]), 1);
+            mbar_init(smem_u32(&Bar.empty[st]), 1);
+        }
+        for (int b = 0; b < 2; ++b)
+        {
+            mbar_init(smem_u32(&Bar.tfull[b]), 1);
+            mbar_init(smem_u32(&Bar.tempty[b]), 8);  // all 8 epilogue warps read each buffer
+        }
+        mbar_init(smem_u32(&Bar.afull), 1);
+        mbar_init(smem_u32(&Bar.fin), 1);
+        Bar.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int t = threadIdx.x; t < C::AX_BYTES / 4; t += blockDim.x)
+        reinterpret_cast<uint32_t*>(gbase + C::OFF_AX)[t] = 0x70007000u;  // 2^13 everywhere
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (warp == 9)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&Bar.tmem_base)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = Bar.tmem_base;
+
+    if (warp == 8)
+    {
+        // ------------------------------------------------------------ producer
+        if (lane == 0)
+        {
+            const uint32_t afull = smem_u32(&Bar.afull);
+            mbar_expect_tx(afull, C::A_BYTES);
+            tma_load_2d(A_s, &tmA_hi, 0, (int)q0, afull);
+            tma_load_2d(A_s + C::A_ATOM, &tmA_lo, 0, (int)q0, afull);
+            ZigZag zz((int)(q0 / TW_N), ntiles);
+            int issued = 0;
+            for (int it = 0; it < ntiles; ++it)
+            {
+                const int tile = zz.next();
+                const int slot = it % C::STAGES;
+                const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
+                if (!mbar_wait(smem_u32(&Bar.empty[slot]), ph ^ 1u, abort, err))
+                    break;
+                const uint32_t fb = smem_u32(&Bar.full[slot]);
+                const uint32_t bst = B_s + slot * C::B_STAGE;
+                mbar_expect_tx(fb, C::B_STAGE);
+                tma_load_2d(bst, &tmB_hi, 0, tile * TW_N, fb);
+                tma_load_2d(bst + C::B_ATOM, &tmB_lo, 0, tile * TW_N, fb);
+                tma_load_2d(bst + 2 * C::B_ATOM, &tm_nrm, 0, tile * TW_N, fb);
+                issued = it + 1;
+            }
+            if (*abort)
+            {
+                volatile int no_abort = 0;
+                mbar_wait(afull, 0u, &no_abort, err);
+                for (int g = (issued > C::STAGES ? issued - C::STAGES : 0); g < issued; ++g)
+                    mbar_wait(smem_u32(&Bar.full[g % C::STAGES]), (uint32_t)(g / C::STAGES) & 1u, &no_abort, err);
+            }
+        }
+    }
+    else if (warp == 9)
+    {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0)
+        {
+            bool ok = mbar_wait(smem_u32(&Bar.afull), 0u, abort, err);
+            tc_fence_after();
+            int issued_any = 0;
+            const uint64_t axd = umma_desc_sw32(AX_s);
+            uint64_t adesc[2][4], bdesc0[2][4];
+#pragma unroll
+            for (int part = 0; part < 2; ++part)
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                {
+                    adesc[part][kk] = umma_desc(A_s + part * C::A_ATOM + (uint32_t)kk * 32u);
+                    bdesc0[part][kk] = umma_desc(B_s + part * C::B_ATOM + (uint32_t)kk * 32u);
+                }
+            const uint64_t bx0 = umma_desc_sw32(B_s + 2 * C::B_ATOM);
+            for (int it = 0; ok && it < ntiles; ++it)
+            {
+                const int slot = it % C::STAGES;
+                const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
+                const int buf = it & 1;
+                const uint32_t bph = (uint32_t)(it >> 1) & 1u;
+                if (!mbar_wait(smem_u32(&Bar.full[slot]), ph, abort, err))
+                    break;
+                if (!mbar_wait(smem_u32(&Bar.tempty[buf]), bph ^ 1u, abort, err))
+                    break;
+                tc_fence_after();
+                const uint64_t soff = (uint64_t)((slot * C::B_STAGE) >> 4);
+                const uint32_t d = tmem + (uint32_t)(buf * TW_N);
+                umma_f16_w(d, axd, bx0 + soff, 0u);  // -|2^s y|^2 / 2 in every row
+#pragma unroll
+                for (int prod = 0; prod < 3; ++prod)
+                {
+                    const int apart = (prod == 2) ? 1 : 0;  // l_x . h_y
+                    const int bpart = (prod == 1) ? 1 : 0;  // h_x . l_y
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk)
+                        umma_f16_w(d, adesc[apart][kk], bdesc0[bpart][kk] + soff, 1u);
+                }
+                umma_commit(smem_u32(&Bar.tfull[buf]));
+                umma_commit(smem_u32(&Bar.empty[slot]));
+                issued_any = 1;
+            }
+            if (issued_any)
+            {
+                volatile int no_abort = 0;
+                umma_commit(smem_u32(&Bar.fin));
+                mbar_wait(smem_u32(&Bar.fin), 0u, &no_abort, err);
+            }
+        }
+    }
+    else
+    {
+        // ------------------------------------------------------------ epilogue
+        const int quad = warp & 3;
+        const int half = warp >> 2;
+        const int row = quad * 32 + lane;
+        const int64_t q = q0 + row;
+        const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);
+        const float inv_m2 = 1.0f / m2;
+        float* stash = stash_all + (warp * 32 + lane) * (C::STASH + 1);
+        float L[KC];
+        int32_t Ix[KC];
+#pragma unroll
+        for (int s = 0; s < KC; ++s)
+        {
+            L[s] = FLT_MAX;
+            Ix[s] = -1;
+        }
+        float cmp = FLT_MAX;
+        float thr = -__int_as_float(0x7f800000);
+        ZigZag zz((int)(q0 / TW_N), ntiles);
+        bool alive = true;
+        for (int it = 0; it < ntiles; ++it)
+        {
+            const int tile = zz.next();
+            const int buf = it & 1;
+            const uint32_t bph = (uint32_t)(it >> 1) & 1u;
+            const bool ok = mbar_wait(smem_u32(&Bar.tfull[buf]), bph, abort, err);
+            if (!__all_sync(0xffffffffu, ok))
+            {
+                alive = false;
+                break;
+            }
+            tc_fence_after();
+            const int64_t c0 = (int64_t)tile * TW_N + half * 128;
+            const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * TW_N + half * 128);
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h)
+            {
+                float v[64];
+                tmem_ld32_nowait(tacc + h * 64, v);
+                tmem_ld32_nowait(tacc + h * 64 + 32, v + 32);
+                tmem_wait_ld();
+                if (h == 1)
+                {
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0)
+                        mbar_arrive(smem_u32(&Bar.tempty[buf]));
+                }
+#pragma unroll
+                for (int s32 = 0; s32 < 2; ++s32)
+                {
+                    float gm[4];
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+                    {
+                        const float* w = v + s32 * 32 + g * 8;
+                        gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
+                                      fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
+                    }
+                    if (fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3])) > thr)
+                    {
+#pragma unroll
+                        for (int g = 0; g < 4; ++g)
+                        {
+                            if (gm[g] > thr)
+                            {
+#pragma unroll
+                                for (int e = 0; e < 8; ++e)
+                                    stash[e] = v[s32 * 32 + g * 8 + e];
+                                const int64_t cb = c0 + h * 64 + s32 * 32 + g * 8;
+#pragma unroll 1
+                                for (int e = 0; e < 8; ++e)
+                                {
+                                    const float t = m2 * stash[e];
+                                    if (t < cmp && cb + e < N)
+                                    {
+                                        reg_insert<KC>(L, Ix, t, (int32_t)(cb + e));
+                                        cmp = L[KC - 1];
+                                        thr = cmp * inv_m2;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        // merge the two half lists of each row (named barrier of the 8 epilogue warps)
+        if (half == 1)
+        {
+#pragma unroll
+            for (int s = 0; s < KC; ++s)
+            {
+                merge_v[(quad * KC + s) * 32 + lane] = L[s];
+                merge_i[(quad * KC + s) * 32 + lane] = Ix[s];
+            }
+        }
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+        if (half == 0 && __all_sync(0xffffffffu, alive))
+        {
+#pragma unroll 1
+            for (int s = 0; s < KC; ++s)
+            {
+                const float t = merge_v[(quad * KC + s) * 32 + lane];
+                if (t < cmp)  // the other list is sorted: later entries are no smaller
+                {
+                    reg_insert<KC>(L, Ix, t, merge_i[(quad * KC + s) * 32 + lane]);
+                    cmp = L[KC - 1];
+                }
+            }
+            const float nq = nrm[q];
+#pragma unroll
+            for (int s = 0; s < KC; ++s)
+            {
+                cand_idx[q * KC + s] = Ix[s];
+                cand_val[q * KC + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 9)
+    {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -626,11 +953,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int box_cols, CUtensorMapSwizzle sw)
+void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int box_cols, CUtensorMapSwizzle sw,
+              int box_rows = 128)
 {
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)box_cols, 128};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
     CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, (void*)base, dims, strides, box, estr,
                              CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -657,6 +985,21 @@ void launch(tk_ctx* ctx, const uint16_t* xh, const uint16_t* xl, const uint16_t*
     TK_CHECK_LAUNCH();
 }
 
+void launch_wide(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
+{
+    CUtensorMap ah, al, bh, bl, bn;
+    make_map(&ah, P.xh, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, 128);
+    make_map(&al, P.xl, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, 128);
+    make_map(&bh, P.xh, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, TW_N);
+    make_map(&bl, P.xl, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, TW_N);
+    make_map(&bn, P.xn, P.Npad, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B, TW_N);
+    TK_CUDA(cudaFuncSetAttribute(k_screen_tc_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TwCfg::SMEM));
+    const int grid = (int)(P.Npad / TC_M);
+    k_screen_tc_wide<<<grid, TC_THREADS, TwCfg::SMEM, ctx->stream>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad,
+                                                                     cand_idx, cand_val, P.nrm, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+}
+
 template <int DP, int KC>
 void launch_single(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
 {
@@ -676,7 +1019,7 @@ void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, fl
     if (P.Dp == 64)
     {
         if (kc == 32)
-            launch_single<64, 32>(ctx, P, cand_idx, cand_val);
+            launch_wide(ctx, P, cand_idx, cand_val);
         else
             launch_single<64, 64>(ctx, P, cand_idx, cand_val);
     }
