@@ -334,39 +334,13 @@ __global__ void k_codes(const float* proj, int64_t N, const unsigned* bbox, int 
     }
 }
 
-// exclusive scan of nb counters by one block of 1024 threads
-__global__ void k_scan(unsigned* hist, int nb)
-{
-    __shared__ unsigned part[1024];
-    const int t = threadIdx.x;
-    const int per = (nb + 1023) / 1024;
-    const int b0 = t * per, b1 = min(nb, b0 + per);
-    unsigned s = 0;
-    for (int b = b0; b < b1; ++b)
-        s += hist[b];
-    part[t] = s;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1)
-    {
-        unsigned v = (t >= o) ? part[t - o] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    unsigned run = part[t] - s;
-    for (int b = b0; b < b1; ++b)
-    {
-        const unsigned c = hist[b];
-        hist[b] = run;
-        run += c;
-    }
-}
-
-__global__ void k_scatter(const unsigned* bucket, int64_t N, unsigned* offs, int32_t* perm)
+// position = bucket offset (exclusive scan of the histogram) + arrival order
+__global__ void k_scatter(const unsigned* bucket, int64_t N, const int64_t* offs, unsigned* fill, int32_t* perm)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
     {
-        const unsigned pos = atomicAdd(&offs[bucket[i]], 1u);
+        const unsigned b = bucket[i];
+        const int64_t pos = offs[b] + atomicAdd(&fill[b], 1u);
         perm[pos] = (int32_t)i;
     }
 }
@@ -500,14 +474,15 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     const int nb = 1 << bits;
     const int shift = 30 - bits;
     unsigned* bucket = (unsigned*)ctx->scratch.get("prep.bucket", sizeof(unsigned) * (size_t)N);
-    unsigned* hist = (unsigned*)ctx->scratch.get("prep.hist", sizeof(unsigned) * (size_t)nb);
-    TK_CUDA(cudaMemsetAsync(hist, 0, sizeof(unsigned) * (size_t)nb, st));
+    unsigned* hist = (unsigned*)ctx->scratch.get("prep.hist", sizeof(unsigned) * (size_t)nb * 2);
+    unsigned* fill = hist + nb;
+    int64_t* offs = (int64_t*)ctx->scratch.get("prep.offs", sizeof(int64_t) * ((size_t)nb + 1));
+    TK_CUDA(cudaMemsetAsync(hist, 0, sizeof(unsigned) * (size_t)nb * 2, st));
     k_codes<<<2 * sms, 256, 0, st>>>(proj, N, small + 8, shift, bucket, hist);
     TK_CHECK_LAUNCH();
-    k_scan<<<1, 1024, 0, st>>>(hist, nb);
-    TK_CHECK_LAUNCH();
+    scan_to_offsets(ctx, reinterpret_cast<const int*>(hist), nb, offs);
     P.perm = (int32_t*)ctx->scratch.get("prep.perm", sizeof(int32_t) * (size_t)N);
-    k_scatter<<<2 * sms, 256, 0, st>>>(bucket, N, hist, P.perm);
+    k_scatter<<<2 * sms, 256, 0, st>>>(bucket, N, offs, fill, P.perm);
     TK_CHECK_LAUNCH();
 
     // 5. layout
