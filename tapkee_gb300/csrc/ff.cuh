@@ -56,6 +56,33 @@ __device__ __forceinline__ ff ff_fma(ff acc, float ah, float al, float bh, float
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+
+// a * b, dropping a.lo * b.lo
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+    ff p = two_prod(a.hi, b.hi);
+    p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+    return fast_two_sum(p.hi, p.lo);
+}
+
+// a / n for a float n (one correction step: ~2^-46 relative)
+__device__ __forceinline__ ff ff_div_f(ff a, float n)
+{
+    const float q = a.hi / n;
+    const float r = fmaf(-q, n, a.hi) + a.lo;
+    return fast_two_sum(q, r / n);
+}
+
+// 1 / sqrt(a) for a > 0: one Newton step from the FP32 estimate (~2^-44)
+__device__ __forceinline__ ff ff_rsqrt(ff a)
+{
+    const float y = rsqrtf(a.hi);
+    const ff yy = two_prod(y, y);
+    const ff e = ff_add(ff{1.f, 0.f}, ff_neg(ff_mul(a, yy)));  // 1 - a y^2
+    return fast_two_sum(y, 0.5f * y * (e.hi + e.lo));
+}
+
 __device__ __forceinline__ ff ff_shfl_xor(ff a, int m)
 {
     return ff{__shfl_xor_sync(0xffffffffu, a.hi, m), __shfl_xor_sync(0xffffffffu, a.lo, m)};

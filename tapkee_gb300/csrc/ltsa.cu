@@ -20,11 +20,6 @@
 namespace tk {
 namespace {
 
-__device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
-{
-    return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
-}
-
 template <int M, typename T>
 struct JacobiSmem
 {
@@ -33,12 +28,50 @@ struct JacobiSmem
     T rc[M / 2], rs[M / 2];
     int rp[M / 2], rq[M / 2];
     float Z[M][33];
-    float Zl[M][33];     // low parts of the centred coordinates (refinement)
+    float Zl[M][33];     // low parts of the centred coordinates
     float th[32][8], tl[32][8];  // t = Zc^T V for one chunk, float-float
-    double GV[M][8];     // G V for the refined basis
-    double Vt[M][8];     // refined basis
-    double lam[M];
+    float Vf[M][8];      // FP32 top eigenvectors
+    float GVh[M][8], GVl[M][8];  // G V, float-float
+    float Rf[M][8];      // residual G V - V Lam
+    float UR[M][8];      // (u_j . R_t) / (Lam_t - lambda_j)
+    float Oh[M][8], Ol[M][8];    // refined basis, float-float
+    float Lh[8][8], Ll[8][8];    // Rayleigh quotient V^T G V, float-float
 };
+
+// x as a float pair (exact for float32 input, hi + lo split for float64)
+__device__ __forceinline__ ff x_ff(const void* X, int dtype, int64_t off)
+{
+    if (dtype == TK_F64)
+    {
+        const double v = reinterpret_cast<const double*>(X)[off];
+        const float h = (float)v;
+        return ff{h, (float)(v - (double)h)};
+    }
+    return ff{reinterpret_cast<const float*>(X)[off], 0.f};
+}
+
+// Coordinates of the neighbours of one point in dimensions [d0, d0 + 32),
+// centred on their mean, in float-float: Z[a][lane] + Zl[a][lane] = x_{n_a} -
+// mean for d = d0 + lane (zero for a >= k or d >= D).
+template <int M, typename T>
+__device__ __forceinline__ void stage_centred(JacobiSmem<M, T>& S, int lane, const void* X, int dtype, int64_t ldx,
+                                              int D, const int32_t* nbrs, int k, int d0)
+{
+    const int d = d0 + lane;
+    ff sum = ff_zero();
+    if (d < D)
+        for (int a = 0; a < k; ++a)
+            sum = ff_add(sum, x_ff(X, dtype, (int64_t)nbrs[a] * ldx + d));
+    const ff mean = ff_div_f(sum, (float)k);
+    for (int a = 0; a < M; ++a)
+    {
+        ff z = ff_zero();
+        if (a < k && d < D)
+            z = ff_add(x_ff(X, dtype, (int64_t)nbrs[a] * ldx + d), ff_neg(mean));
+        S.Z[a][lane] = z.hi;
+        S.Zl[a][lane] = z.lo;
+    }
+}
 
 // Parallel cyclic Jacobi on the symmetric M x M matrix S.A (one warp). On exit
 // diag(A) holds the eigenvalues and the columns of V the eigenvectors.
@@ -66,10 +99,13 @@ __device__ void warp_jacobi(JacobiSmem<M, T>& S, int lane, int max_sweeps)
             off += __shfl_xor_sync(0xffffffffu, off, o);
             dia += __shfl_xor_sync(0xffffffffu, dia, o);
         }
-        // stop when the off-diagonal mass is at the working precision's level:
-        // FP32 -> rms off-diagonal ~1e-6 of the diagonal, enough for the
-        // float-float refinement that follows; FP64 -> ~1e-13
-        const T tol = sizeof(T) == 8 ? T(1e-26) : T(1e-12);
+        // stop when the off-diagonal mass reaches the rounding floor of the
+        // working precision: rotations leave off-diagonal entries of order
+        // eps |A|, so off / dia cannot fall much below (M eps)^2; (8 M eps)^2
+        // sits safely above that floor (FP32: ~1e-10 at M = 20, enough for the
+        // float-float refinement that follows)
+        const T eps = sizeof(T) == 8 ? T(1.1102230246251565e-16) : T(5.9604644775390625e-08);
+        const T tol = (T(8 * M) * eps) * (T(8 * M) * eps);
         if (off <= tol * dia || dia == T(0))
             break;
         for (int round = 0; round < M - 1; ++round)
@@ -128,7 +164,9 @@ __device__ void warp_jacobi(JacobiSmem<M, T>& S, int lane, int max_sweeps)
     }
 }
 
-// Builds the centred neighbour Gram of point i into S.A (type T, M x M, zero padded).
+// Builds the centred neighbour Gram of point i into S.A (type T, M x M, zero
+// padded): FP32 products of the high parts for T = float (the refinement
+// corrects what this drops), exact pair products in FP64 for T = double.
 template <int M, typename T>
 __device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
                              const int32_t* nbrs, int k)
@@ -138,14 +176,7 @@ __device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int d
     __syncwarp();
     for (int d0 = 0; d0 < D; d0 += 32)
     {
-        const int d = d0 + lane;
-        double mean = 0.0;
-        if (d < D)
-            for (int a = 0; a < k; ++a)
-                mean += ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d);
-        mean /= (double)k;
-        for (int a = 0; a < M; ++a)
-            S.Z[a][lane] = (a < k && d < D) ? (float)(ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d) - mean) : 0.f;
+        stage_centred<M, T>(S, lane, X, dtype, ldx, D, nbrs, k, d0);
         __syncwarp();
         for (int e = lane; e < M * M; e += 32)
         {
@@ -154,7 +185,12 @@ __device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int d
                 continue;
             T s = T(0);
             for (int dd = 0; dd < 32; ++dd)
-                s += (T)S.Z[a][dd] * (T)S.Z[b][dd];
+            {
+                if (sizeof(T) == 8)
+                    s += ((T)S.Z[a][dd] + (T)S.Zl[a][dd]) * ((T)S.Z[b][dd] + (T)S.Zl[b][dd]);
+                else
+                    s += (T)S.Z[a][dd] * (T)S.Z[b][dd];
+            }
             S.A[a][b] += s;
             if (a != b)
                 S.A[b][a] += s;
@@ -165,23 +201,23 @@ __device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int d
 
 // First-order refinement of the top-td invariant subspace. The FP32 Jacobi gives
 // eigenpairs (lambda_j, u_j) of the FP32 Gram; the residual R = G V - V (V^T G V)
-// of the exact Gram G = Zc Zc^T is formed in float-float from the FP64-centred
+// of the exact Gram G = Zc Zc^T is formed in float-float from the exactly centred
 // coordinates, and each top vector is corrected by
 //     v_i += sum_{j not top} u_j (u_j . R_i) / (lambda_i - lambda_j),
-// then the basis is re-orthonormalised in FP64. This removes the FP32 Gram and
-// Jacobi errors to first order (error ~ eps^2 / gap).
+// then the basis is re-orthonormalised (modified Gram-Schmidt) in float-float.
+// This removes the FP32 Gram and Jacobi errors to first order (error ~ eps^2 /
+// gap). Everything runs on the FP32 pipes; the result is S.Oh + S.Ol.
 template <int M>
 __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
                                 const int32_t* nbrs, int k, int td, const int* top)
 {
-    // V_t (FP32 columns of the top eigenvectors, k x td)
+    constexpr int RPL = (M + 31) / 32;  // basis rows per lane: a = lane + 32 r
     for (int e = lane; e < M * td; e += 32)
     {
         const int a = e / td, t = e % td;
-        S.Vt[a][t] = (a < k) ? (double)S.V[a][top[t]] : 0.0;
+        S.Vf[a][t] = (a < k) ? S.V[a][top[t]] : 0.f;
     }
     __syncwarp();
-    constexpr int RPL = (M + 31) / 32;  // basis rows per lane: a = lane + 32 r
     ff acc[RPL][8];
 #pragma unroll
     for (int r = 0; r < RPL; ++r)
@@ -189,33 +225,16 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
             acc[r][t] = ff_zero();
     for (int d0 = 0; d0 < D; d0 += 32)
     {
-        const int d = d0 + lane;
-        double mean = 0.0;
-        if (d < D)
-            for (int a = 0; a < k; ++a)
-                mean += ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d);
-        mean /= (double)k;
-        for (int a = 0; a < M; ++a)
-        {
-            float h = 0.f, l = 0.f;
-            if (a < k && d < D)
-            {
-                const double z = ldx_elem(X, dtype, (int64_t)nbrs[a] * ldx + d) - mean;
-                h = (float)z;
-                l = (float)(z - (double)h);
-            }
-            S.Z[a][lane] = h;
-            S.Zl[a][lane] = l;
-        }
+        stage_centred<M, float>(S, lane, X, dtype, ldx, D, nbrs, k, d0);
         __syncwarp();
         // t_d = sum_a z_ad v_a   (lane = d)
         for (int t = 0; t < td; ++t)
         {
-            ff s = ff_zero();
+            ff sacc = ff_zero();
             for (int a = 0; a < k; ++a)
-                s = ff_fma(s, S.Z[a][lane], S.Zl[a][lane], (float)S.Vt[a][t], 0.f);
-            S.th[lane][t] = s.hi;
-            S.tl[lane][t] = s.lo;
+                sacc = ff_fma(sacc, S.Z[a][lane], S.Zl[a][lane], S.Vf[a][t], 0.f);
+            S.th[lane][t] = sacc.hi;
+            S.tl[lane][t] = sacc.lo;
         }
         __syncwarp();
         // (G V)_a += sum_d z_ad t_d   (a = lane + 32 r)
@@ -239,86 +258,107 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
         const int a = lane + 32 * r;
         if (a < M)
             for (int t = 0; t < td; ++t)
-                S.GV[a][t] = (a < k) ? ff_to_double(acc[r][t]) : 0.0;
+            {
+                S.GVh[a][t] = (a < k) ? acc[r][t].hi : 0.f;
+                S.GVl[a][t] = (a < k) ? acc[r][t].lo : 0.f;
+            }
     }
     __syncwarp();
-    // Rayleigh quotient Lambda = V^T G V (td x td) and residual R = G V - V Lambda
-    __shared__ double Lam_s[4][8][8];  // up to 4 warps per block
-    double* Lam = &Lam_s[(threadIdx.x >> 5) & 3][0][0];
+    // Rayleigh quotient Lam = V^T G V (td x td)
     for (int e = lane; e < td * td; e += 32)
     {
-        const int i = e / td, j = e % td;
-        double s = 0.0;
+        const int ii = e / td, jj = e % td;
+        ff sacc = ff_zero();
         for (int a = 0; a < k; ++a)
-            s += S.Vt[a][i] * S.GV[a][j];
-        Lam[i * 8 + j] = s;
+            sacc = ff_fma(sacc, S.Vf[a][ii], 0.f, S.GVh[a][jj], S.GVl[a][jj]);
+        S.Lh[ii][jj] = sacc.hi;
+        S.Ll[ii][jj] = sacc.lo;
     }
     __syncwarp();
-    // corrections (rows a = lane + 32 r of the basis)
-    double corr[RPL][8];
-#pragma unroll
-    for (int r = 0; r < RPL; ++r)
-        for (int t = 0; t < td; ++t)
-            corr[r][t] = 0.0;
-    for (int j = 0; j < k; ++j)
-    {
-        bool is_top = false;
-        for (int t = 0; t < td; ++t)
-            is_top |= (top[t] == j);
-        if (is_top)
-            continue;
-        const double lj = (double)S.A[j][j];
-        for (int t = 0; t < td; ++t)
-        {
-            // u_j . R_t with R_t = GV_t - sum_s V_s Lam[s][t]
-            double ur = 0.0;
-            for (int a = 0; a < k; ++a)
-            {
-                double r = S.GV[a][t];
-                for (int q = 0; q < td; ++q)
-                    r -= S.Vt[a][q] * Lam[q * 8 + t];
-                ur += (double)S.V[a][j] * r;
-            }
-            const double gap = Lam[t * 8 + t] - lj;
-#pragma unroll
-            for (int r = 0; r < RPL; ++r)
-            {
-                const int a = lane + 32 * r;
-                if (a < k && gap != 0.0)
-                    corr[r][t] += (double)S.V[a][j] * ur / gap;
-            }
-        }
-    }
-    __syncwarp();
+    // residual R = G V - V Lam, in float-float, kept in FP32
 #pragma unroll
     for (int r = 0; r < RPL; ++r)
     {
         const int a = lane + 32 * r;
-        if (a < k)
+        if (a < M)
             for (int t = 0; t < td; ++t)
-                S.Vt[a][t] += corr[r][t];
+            {
+                ff rr = ff{S.GVh[a][t], S.GVl[a][t]};
+                for (int q = 0; q < td; ++q)
+                    rr = ff_fma(rr, -S.Vf[a][q], 0.f, S.Lh[q][t], S.Ll[q][t]);
+                S.Rf[a][t] = (a < k) ? rr.hi + rr.lo : 0.f;
+            }
     }
     __syncwarp();
-    // modified Gram-Schmidt (FP64) on the td columns
+    // (u_j . R_t) / (Lam_t - lambda_j) for every non-top eigenvector (lanes over j)
+    for (int j = lane; j < M; j += 32)
+    {
+        bool is_top = false;
+        for (int t = 0; t < td; ++t)
+            is_top |= (top[t] == j);
+        const float lj = S.A[j][j];
+        for (int t = 0; t < td; ++t)
+        {
+            float ur = 0.f;
+            if (!is_top)
+                for (int a = 0; a < k; ++a)
+                    ur = fmaf(S.V[a][j], S.Rf[a][t], ur);
+            const float gap = S.Lh[t][t] - lj;
+            S.UR[j][t] = (!is_top && gap != 0.f) ? ur / gap : 0.f;
+        }
+    }
+    __syncwarp();
+    // corrected basis (rows a = lane + 32 r), float-float
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+    {
+        const int a = lane + 32 * r;
+        if (a < M)
+            for (int t = 0; t < td; ++t)
+            {
+                float c = 0.f;
+                if (a < k)
+                    for (int j = 0; j < M; ++j)
+                        c = fmaf(S.V[a][j], S.UR[j][t], c);
+                const ff o = two_sum(S.Vf[a][t], c);
+                S.Oh[a][t] = o.hi;
+                S.Ol[a][t] = o.lo;
+            }
+    }
+    __syncwarp();
+    // modified Gram-Schmidt in float-float on the td columns
     for (int t = 0; t < td; ++t)
     {
-        for (int q = 0; q < t; ++q)
+        for (int q = 0; q <= t; ++q)
         {
-            double dot = 0.0;
-            for (int a = 0; a < k; ++a)
-                dot += S.Vt[a][t] * S.Vt[a][q];
-            __syncwarp();
+            ff dot = ff_zero();
             for (int a = lane; a < k; a += 32)
-                S.Vt[a][t] -= dot * S.Vt[a][q];
+                dot = ff_fma(dot, S.Oh[a][t], S.Ol[a][t], S.Oh[a][q], S.Ol[a][q]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                dot = ff_add(dot, ff_shfl_xor(dot, o));
+            __syncwarp();
+            if (q < t)
+            {
+                for (int a = lane; a < k; a += 32)
+                {
+                    const ff v = ff_add(ff{S.Oh[a][t], S.Ol[a][t]}, ff_neg(ff_mul(dot, ff{S.Oh[a][q], S.Ol[a][q]})));
+                    S.Oh[a][t] = v.hi;
+                    S.Ol[a][t] = v.lo;
+                }
+            }
+            else
+            {
+                const ff inv = ff_rsqrt(dot);
+                for (int a = lane; a < k; a += 32)
+                {
+                    const ff v = ff_mul(ff{S.Oh[a][t], S.Ol[a][t]}, inv);
+                    S.Oh[a][t] = v.hi;
+                    S.Ol[a][t] = v.lo;
+                }
+            }
             __syncwarp();
         }
-        double nrm = 0.0;
-        for (int a = 0; a < k; ++a)
-            nrm += S.Vt[a][t] * S.Vt[a][t];
-        __syncwarp();
-        for (int a = lane; a < k; a += 32)
-            S.Vt[a][t] /= sqrt(nrm);
-        __syncwarp();
     }
 }
 
@@ -339,36 +379,56 @@ __global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, i
         __syncwarp();
         centred_gram<M, float>(S, lane, X, dtype, ldx, D, nb_s[wib], k);
         warp_jacobi<M, float>(S, lane, 30);
-        // order eigenvalues (lane 0): top td indices and the next one
+        // top td eigenvalues and the next one: warp arg-max rounds over the
+        // diagonal (ties to the lower index)
         __shared__ int top_s[WARPS][8];
-        if (lane == 0)
         {
-            float lmax = -FLT_MAX;
-            int chosen[9];
+            float dv[(M + 31) / 32];
+#pragma unroll
+            for (int r = 0; r < (M + 31) / 32; ++r)
+            {
+                const int c = lane + 32 * r;
+                dv[r] = (c < M) ? S.A[c][c] : -FLT_MAX;
+            }
+            float lmax = 0.f, lsel[9];
             for (int t = 0; t <= td && t < M; ++t)
             {
-                int best = -1;
                 float bv = -FLT_MAX;
-                for (int c = 0; c < M; ++c)
-                {
-                    bool used = false;
-                    for (int u = 0; u < t; ++u)
-                        used |= (chosen[u] == c);
-                    if (!used && S.A[c][c] > bv)
+                int bi = 0x7fffffff;
+#pragma unroll
+                for (int r = 0; r < (M + 31) / 32; ++r)
+                    if (dv[r] > bv)
                     {
-                        bv = S.A[c][c];
-                        best = c;
+                        bv = dv[r];
+                        bi = lane + 32 * r;
+                    }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ov > bv || (ov == bv && oi < bi))
+                    {
+                        bv = ov;
+                        bi = oi;
                     }
                 }
-                chosen[t] = best;
+#pragma unroll
+                for (int r = 0; r < (M + 31) / 32; ++r)
+                    if (lane + 32 * r == bi)
+                        dv[r] = -FLT_MAX;
+                if (lane == 0 && t < td)
+                    top_s[wib][t] = bi;
                 if (t == 0)
                     lmax = bv;
+                lsel[t] = bv;
             }
-            for (int t = 0; t < td; ++t)
-                top_s[wib][t] = chosen[t];
-            const float gap = S.A[chosen[td - 1]][chosen[td - 1]] - (td < M ? S.A[chosen[td]][chosen[td]] : 0.f);
-            if (!(gap > 1e-6f * fabsf(lmax)))
-                refine[atomicAdd(nrefine, 1u)] = (int32_t)i;
+            if (lane == 0)
+            {
+                const float gap = lsel[td - 1] - (td < M ? lsel[td] : 0.f);
+                if (!(gap > 1e-6f * fabsf(lmax)))
+                    refine[atomicAdd(nrefine, 1u)] = (int32_t)i;
+            }
         }
         __syncwarp();
         int top[8];
@@ -378,7 +438,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, i
         for (int e = lane; e < k * td; e += 32)
         {
             const int a = e / td, t = e % td;
-            V[(i * k + a) * td + t] = S.Vt[a][t];
+            V[(i * k + a) * td + t] = (double)S.Oh[a][t] + (double)S.Ol[a][t];
         }
         __syncwarp();
     }
