@@ -622,6 +622,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // their half's 32 smallest values, so the merged list is the top 32 of the
 // union and its last value bounds every candidate outside it, as the
 // certification needs.
+// Near and far tiles: tiles whose bounding sphere is close to the query block's
+// (k_classify) get the full 3-product split; the others only h_x . h_y (5 MMAs
+// instead of 13, and no low-part loads). The epilogue records, per row, the
+// smallest screened value over far tiles (far_val), which the re-rank certifies
+// against with the larger error bound of high-part products.
 constexpr int TW_N = 256;
 constexpr int TW_KC = 32;
 constexpr uint32_t IDESC_W = (1u << 4) | ((uint32_t)(TW_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
@@ -642,7 +647,7 @@ struct TwCfg
     static constexpr size_t OFF_BAR = OFF_AX + AX_BYTES;
     static constexpr size_t OFF_MERGE = OFF_BAR + 256;
     static constexpr size_t OFF_STASH = OFF_MERGE + MERGE_BYTES;
-    static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 1024;
+    static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 128 * 4 + 1024;
     static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
@@ -665,7 +670,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     k_screen_tc_wide(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
                      const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo,
                      const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
-                     int64_t Npad, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
+                     int64_t Npad, const uint32_t* __restrict__ near_bits, int nwords,
+                     int32_t* __restrict__ cand_idx, float* __restrict__ cand_val, float* __restrict__ far_val,
                      const float* __restrict__ nrm, unsigned* err)
 {
     using C = TwCfg;
@@ -686,6 +692,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ntiles = (int)(Npad / TW_N);
     const int64_t q0 = (int64_t)blockIdx.x * TC_M;
+    // near (full fp16 split) or far (high parts only) pair of this query block and a tile
+    const uint32_t* nb_row = near_bits + (int64_t)blockIdx.x * nwords;
+    auto is_near = [&](int tile) { return ((__ldg(nb_row + (tile >> 5)) >> (tile & 31)) & 1u) != 0u; };
 
     if (threadIdx.x == 0)
     {
@@ -738,9 +747,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 const uint32_t fb = smem_u32(&Bar.full[slot]);
                 const uint32_t bst = B_s + slot * C::B_STAGE;
-                mbar_expect_tx(fb, C::B_STAGE);
+                const bool nr = is_near(tile);
+                mbar_expect_tx(fb, nr ? (uint32_t)C::B_STAGE : (uint32_t)(C::B_ATOM + C::BX_BYTES));
                 tma_load_2d(bst, &tmB_hi, 0, tile * TW_N, fb);
-                tma_load_2d(bst + C::B_ATOM, &tmB_lo, 0, tile * TW_N, fb);
+                if (nr)
+                    tma_load_2d(bst + C::B_ATOM, &tmB_lo, 0, tile * TW_N, fb);
                 tma_load_2d(bst + 2 * C::B_ATOM, &tm_nrm, 0, tile * TW_N, fb);
                 issued = it + 1;
             }
@@ -772,8 +783,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     bdesc0[part][kk] = umma_desc(B_s + part * C::B_ATOM + (uint32_t)kk * 32u);
                 }
             const uint64_t bx0 = umma_desc_sw32(B_s + 2 * C::B_ATOM);
+            ZigZag zz((int)(q0 / TW_N), ntiles);
             for (int it = 0; ok && it < ntiles; ++it)
             {
+                const bool nr = is_near(zz.next());
                 const int slot = it % C::STAGES;
                 const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
                 const int buf = it & 1;
@@ -787,13 +800,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t d = tmem + (uint32_t)(buf * TW_N);
                 umma_f16_w(d, axd, bx0 + soff, 0u);  // -|2^s y|^2 / 2 in every row
 #pragma unroll
-                for (int prod = 0; prod < 3; ++prod)
+                for (int kk = 0; kk < 4; ++kk)
+                    umma_f16_w(d, adesc[0][kk], bdesc0[0][kk] + soff, 1u);  // h_x . h_y
+                if (nr)
                 {
-                    const int apart = (prod == 2) ? 1 : 0;  // l_x . h_y
-                    const int bpart = (prod == 1) ? 1 : 0;  // h_x . l_y
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk)
-                        umma_f16_w(d, adesc[apart][kk], bdesc0[bpart][kk] + soff, 1u);
+                        umma_f16_w(d, adesc[0][kk], bdesc0[1][kk] + soff, 1u);  // h_x . l_y
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk)
+                        umma_f16_w(d, adesc[1][kk], bdesc0[0][kk] + soff, 1u);  // l_x . h_y
                 }
                 umma_commit(smem_u32(&Bar.tfull[buf]));
                 umma_commit(smem_u32(&Bar.empty[slot]));
@@ -827,6 +843,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         float cmp = FLT_MAX;
         float thr = -__int_as_float(0x7f800000);
+        float far_max = -__int_as_float(0x7f800000);  // largest accumulator over far tiles
         ZigZag zz((int)(q0 / TW_N), ntiles);
         bool alive = true;
         for (int it = 0; it < ntiles; ++it)
@@ -843,6 +860,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc_fence_after();
             const int64_t c0 = (int64_t)tile * TW_N + half * 128;
             const uint32_t tacc = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * TW_N + half * 128);
+            const bool far_tile = !is_near(tile);
+            const bool ragged = c0 + 128 > N;  // padding columns must not enter far_max
 #pragma unroll 1
             for (int h = 0; h < 2; ++h)
             {
@@ -868,7 +887,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
                                       fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
                     }
-                    if (fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3])) > thr)
+                    const float g32 = fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3]));
+                    if (far_tile)
+                    {
+                        if (!ragged)
+                            far_max = fmaxf(far_max, g32);
+                        else
+                        {
+#pragma unroll
+                            for (int e = 0; e < 32; ++e)
+                                if (c0 + h * 64 + s32 * 32 + e < N)
+                                    far_max = fmaxf(far_max, v[s32 * 32 + e]);
+                        }
+                    }
+                    if (g32 > thr)
                     {
 #pragma unroll
                         for (int g = 0; g < 4; ++g)
@@ -897,6 +929,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
         // merge the two half lists of each row (named barrier of the 8 epilogue warps)
+        float* merge_far = stash_all + 8 * 32 * (C::STASH + 1);  // 128 floats after the stashes
         if (half == 1)
         {
 #pragma unroll
@@ -905,6 +938,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 merge_v[(quad * KC + s) * 32 + lane] = L[s];
                 merge_i[(quad * KC + s) * 32 + lane] = Ix[s];
             }
+            merge_far[row] = far_max;
         }
         asm volatile("bar.sync 1, 256;" ::: "memory");
         if (half == 0 && __all_sync(0xffffffffu, alive))
@@ -926,6 +960,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 cand_idx[q * KC + s] = Ix[s];
                 cand_val[q * KC + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
             }
+            // smallest screened value over far tiles (high-part products only)
+            const float fm = fmaxf(far_max, merge_far[row]);
+            far_val[q] = (fm > -FLT_MAX) ? m2 * fm + nq : FLT_MAX;
         }
     }
 
@@ -935,6 +972,105 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    }
+}
+
+// Bounding sphere (centre, radius) of every block of ROWS sorted rows of xc
+// (valid rows only; radius -1 for a block without valid rows). One CTA per block.
+template <int ROWS>
+__global__ void __launch_bounds__(256) k_spheres(const float* __restrict__ xc, int64_t N, int Dp, float* ctr,
+                                                 float* rad)
+{
+    __shared__ float part[256];
+    __shared__ float c_s[128];
+    __shared__ float wmax[8];
+    const int64_t r0 = (int64_t)blockIdx.x * ROWS;
+    const int nvalid = (int)max((int64_t)0, min((int64_t)ROWS, N - r0));
+    const int t = threadIdx.x;
+    // centre: thread t sums dimension t % Dp over rows t / Dp, + 256 / Dp, ...
+    const int per = 256 / Dp;
+    float sacc = 0.f;
+    if (t < per * Dp)
+        for (int r = t / Dp; r < nvalid; r += per)
+            sacc += xc[(r0 + r) * Dp + t % Dp];
+    part[t] = sacc;
+    __syncthreads();
+    if (t < Dp)
+    {
+        float tot = 0.f;
+        for (int q = 0; q < per; ++q)
+            tot += part[q * Dp + t];
+        c_s[t] = nvalid > 0 ? tot / (float)nvalid : 0.f;
+        ctr[(int64_t)blockIdx.x * Dp + t] = c_s[t];
+    }
+    __syncthreads();
+    const int lane = t & 31, w = t >> 5;
+    float rmax2 = 0.f;
+    for (int r = w; r < nvalid; r += 8)
+    {
+        float d2 = 0.f;
+        for (int d = lane; d < Dp; d += 32)
+        {
+            const float z = xc[(r0 + r) * Dp + d] - c_s[d];
+            d2 = fmaf(z, z, d2);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+        rmax2 = fmaxf(rmax2, d2);
+    }
+    if (lane == 0)
+        wmax[w] = rmax2;
+    __syncthreads();
+    if (t == 0)
+    {
+        float m = 0.f;
+        for (int q = 0; q < 8; ++q)
+            m = fmaxf(m, wmax[q]);
+        // FP32 rounding of the centre and of the squares: widen by a relative 1e-5
+        rad[blockIdx.x] = nvalid > 0 ? sqrtf(m) * 1.00001f + 1e-6f : -1.f;
+    }
+}
+
+// near_bits[b][t] = 1 when candidate tile t may hold one of query block b's
+// screened neighbours: the gap between their spheres, squared, is below tau_b =
+// 4 (2 r_b)^2 + 2 eps_far(b), where (2 r_b)^2 bounds the block's own spread and
+// eps_far(b) the error of a high-part-only product for its queries. Any value of
+// tau is safe (far tiles are certified separately); it only decides how many
+// tiles get the full fp16 split.
+__global__ void k_classify(const float* __restrict__ qc, const float* __restrict__ qr, const float* __restrict__ tc,
+                           const float* __restrict__ tr, int nq, int nt, int nwords, int Dp, const float* rmax,
+                           float c1, float c2f, uint32_t* near_bits)
+{
+    const int64_t total = (int64_t)nq * nwords;
+    const float R = rmax[0];
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int b = (int)(e / nwords), wd = (int)(e % nwords);
+        const float rb = qr[b];
+        float cn2 = 0.f;
+        for (int d = 0; d < Dp; ++d)
+            cn2 = fmaf(qc[(int64_t)b * Dp + d], qc[(int64_t)b * Dp + d], cn2);
+        const float xm = sqrtf(cn2) + fmaxf(rb, 0.f);  // bound of |x| over the block
+        const float eps_far = c1 * (xm * xm + R * R) + c2f * xm * R;
+        const float tau = 16.f * rb * rb + 2.f * eps_far;
+        uint32_t word = 0u;
+        for (int j = 0; j < 32; ++j)
+        {
+            const int t = wd * 32 + j;
+            if (t >= nt || rb < 0.f || tr[t] < 0.f)
+                continue;
+            float d2 = 0.f;
+            for (int d = 0; d < Dp; ++d)
+            {
+                const float z = qc[(int64_t)b * Dp + d] - tc[(int64_t)t * Dp + d];
+                d2 = fmaf(z, z, d2);
+            }
+            const float gap = fmaxf(0.f, sqrtf(d2) - rb - tr[t]);
+            if (gap * gap < tau)
+                word |= 1u << j;
+        }
+        near_bits[e] = word;
     }
 }
 
@@ -985,8 +1121,27 @@ void launch(tk_ctx* ctx, const uint16_t* xh, const uint16_t* xl, const uint16_t*
     TK_CHECK_LAUNCH();
 }
 
-void launch_wide(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
+void launch_wide(tk_ctx* ctx, Prepared& P, int32_t* cand_idx, float* cand_val)
 {
+    cudaStream_t st = ctx->stream;
+    const int nq = (int)(P.Npad / TC_M), nt = (int)(P.Npad / TW_N);
+    const int nwords = (nt + 31) / 32;
+    float* qc = (float*)ctx->scratch.get("tw.qc", sizeof(float) * (size_t)nq * P.Dp);
+    float* qr = (float*)ctx->scratch.get("tw.qr", sizeof(float) * (size_t)nq);
+    float* tc = (float*)ctx->scratch.get("tw.tc", sizeof(float) * (size_t)nt * P.Dp);
+    float* tr = (float*)ctx->scratch.get("tw.tr", sizeof(float) * (size_t)nt);
+    uint32_t* bits = (uint32_t*)ctx->scratch.get("tw.bits", sizeof(uint32_t) * (size_t)nq * nwords);
+    P.far_val = (float*)ctx->scratch.get("tw.far", sizeof(float) * (size_t)P.Npad);
+    float c1, c2, c2f;
+    screen_error_model(TK_SCREEN_TENSOR, P.Dp, &c1, &c2);
+    screen_error_model_far(P.Dp, &c2f);
+    P.c2_far = c2f;
+    k_spheres<TC_M><<<nq, 256, 0, st>>>(P.xc, P.N, P.Dp, qc, qr);
+    TK_CHECK_LAUNCH();
+    k_spheres<TW_N><<<nt, 256, 0, st>>>(P.xc, P.N, P.Dp, tc, tr);
+    TK_CHECK_LAUNCH();
+    k_classify<<<2 * ctx->num_sms, 256, 0, st>>>(qc, qr, tc, tr, nq, nt, nwords, P.Dp, P.rmax, c1, c2f, bits);
+    TK_CHECK_LAUNCH();
     CUtensorMap ah, al, bh, bl, bn;
     make_map(&ah, P.xh, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, 128);
     make_map(&al, P.xl, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, 128);
@@ -994,9 +1149,8 @@ void launch_wide(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_
     make_map(&bl, P.xl, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, TW_N);
     make_map(&bn, P.xn, P.Npad, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B, TW_N);
     TK_CUDA(cudaFuncSetAttribute(k_screen_tc_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TwCfg::SMEM));
-    const int grid = (int)(P.Npad / TC_M);
-    k_screen_tc_wide<<<grid, TC_THREADS, TwCfg::SMEM, ctx->stream>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad,
-                                                                     cand_idx, cand_val, P.nrm, ctx->dev_err);
+    k_screen_tc_wide<<<nq, TC_THREADS, TwCfg::SMEM, st>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad, bits, nwords,
+                                                          cand_idx, cand_val, P.far_val, P.nrm, ctx->dev_err);
     TK_CHECK_LAUNCH();
 }
 
@@ -1012,7 +1166,7 @@ void launch_single(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* can
 
 bool tensor_screen_supported(int Dp) { return Dp == 64 || Dp == 128; }
 
-void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
+void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
 {
     if (!P.xh || !P.xl || !P.xn)
         throw Error(TK_ERR_INTERNAL, "tensor screen needs the fp16 split layout");

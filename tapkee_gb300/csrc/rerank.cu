@@ -344,6 +344,19 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                 const double eps = (double)c1 * (nx + R * R) + (double)c2 * sqrt(nx) * R;
                 certified = ek < (double)T - eps;
             }
+            if (RS.far_val)
+            {
+                // candidates in tiles screened with high parts only: all have
+                // screened values >= far_val, with the larger far error bound
+                const float A = RS.far_val[p];
+                if (A < FLT_MAX)
+                {
+                    const double R = (double)V.R;
+                    const double nx = (double)nrm[p];
+                    const double eps_far = (double)c1 * (nx + R * R) + (double)RS.c2_far * sqrt(nx) * R;
+                    certified = certified && ek < (double)A - eps_far;
+                }
+            }
         }
         certified = __shfl_sync(0xffffffffu, certified, 0);
         if (certified)
@@ -445,6 +458,18 @@ __global__ void __launch_bounds__(256) k_fallback(const RowSpace RS, const int32
 
 } // namespace
 
+void screen_error_model_far(int Dp, float* c2)
+{
+    const double u = 5.9604644775390625e-08;  // 2^-24
+    // x.y ~ h_x.h_y: the dropped h_x.l_y + l_x.h_y + l_x.l_y is at most
+    // (2 2^-11 + 2^-22) |x||y| (|l| <= 2^-11 |x| elementwise, Cauchy-Schwarz),
+    // plus FP32 accumulation of Dp / 16 + 1 K-steps (2 ulp each) and the
+    // intra-instruction sum (8 ulp); doubled for the 2 x.y term and again for safety
+    const double split = 2.0 * 4.8828125e-04 + 2.384185791015625e-07;
+    const double accum = (Dp / 16.0 * 2.0 + 10.0) * 2.0 * u;
+    *c2 = (float)(2.0 * (split + accum) * 2.0);
+}
+
 void screen_error_model(int screen, int Dp, float* c1, float* c2)
 {
     const double u = 5.9604644775390625e-08;  // 2^-24
@@ -522,6 +547,8 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
     S.R = P.rmax;
     S.idx_out = idx_out;
     S.d2_out = d2_out;
+    S.far_val = P.far_val;
+    S.c2_far = P.c2_far;
     launch_rerank<false>(ctx, S, N, kc, cand_idx, cand_val, P.nrm, eps_c1, eps_c2, failed, failed_ub, nfailed);
     TK_CUDA(cudaMemcpyAsync(ctx->host_i64, nfailed, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     TK_CUDA(cudaStreamSynchronize(st));

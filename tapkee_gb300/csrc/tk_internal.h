@@ -80,6 +80,11 @@ struct Prepared
     int32_t* perm = nullptr;    // sorted position -> original index
     float* rmax = nullptr;      // device scalars: [0] R = max |xc|, [1] fp16 scale exponent s
     float scale_log2 = 0.f;     // xh/xl hold xc * 2^scale_log2
+    // set by the wide tensor screen: per sorted row, the smallest screened value
+    // over the candidate tiles screened with high parts only (FLT_MAX: none),
+    // and the relative error constant of those values
+    float* far_val = nullptr;
+    float c2_far = 0.f;
 };
 
 } // namespace tk
@@ -117,7 +122,7 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
 // knn_simt.cu / knn_tc.cu: screening, K candidates per row (sorted-space indices).
 constexpr int KCAND_MAX = 64;
 void screen_fp32(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
-void screen_tensor(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
+void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
 
 // ---- batches of independent problems -----------------------------------------
 
@@ -173,6 +178,8 @@ struct RowSpace
     const BatchProb* probs = nullptr;
     const float* prob_R = nullptr;
     int32_t* idx_all = nullptr;
+    const float* far_val = nullptr;  // per row: smallest far-tile screened value (wide screen)
+    float c2_far = 0.f;
 };
 // Re-rank + certification + exact fallback of a batch group; the fallback reads
 // its row count on the device (no host synchronisation).
@@ -223,5 +230,8 @@ void assemble_numeric(tk_ctx* ctx, int method, int64_t N, int k, int td, const i
 
 // Screening error model (see rerank.cu): |approx - exact| <= c1 (|x|^2 + R^2) + c2 |x| R.
 void screen_error_model(int screen, int Dp, float* c1, float* c2);
+// Relative error constant c2 of screened values formed from the fp16 high parts
+// only (x.y ~ h_x.h_y): |a - d^2| <= c1 (|x|^2 + R^2) + c2 |x| R.
+void screen_error_model_far(int Dp, float* c2);
 
 } // namespace tk
