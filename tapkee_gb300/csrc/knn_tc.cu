@@ -641,13 +641,14 @@ struct TwCfg
     static constexpr int B_STAGE = 2 * B_ATOM + BX_BYTES;    // 72 KB
     static constexpr int STAGES = 2;
     static constexpr int MERGE_BYTES = 4 * TW_KC * 32 * 8;   // warps 4-7 lists: value + id
-    static constexpr int STASH = 8;
+    static constexpr int NB_WORDS = 2048;                    // near bits staged in shared memory
     static constexpr size_t OFF_B = A_BYTES;
     static constexpr size_t OFF_AX = OFF_B + (size_t)STAGES * B_STAGE;
     static constexpr size_t OFF_BAR = OFF_AX + AX_BYTES;
     static constexpr size_t OFF_MERGE = OFF_BAR + 256;
-    static constexpr size_t OFF_STASH = OFF_MERGE + MERGE_BYTES;
-    static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 128 * 4 + 1024;
+    static constexpr size_t OFF_FAR = OFF_MERGE + MERGE_BYTES;
+    static constexpr size_t OFF_NB = OFF_FAR + 128 * 4;
+    static constexpr size_t SMEM = OFF_NB + (size_t)NB_WORDS * 4 + 1024;
     static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
@@ -664,6 +665,13 @@ __device__ __forceinline__ void umma_f16_w(uint32_t dtmem, uint64_t adesc, uint6
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
             dtmem),
         "l"(adesc), "l"(bdesc), "r"(IDESC_W), "r"(accumulate));
+}
+
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -686,15 +694,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     TwBarriers& Bar = *reinterpret_cast<TwBarriers*>(gbase + C::OFF_BAR);
     float* merge_v = reinterpret_cast<float*>(gbase + C::OFF_MERGE);
     int32_t* merge_i = reinterpret_cast<int32_t*>(gbase + C::OFF_MERGE + C::MERGE_BYTES / 2);
-    float* stash_all = reinterpret_cast<float*>(gbase + C::OFF_STASH);
+    float* merge_far = reinterpret_cast<float*>(gbase + C::OFF_FAR);
     volatile int* abort = &Bar.abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ntiles = (int)(Npad / TW_N);
     const int64_t q0 = (int64_t)blockIdx.x * TC_M;
-    // near (full fp16 split) or far (high parts only) pair of this query block and a tile
+    // near (full fp16 split) or far (high parts only) pair of this query block and
+    // a tile; the block's bits are staged in shared memory when they fit
     const uint32_t* nb_row = near_bits + (int64_t)blockIdx.x * nwords;
-    auto is_near = [&](int tile) { return ((__ldg(nb_row + (tile >> 5)) >> (tile & 31)) & 1u) != 0u; };
+    uint32_t* nb_s = reinterpret_cast<uint32_t*>(gbase + C::OFF_NB);
+    const bool nb_staged = nwords <= C::NB_WORDS;
+    if (nb_staged)
+        for (int t = threadIdx.x; t < nwords; t += blockDim.x)
+            nb_s[t] = __ldg(nb_row + t);
+    const uint32_t* nb = nb_staged ? nb_s : nb_row;
+    auto is_near = [&](int tile) { return ((nb[tile >> 5] >> (tile & 31)) & 1u) != 0u; };
 
     if (threadIdx.x == 0)
     {
@@ -830,9 +845,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int half = warp >> 2;
         const int row = quad * 32 + lane;
         const int64_t q = q0 + row;
-        const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);
+        const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);  // a power of two: thr below is exact
         const float inv_m2 = 1.0f / m2;
-        float* stash = stash_all + (warp * 32 + lane) * (C::STASH + 1);
         float L[KC];
         int32_t Ix[KC];
 #pragma unroll
@@ -876,51 +890,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     if (lane == 0)
                         mbar_arrive(smem_u32(&Bar.tempty[buf]));
                 }
+                // largest value of each group of 8 columns and of all 64: one
+                // branch per 64 columns in the common case (nothing passes)
+                float gm[8];
 #pragma unroll
-                for (int s32 = 0; s32 < 2; ++s32)
+                for (int g = 0; g < 8; ++g)
                 {
-                    float gm[4];
-#pragma unroll
-                    for (int g = 0; g < 4; ++g)
+                    const float* w = v + g * 8;
+                    gm[g] = fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7]));
+                }
+                const float g64 =
+                    fmax3(fmax3(gm[0], gm[1], gm[2]), fmax3(gm[3], gm[4], gm[5]), fmaxf(gm[6], gm[7]));
+                if (far_tile)
+                {
+                    if (!ragged)
+                        far_max = fmaxf(far_max, g64);
+                    else
                     {
-                        const float* w = v + s32 * 32 + g * 8;
-                        gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
-                                      fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
+#pragma unroll
+                        for (int e = 0; e < 64; ++e)
+                            if (c0 + h * 64 + e < N)
+                                far_max = fmaxf(far_max, v[e]);
                     }
-                    const float g32 = fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3]));
-                    if (far_tile)
+                }
+                if (g64 > thr)
+                {
+#pragma unroll
+                    for (int g = 0; g < 8; ++g)
                     {
-                        if (!ragged)
-                            far_max = fmaxf(far_max, g32);
-                        else
+                        if (gm[g] > thr)
                         {
+                            // columns of the group that pass, then one insertion each
+                            const float* w = v + g * 8;
+                            unsigned msk = 0u;
 #pragma unroll
-                            for (int e = 0; e < 32; ++e)
-                                if (c0 + h * 64 + s32 * 32 + e < N)
-                                    far_max = fmaxf(far_max, v[s32 * 32 + e]);
-                        }
-                    }
-                    if (g32 > thr)
-                    {
-#pragma unroll
-                        for (int g = 0; g < 4; ++g)
-                        {
-                            if (gm[g] > thr)
-                            {
-#pragma unroll
-                                for (int e = 0; e < 8; ++e)
-                                    stash[e] = v[s32 * 32 + g * 8 + e];
-                                const int64_t cb = c0 + h * 64 + s32 * 32 + g * 8;
+                            for (int e = 0; e < 8; ++e)
+                                msk |= (w[e] > thr) ? (1u << e) : 0u;
+                            const int64_t cb = c0 + h * 64 + g * 8;
 #pragma unroll 1
-                                for (int e = 0; e < 8; ++e)
+                            while (msk)
+                            {
+                                const int e = __ffs(msk) - 1;
+                                msk &= msk - 1u;
+                                float x = w[0];
+#pragma unroll
+                                for (int e2 = 1; e2 < 8; ++e2)
+                                    x = (e == e2) ? w[e2] : x;
+                                const float t = m2 * x;
+                                if (t < cmp && cb + e < N)
                                 {
-                                    const float t = m2 * stash[e];
-                                    if (t < cmp && cb + e < N)
-                                    {
-                                        reg_insert<KC>(L, Ix, t, (int32_t)(cb + e));
-                                        cmp = L[KC - 1];
-                                        thr = cmp * inv_m2;
-                                    }
+                                    reg_insert<KC>(L, Ix, t, (int32_t)(cb + e));
+                                    cmp = L[KC - 1];
+                                    thr = cmp * inv_m2;
                                 }
                             }
                         }
@@ -929,7 +950,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
         // merge the two half lists of each row (named barrier of the 8 epilogue warps)
-        float* merge_far = stash_all + 8 * 32 * (C::STASH + 1);  // 128 floats after the stashes
         if (half == 1)
         {
 #pragma unroll
@@ -1032,15 +1052,19 @@ __global__ void __launch_bounds__(256) k_spheres(const float* __restrict__ xc, i
     }
 }
 
-// near_bits[b][t] = 1 when candidate tile t may hold one of query block b's
-// screened neighbours: the gap between their spheres, squared, is below tau_b =
-// 4 (2 r_b)^2 + 2 eps_far(b), where (2 r_b)^2 bounds the block's own spread and
-// eps_far(b) the error of a high-part-only product for its queries. Any value of
-// tau is safe (far tiles are certified separately); it only decides how many
-// tiles get the full fp16 split.
+// near_bits[b][t] = 1 when candidate tile t may hold one of the k nearest
+// neighbours of a query of block b. A query x of a block with at least 40 valid
+// rows has 39 other rows within 2 r_b, so its k-th neighbour distance e_k is at
+// most (2 r_b)^2 for every k of the 32-entry lists. Every point of a far tile
+// lies at least the sphere gap g away, and its screened value is at least
+// g^2 - eps_far(b); the re-rank certifies x when e_k < far_val - eps_far, which
+// g^2 >= (2 r_b)^2 + 2 eps_far(b) guarantees (eps_far(b) uses the largest |x| of
+// the block, so it covers every row's own bound). tau_b carries 1 % for the FP32
+// rounding of the gap. Any value of tau is safe: a row that fails certification
+// is rescanned exactly; tau only decides how many tiles get the full fp16 split.
 __global__ void k_classify(const float* __restrict__ qc, const float* __restrict__ qr, const float* __restrict__ tc,
-                           const float* __restrict__ tr, int nq, int nt, int nwords, int Dp, const float* rmax,
-                           float c1, float c2f, uint32_t* near_bits)
+                           const float* __restrict__ tr, int nq, int nt, int nwords, int Dp, int64_t N,
+                           const float* rmax, float c1, float c2f, uint32_t* near_bits)
 {
     const int64_t total = (int64_t)nq * nwords;
     const float R = rmax[0];
@@ -1053,7 +1077,8 @@ __global__ void k_classify(const float* __restrict__ qc, const float* __restrict
             cn2 = fmaf(qc[(int64_t)b * Dp + d], qc[(int64_t)b * Dp + d], cn2);
         const float xm = sqrtf(cn2) + fmaxf(rb, 0.f);  // bound of |x| over the block
         const float eps_far = c1 * (xm * xm + R * R) + c2f * xm * R;
-        const float tau = 16.f * rb * rb + 2.f * eps_far;
+        const int64_t nvalid = N - (int64_t)b * 128;  // rows of the block (at most 128)
+        const float tau = nvalid >= 40 ? 1.01f * (4.f * rb * rb + 2.f * eps_far) : __int_as_float(0x7f800000);
         uint32_t word = 0u;
         for (int j = 0; j < 32; ++j)
         {
@@ -1140,7 +1165,7 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int32_t* cand_idx, float* cand_val)
     TK_CHECK_LAUNCH();
     k_spheres<TW_N><<<nt, 256, 0, st>>>(P.xc, P.N, P.Dp, tc, tr);
     TK_CHECK_LAUNCH();
-    k_classify<<<2 * ctx->num_sms, 256, 0, st>>>(qc, qr, tc, tr, nq, nt, nwords, P.Dp, P.rmax, c1, c2f, bits);
+    k_classify<<<2 * ctx->num_sms, 256, 0, st>>>(qc, qr, tc, tr, nq, nt, nwords, P.Dp, P.N, P.rmax, c1, c2f, bits);
     TK_CHECK_LAUNCH();
     CUtensorMap ah, al, bh, bl, bn;
     make_map(&ah, P.xh, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, 128);
