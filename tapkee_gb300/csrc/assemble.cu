@@ -13,10 +13,15 @@
 //     Contributions of one source to one row have distinct columns, so one
 //     source is one lane-parallel batch and every (row, col) sum is formed in
 //     the reference's serial triplet order;
-//   * the table is compacted, sorted by column (bitonic) and written.
-// Two passes: count (keys only) -> exclusive scan -> fill. A row whose distinct
-// columns overflow the 256-slot table is redone by a one-warp kernel with an
-// 8192-slot table.
+//   * the table is compacted, sorted by column (bitonic, in registers) and
+//     written to a per-row scratch of RCAP entries together with its count.
+// One pass over the rows (k_rows_fused), then an exclusive scan of the counts
+// and a copy of every row into the CSR (k_compact). The contributions of a
+// round of sources are loaded into shared memory together before they are
+// added, so a row waits for one round of gathers rather than one per source. A
+// row whose distinct columns overflow the 256-slot table or the scratch is
+// redone by a one-warp kernel with an 8192-slot table, in a count and a fill
+// pass.
 //
 //   LLE  row j: source j  -> (j, 1+shift), (n_a, -w_ja)
 //               source r  -> (r, -w_ra), (n_b, w_ra w_rb)       [j = n_a of r]
@@ -33,6 +38,8 @@ namespace {
 constexpr int HC = 256;         // hash slots per warp (normal rows)
 constexpr int HC_BIG = 8192;    // hash slots for rows that overflow HC
 constexpr int ROW_WARPS = 8;
+constexpr int RCAP = 128;       // entries per row in the row scratch
+constexpr int STAGE = 256;      // staged (column, value) contributions per warp
 
 __global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, int* cnt, unsigned* err)
 {
@@ -192,8 +199,8 @@ struct RowTable
 };
 
 // insert-or-add; returns false if the table is full
-template <int CAP, bool VALUES>
-__device__ __forceinline__ bool table_add(RowTable<CAP>& T, int col, double v)
+template <int CAP, bool VALUES, class Table>
+__device__ __forceinline__ bool table_add(Table& T, int col, double v)
 {
     unsigned h = hash_col(col) & (CAP - 1);
     for (int probe = 0; probe < CAP; ++probe)
@@ -214,6 +221,26 @@ __device__ __forceinline__ bool table_add(RowTable<CAP>& T, int col, double v)
         h = (h + 1) & (CAP - 1);
     }
     return false;
+}
+
+// One lane-parallel batch of adds, called by the whole warp (valid marks the
+// lanes with a contribution). Lanes whose columns coincide -- possible only for
+// a caller's idx that lists a point as its own neighbour or twice -- add in
+// lane order, one per step, so no update is lost and the sum is reproducible.
+template <int CAP, bool VALUES, class Table>
+__device__ __forceinline__ bool warp_add(Table& T, int lane, bool valid, int col, double v)
+{
+    const unsigned grp = __match_any_sync(0xffffffffu, valid ? col : -2 - lane);
+    const int rank = __popc(grp & ((1u << lane) - 1u));
+    const int last = (int)__reduce_max_sync(0xffffffffu, valid ? (unsigned)rank : 0u);
+    bool ok = true;
+    for (int r = 0; r <= last; ++r)
+    {
+        if (valid && rank == r)
+            ok = table_add<CAP, VALUES>(T, col, v);
+        __syncwarp();
+    }
+    return ok;
 }
 
 // Upper bound of the number of distinct columns in row j.
@@ -272,13 +299,10 @@ __device__ bool process_row(RowTable<CAP>& T, int lane, int method, int64_t j, i
                 for (int t0 = 0; t0 < k + 1; t0 += 32)
                 {
                     const int t = t0 + lane;
-                    if (t < k + 1)
-                    {
-                        const int col = (t == 0) ? (int)j : idx[j * k + t - 1];
-                        const double v = VALUES ? ((t == 0) ? 1.0 + shift : -wts[j * k + t - 1]) : 0.0;
-                        ok &= table_add<CAP, VALUES>(T, col, v);
-                    }
-                    __syncwarp();
+                    const bool valid = t < k + 1;
+                    const int col = !valid ? 0 : (t == 0) ? (int)j : idx[j * k + t - 1];
+                    const double v = (VALUES && valid) ? ((t == 0) ? 1.0 + shift : -wts[j * k + t - 1]) : 0.0;
+                    ok &= warp_add<CAP, VALUES>(T, lane, valid, col, v);
                 }
             }
             else
@@ -288,13 +312,10 @@ __device__ bool process_row(RowTable<CAP>& T, int lane, int method, int64_t j, i
                 for (int t0 = 0; t0 < k + 1; t0 += 32)
                 {
                     const int t = t0 + lane;
-                    if (t < k + 1)
-                    {
-                        const int col = (t == 0) ? (int)src : idx[src * k + t - 1];
-                        const double v = VALUES ? ((t == 0) ? -wa : wa * wts[src * k + t - 1]) : 0.0;
-                        ok &= table_add<CAP, VALUES>(T, col, v);
-                    }
-                    __syncwarp();
+                    const bool valid = t < k + 1;
+                    const int col = !valid ? 0 : (t == 0) ? (int)src : idx[src * k + t - 1];
+                    const double v = (VALUES && valid) ? ((t == 0) ? -wa : wa * wts[src * k + t - 1]) : 0.0;
+                    ok &= warp_add<CAP, VALUES>(T, lane, valid, col, v);
                 }
             }
         }
@@ -315,20 +336,17 @@ __device__ bool process_row(RowTable<CAP>& T, int lane, int method, int64_t j, i
                 for (int t0 = 0; t0 < k; t0 += 32)
                 {
                     const int t = t0 + lane;
-                    if (t < k)
+                    const bool valid = t < k;
+                    double v = 0.0;
+                    if (VALUES && valid)
                     {
-                        double v = 0.0;
-                        if (VALUES)
-                        {
-                            const double* Vb = wts + (src * k + t) * (int64_t)td;
-                            double pab = 1.0 / k;
-                            for (int q = 0; q < td; ++q)
-                                pab += Va[q] * Vb[q];
-                            v = -pab;
-                        }
-                        ok &= table_add<CAP, VALUES>(T, idx[src * k + t], v);
+                        const double* Vb = wts + (src * k + t) * (int64_t)td;
+                        double pab = 1.0 / k;
+                        for (int q = 0; q < td; ++q)
+                            pab += Va[q] * Vb[q];
+                        v = -pab;
                     }
-                    __syncwarp();
+                    ok &= warp_add<CAP, VALUES>(T, lane, valid, valid ? idx[src * k + t] : 0, v);
                 }
             }
         }
@@ -398,56 +416,285 @@ __device__ void table_emit(RowTable<CAP>& T, int lane, int64_t base, int32_t* co
     __syncwarp();
 }
 
-template <bool VALUES>
-__global__ void __launch_bounds__(ROW_WARPS * 32)
-    k_rows(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx, const double* __restrict__ wts,
-           double shift, const int64_t* __restrict__ rptr, const int32_t* __restrict__ rev, int* row_nnz,
-           const int64_t* __restrict__ row_ptr, int32_t* col_idx, double* vals, int32_t* big_rows,
-           unsigned* nbig, unsigned char* row_big, unsigned* err)
+// ---------------------------------------------------------------------------
+// Fused row pass: one warp per row, contributions staged per round of sources.
+
+struct FusedSmem
+{
+    int keys[HC];
+    double vals[HC];
+    int scol[STAGE];
+    double sval[STAGE];  // reused for the 64-bit sort keys of the emission
+};
+
+// Bitonic sort of 32 * NK 64-bit keys held NK per lane (element i = e * 32 + lane).
+template <int NK>
+__device__ __forceinline__ void warp_bitonic(unsigned long long (&key)[NK], int lane)
+{
+    constexpr int LOGP = 5 + (NK == 4 ? 2 : (NK == 2 ? 1 : 0));
+#pragma unroll
+    for (int ls = 1; ls <= LOGP; ++ls)
+    {
+        const int size = 1 << ls;
+#pragma unroll
+        for (int lt = ls - 1; lt >= 0; --lt)
+        {
+            const int stride = 1 << lt;
+            if (lt >= 5)
+            {
+                // partner in the same lane: element e pairs with e ^ (stride / 32)
+                const int es = stride >> 5;
+#pragma unroll
+                for (int e = 0; e < NK; ++e)
+                {
+                    if ((e & es) == 0)
+                    {
+                        const bool asc = ((e * 32 + lane) & size) == 0;
+                        const unsigned long long x = key[e], y = key[e + es];
+                        const bool sw = (x > y) == asc;
+                        key[e] = sw ? y : x;
+                        key[e + es] = sw ? x : y;
+                    }
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int e = 0; e < NK; ++e)
+                {
+                    const unsigned long long other = __shfl_xor_sync(0xffffffffu, key[e], stride);
+                    const bool lower = (lane & stride) == 0;
+                    const bool asc = ((e * 32 + lane) & size) == 0;
+                    const bool keep_min = (lower == asc);
+                    const bool less = key[e] < other;
+                    key[e] = (keep_min == less) ? key[e] : other;
+                }
+            }
+        }
+    }
+}
+
+// Sorts the n occupied slots (keys in F.sval, padded) and writes the row.
+template <int NK>
+__device__ __forceinline__ void emit_sorted(FusedSmem& F, int lane, int n, int32_t* out_col, double* out_val)
+{
+    const unsigned long long* sk = reinterpret_cast<const unsigned long long*>(F.sval);
+    unsigned long long key[NK];
+#pragma unroll
+    for (int e = 0; e < NK; ++e)
+    {
+        const int i = e * 32 + lane;
+        key[e] = (i < n) ? sk[i] : ~0ull;
+    }
+    warp_bitonic<NK>(key, lane);
+#pragma unroll
+    for (int e = 0; e < NK; ++e)
+    {
+        const int i = e * 32 + lane;
+        if (i < n)
+        {
+            out_col[i] = (int32_t)(key[e] >> 8);
+            out_val[i] = F.vals[key[e] & 0xffull];
+        }
+    }
+}
+
+// Row j in one pass: table of (column, sum) in the serial triplet order, then
+// sorted into the row scratch (scol_out/sval_out, RCAP entries per row). Rows
+// that do not fit are listed for the large-table kernel.
+__global__ void __launch_bounds__(ROW_WARPS * 32, 4)
+    k_rows_fused(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx,
+                 const double* __restrict__ wts, double shift, const int64_t* __restrict__ rptr,
+                 const int32_t* __restrict__ rev, int* row_nnz, int32_t* scol_out, double* sval_out,
+                 int32_t* big_rows, unsigned* nbig, unsigned char* row_big)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    RowTable<HC>& T = reinterpret_cast<RowTable<HC>*>(smem_raw)[wib];
+    FusedSmem& F = reinterpret_cast<FusedSmem*>(smem_raw)[wib];
+    const int KS = k + 1;          // contributions per source
+    const int S = STAGE / KS;      // sources per round (0 when k >= STAGE: every row takes the large table)
     const int64_t nw = (int64_t)gridDim.x * ROW_WARPS;
+    const bool lle = method == TK_METHOD_KLLE;
+    const double inv_k = 1.0 / k;
     for (int64_t j = (int64_t)blockIdx.x * ROW_WARPS + wib; j < N; j += nw)
     {
-        // rows whose distinct columns do not fit HC go to the large-table kernel:
-        // decided from the bound when it is certain, else by trying
-        if (VALUES)
+        __syncwarp();
+        const int64_t b = rptr[j], e = rptr[j + 1];
+        const int64_t deg = e - b;
+        bool ok = S > 0 && row_bound(method, k, deg) <= (int64_t)HC_BIG;
+        if (ok)
         {
-            if (row_big[j])
-                continue;
-        }
-        else if (row_bound(method, k, rptr[j + 1] - rptr[j]) > (int64_t)HC_BIG)
-        {
-            if (lane == 0)
+            for (int h = lane; h < HC; h += 32)
             {
-                row_big[j] = 1;
-                big_rows[atomicAdd(nbig, 1u)] = (int32_t)j;
+                F.keys[h] = -1;
+                F.vals[h] = 0.0;
             }
-            continue;
+            // position of j itself among its sources: after every r <= j (a
+            // self-loop r == j, possible in a caller's idx, comes first)
+            int pos_j = 0;
+            for (int64_t p0 = b; p0 < e; p0 += 32)
+            {
+                const int64_t p = p0 + lane;
+                const bool lt = p < e && (int64_t)(rev[p] / k) <= j;
+                pos_j += __popc(__ballot_sync(0xffffffffu, lt));
+            }
+            const int total = (int)deg + 1;
+            for (int r0 = 0; r0 < total && ok; r0 += S)
+            {
+                const int ns = min(S, total - r0);
+                __syncwarp();
+                // stage the round's contributions: item it = (source s, entry t)
+                for (int it = lane; it < ns * KS; it += 32)
+                {
+                    const int s = it / KS, t = it - s * KS;
+                    const int p = r0 + s;
+                    int64_t src = j;
+                    int slot = -1;
+                    if (p != pos_j)
+                    {
+                        const int32_t eid = rev[b + (p < pos_j ? p : p - 1)];
+                        src = eid / k;
+                        slot = eid - (int32_t)src * k;
+                    }
+                    int col = -1;
+                    double v = 0.0;
+                    if (lle)
+                    {
+                        if (slot < 0)
+                        {
+                            // source j: (j, 1 + shift), (n_a, -w_ja)
+                            col = (t == 0) ? (int)j : idx[j * k + t - 1];
+                            v = (t == 0) ? 1.0 + shift : -wts[j * k + t - 1];
+                        }
+                        else
+                        {
+                            // source r, j at slot a: (r, -w_ra), (n_b, w_ra w_rb)
+                            const double wa = wts[src * k + slot];
+                            col = (t == 0) ? (int)src : idx[src * k + t - 1];
+                            v = (t == 0) ? -wa : wa * wts[src * k + t - 1];
+                        }
+                    }
+                    else
+                    {
+                        if (slot < 0)
+                        {
+                            // source j: (j, shift)
+                            col = (t == 0) ? (int)j : -1;
+                            v = shift;
+                        }
+                        else if (t == 0)
+                        {
+                            col = (int)j;  // (j, +1), added before the row of P_r
+                            v = 1.0;
+                        }
+                        else
+                        {
+                            // (n_b, -P_r[a][b]), P_r = (1/k) 1 1^T + V_r V_r^T
+                            const double* Va = wts + (src * k + slot) * (int64_t)td;
+                            const double* Vb = wts + (src * k + t - 1) * (int64_t)td;
+                            double pab = inv_k;
+                            for (int q = 0; q < td; ++q)
+                                pab += Va[q] * Vb[q];
+                            col = idx[src * k + t - 1];
+                            v = -pab;
+                        }
+                    }
+                    F.scol[it] = col;
+                    F.sval[it] = v;
+                }
+                __syncwarp();
+                // add in source order; one source's entries have distinct columns,
+                // except LTSA's (j, +1), which goes first on its own
+                for (int s = 0; s < ns; ++s)
+                {
+                    const int base = s * KS;
+                    if (!lle)
+                    {
+                        if (lane == 0 && F.scol[base] >= 0)
+                            ok &= table_add<HC, true>(F, F.scol[base], F.sval[base]);
+                        __syncwarp();
+                        for (int t0 = 1; t0 < KS; t0 += 32)
+                        {
+                            const int t = t0 + lane;
+                            const bool valid = t < KS && F.scol[base + t] >= 0;
+                            ok &= warp_add<HC, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
+                                                     valid ? F.sval[base + t] : 0.0);
+                        }
+                    }
+                    else
+                    {
+                        for (int t0 = 0; t0 < KS; t0 += 32)
+                        {
+                            const int t = t0 + lane;
+                            const bool valid = t < KS;
+                            ok &= warp_add<HC, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
+                                                     valid ? F.sval[base + t] : 0.0);
+                        }
+                    }
+                    __syncwarp();
+                }
+                ok = __all_sync(0xffffffffu, ok);
+            }
         }
-        const bool ok = process_row<HC, VALUES>(T, lane, method, j, k, td, idx, wts, shift, rptr, rev);
+        int n = 0;
+        if (ok)
+        {
+            // compact the occupied slots into 64-bit sort keys (column << 8 | slot)
+            __syncwarp();
+            unsigned long long* sk = reinterpret_cast<unsigned long long*>(F.sval);
+            for (int h0 = 0; h0 < HC; h0 += 32)
+            {
+                const int h = h0 + lane;
+                const bool occ = F.keys[h] != -1;
+                const unsigned m = __ballot_sync(0xffffffffu, occ);
+                if (occ && n + __popc(m & ((1u << lane) - 1u)) < RCAP)
+                    sk[n + __popc(m & ((1u << lane) - 1u))] =
+                        ((unsigned long long)(unsigned)F.keys[h] << 8) | (unsigned)h;
+                n += __popc(m);
+            }
+            __syncwarp();
+            ok = n <= RCAP;
+        }
         if (!ok)
         {
-            if (!VALUES && lane == 0)
+            if (lane == 0)
             {
                 row_big[j] = 1;
+                row_nnz[j] = 0;
                 big_rows[atomicAdd(nbig, 1u)] = (int32_t)j;
             }
-            else if (VALUES && lane == 0)
-                atomicOr(err, DEV_ERR_OVERFLOW);
             continue;
         }
-        if (!VALUES)
-        {
-            const int c = table_count<HC>(T, lane);
-            if (lane == 0)
-                row_nnz[j] = c;
-        }
+        int32_t* oc = scol_out + j * RCAP;
+        double* ov = sval_out + j * RCAP;
+        if (n <= 64)
+            emit_sorted<2>(F, lane, n, oc, ov);
         else
-            table_emit<HC>(T, lane, row_ptr[j], col_idx, vals);
+            emit_sorted<4>(F, lane, n, oc, ov);
+        if (lane == 0)
+            row_nnz[j] = n;
         __syncwarp();
+    }
+}
+
+// Copies every row that the fused pass kept from the row scratch into the CSR.
+__global__ void k_compact(int64_t N, const int* __restrict__ row_nnz, const unsigned char* __restrict__ row_big,
+                          const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ scol,
+                          const double* __restrict__ sval, int32_t* col_idx, double* vals)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < N; j += nw)
+    {
+        if (row_big[j])
+            continue;
+        const int n = row_nnz[j];
+        const int64_t dst = row_ptr[j];
+        for (int i = lane; i < n; i += 32)
+        {
+            col_idx[dst + i] = scol[j * RCAP + i];
+            vals[dst + i] = sval[j * RCAP + i];
+        }
     }
 }
 
@@ -496,6 +743,8 @@ struct AsmState
     int32_t* big;
     unsigned* nbig;
     unsigned char* row_big;
+    int32_t* scol;
+    double* sval;
 };
 
 AsmState asm_state(tk_ctx* ctx, int64_t N, int k)
@@ -508,15 +757,16 @@ AsmState asm_state(tk_ctx* ctx, int64_t N, int k)
     a.big = (int32_t*)ctx->scratch.get("asm.big", sizeof(int32_t) * (size_t)N);
     a.nbig = (unsigned*)ctx->scratch.get("asm.nbig", 16);
     a.row_big = (unsigned char*)ctx->scratch.get("asm.rowbig", (size_t)N);
+    a.scol = (int32_t*)ctx->scratch.get("asm.scol", sizeof(int32_t) * (size_t)N * RCAP);
+    a.sval = (double*)ctx->scratch.get("asm.sval", sizeof(double) * (size_t)N * RCAP);
     return a;
 }
 
 void set_smem_limits()
 {
-    const size_t smem = sizeof(RowTable<HC>) * ROW_WARPS;
+    const size_t smem = sizeof(FusedSmem) * ROW_WARPS;
     const size_t smem_big = sizeof(RowTable<HC_BIG>);
-    TK_CUDA(cudaFuncSetAttribute(k_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    TK_CUDA(cudaFuncSetAttribute(k_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TK_CUDA(cudaFuncSetAttribute(k_rows_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
 }
@@ -528,8 +778,8 @@ int rows_grid(tk_ctx* ctx, int64_t N)
 }
 } // namespace
 
-void assemble_symbolic_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
-                              int64_t* row_ptr)
+void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
+                          const double* weights, double shift, int64_t* row_ptr)
 {
     cudaStream_t st = ctx->stream;
     const int64_t nk = N * (int64_t)k;
@@ -550,9 +800,8 @@ void assemble_symbolic_device(tk_ctx* ctx, int method, int64_t N, int k, int td,
     k_sort_rev<<<g, 256, 0, st>>>(N, a.rptr, a.rev);
     TK_CHECK_LAUNCH();
     set_smem_limits();
-    k_rows<false><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(RowTable<HC>) * ROW_WARPS, st>>>(
-        method, N, k, td, idx, nullptr, 0.0, a.rptr, a.rev, a.row_nnz, nullptr, nullptr, nullptr, a.big, a.nbig,
-        a.row_big, ctx->dev_err);
+    k_rows_fused<<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem) * ROW_WARPS, st>>>(
+        method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig, a.row_big);
     TK_CHECK_LAUNCH();
     k_rows_big<false><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, nullptr, 0.0,
                                                                            a.rptr, a.rev, a.row_nnz, nullptr,
@@ -562,23 +811,24 @@ void assemble_symbolic_device(tk_ctx* ctx, int method, int64_t N, int k, int td,
     scan_to_offsets(ctx, a.row_nnz, N, row_ptr);
 }
 
-int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, int64_t* row_ptr)
+int64_t assemble_rows(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                      double shift, int64_t* row_ptr)
 {
-    assemble_symbolic_device(ctx, method, N, k, td, idx, row_ptr);
+    assemble_rows_device(ctx, method, N, k, td, idx, weights, shift, row_ptr);
     TK_CUDA(cudaMemcpyAsync(ctx->host_i64, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
     TK_CUDA(cudaStreamSynchronize(ctx->stream));
     return ctx->host_i64[0];
 }
 
-void assemble_numeric(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
-                      double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals)
+void assemble_write(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                    double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals)
 {
     cudaStream_t st = ctx->stream;
     AsmState a = asm_state(ctx, N, k);
     set_smem_limits();
-    k_rows<true><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(RowTable<HC>) * ROW_WARPS, st>>>(
-        method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, row_ptr, col_idx, vals, a.big, a.nbig,
-        a.row_big, ctx->dev_err);
+    const int64_t warps = std::min<int64_t>(N, (int64_t)ctx->num_sms * 64);
+    k_compact<<<(int)((warps + 7) / 8), 256, 0, st>>>(N, a.row_nnz, a.row_big, row_ptr, a.scol, a.sval, col_idx,
+                                                       vals);
     TK_CHECK_LAUNCH();
     k_rows_big<true><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, weights, shift,
                                                                           a.rptr, a.rev, a.row_nnz, row_ptr, col_idx,

@@ -644,9 +644,10 @@ void enqueue(tk_batch* B)
         k_b_globalize<<<2 * sms, 256, 0, st>>>(B->probs, B->row_prob_out + K.out_row0, K.out_row0, K.rows, K.k,
                                                B->idx_all + K.idx_off, K.idx_g);
         TK_CHECK_LAUNCH();
-        assemble_symbolic_device(ctx, TK_METHOD_KLLE, K.rows, K.k, 0, K.idx_g, K.row_ptr);
-        assemble_numeric(ctx, TK_METHOD_KLLE, K.rows, K.k, 0, K.idx_g, B->w_all + K.idx_off, B->nullspace_shift,
-                         K.row_ptr, K.col, K.val);
+        assemble_rows_device(ctx, TK_METHOD_KLLE, K.rows, K.k, 0, K.idx_g, B->w_all + K.idx_off,
+                             B->nullspace_shift, K.row_ptr);
+        assemble_write(ctx, TK_METHOD_KLLE, K.rows, K.k, 0, K.idx_g, B->w_all + K.idx_off, B->nullspace_shift,
+                       K.row_ptr, K.col, K.val);
     }
 }
 

@@ -515,7 +515,7 @@ int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t
         int64_t* rp_d = row_ptr ? device_out(ctx, row_ptr, (size_t)N + 1, "io.rowptr", &rh)
                                 : (int64_t*)ctx->scratch.get("io.rowptr", sizeof(int64_t) * ((size_t)N + 1));
         const int64_t cap = *nnz_io;
-        const int64_t nnz = assemble_symbolic(ctx, method, N, k, td, idx_d, rp_d);
+        const int64_t nnz = assemble_rows(ctx, method, N, k, td, idx_d, w_d, shift, rp_d);
         check_device_errors(ctx);
         if (rh)
             copy_back(ctx, row_ptr, rp_d, (size_t)N + 1);
@@ -531,7 +531,7 @@ int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t
         bool ch, vh;
         int32_t* c_d = device_out(ctx, col_idx, (size_t)nnz, "io.col", &ch);
         double* v_d = device_out(ctx, vals, (size_t)nnz, "io.vals", &vh);
-        assemble_numeric(ctx, method, N, k, td, idx_d, w_d, shift, rp_d, c_d, v_d);
+        assemble_write(ctx, method, N, k, td, idx_d, w_d, shift, rp_d, c_d, v_d);
         check_device_errors(ctx);
         if (ch)
             copy_back(ctx, col_idx, c_d, (size_t)nnz);
@@ -630,10 +630,10 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
 
         // M
         int64_t* rp_d = (int64_t*)ctx->scratch.get("op.rowptr", sizeof(int64_t) * ((size_t)N + 1));
-        const int64_t nnz = assemble_symbolic(ctx, p.method, N, k, td, idx_d, rp_d);
+        const int64_t nnz = assemble_rows(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d);
         int32_t* col_d = (int32_t*)ctx->scratch.get("op.col", sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1));
         double* val_d = (double*)ctx->scratch.get("op.vals", sizeof(double) * (size_t)std::max<int64_t>(nnz, 1));
-        assemble_numeric(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, col_d, val_d);
+        assemble_write(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, col_d, val_d);
         TK_CUDA(cudaEventRecord(ctx->ev[6], st));
         check_device_errors(ctx);
 

@@ -215,18 +215,19 @@ void lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, i
 void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
                 int k, int td, double* V);
 
-// assemble.cu: symbolic phase (reverse adjacency, row counts, row_ptr) returns
-// nnz; the numeric phase then fills col_idx/vals (device pointers) using the
-// symbolic state kept in the context's scratch.
+// assemble.cu: the row phase (reverse adjacency, every row's sorted columns and
+// values into a row scratch, row counts, row_ptr) returns nnz; the write phase
+// then copies the rows into col_idx/vals (device pointers) from the state kept
+// in the context's scratch.
 // Exclusive scan of n int counters into n + 1 int64 offsets (deterministic).
 void scan_to_offsets(tk_ctx* ctx, const int* in, int64_t n, int64_t* out);
-// The same without reading nnz back (row_ptr[N] holds it on the device).
-void assemble_symbolic_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
-                              int64_t* row_ptr);
-int64_t assemble_symbolic(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
-                          int64_t* row_ptr);
-void assemble_numeric(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
-                      double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals);
+// The row phase without reading nnz back (row_ptr[N] holds it on the device).
+void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
+                          const double* weights, double shift, int64_t* row_ptr);
+int64_t assemble_rows(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                      double shift, int64_t* row_ptr);
+void assemble_write(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
+                    double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals);
 
 // Screening error model (see rerank.cu): |approx - exact| <= c1 (|x|^2 + R^2) + c2 |x| R.
 void screen_error_model(int screen, int Dp, float* c1, float* c2);

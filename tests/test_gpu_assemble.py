@@ -57,3 +57,42 @@ def test_hub_rows_use_the_large_table(ctx):
     rr, rc, rv = oracle.assemble(0, idx, W, 1e-9)
     assert np.array_equal(rp, rr) and np.array_equal(col, rc)
     assert np.abs(vals - rv).max() <= 1e-12 * np.abs(rv).max()
+
+
+@pytest.mark.parametrize("method,k", [("lle", 12), ("ltsa", 33)])
+def test_assembly_wide_rows_and_long_sources(ctx, method, k):
+    # skewed in-degree (neighbour j drawn with probability ~ 1 / (1 + j)): rows
+    # from a dozen columns to past the 128-entry row scratch and the 256-slot
+    # table; LTSA k=33 sources hold more contributions than a warp has lanes
+    rng = np.random.default_rng(7)
+    N, td = 900, 2
+    p = 1.0 / (1.0 + np.arange(N))
+    p /= p.sum()
+    idx = np.stack([rng.choice(N, size=k, replace=False, p=p) for _ in range(N)]).astype(np.int32)
+    if method == "lle":
+        w = rng.random((N, k))
+        w /= w.sum(1, keepdims=True)
+        m = 0
+    else:
+        w = rng.standard_normal((N, k, td)) / np.sqrt(k)
+        m = 1
+    rp, col, vals = ctx.assemble(method, idx, w, 1e-9)
+    rr, rc, rv = oracle.assemble(m, idx, w, 1e-9)
+    d = np.diff(rr)
+    assert (d <= 128).any() and ((d > 128) & (d <= 256)).any() and (d > 256).any()
+    assert np.array_equal(rp, rr) and np.array_equal(col, rc)
+    assert np.abs(vals - rv).max() <= 1e-12 * np.abs(rv).max()
+
+
+def test_assembly_self_loops(ctx):
+    # a caller's idx may list a point as its own neighbour
+    rng = np.random.default_rng(3)
+    N, k = 500, 6
+    idx = np.stack([rng.choice(N, size=k, replace=False) for _ in range(N)]).astype(np.int32)
+    idx[::7, 0] = np.arange(0, N, 7)
+    w = rng.random((N, k))
+    w /= w.sum(1, keepdims=True)
+    rp, col, vals = ctx.assemble("lle", idx, w, 1e-9)
+    rr, rc, rv = oracle.assemble(0, idx, w, 1e-9)
+    assert np.array_equal(rp, rr) and np.array_equal(col, rc)
+    assert np.abs(vals - rv).max() <= 1e-12 * np.abs(rv).max()
