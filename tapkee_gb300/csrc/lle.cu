@@ -45,6 +45,7 @@ struct LleSmem
     float vh[32], vl[32];
     float r[KP];
     float w[KP];
+    float ivd[KP];  // 1 / L_aa of the register factor
 };
 
 template <int KP>
@@ -126,31 +127,35 @@ __device__ __forceinline__ void reg_cholesky(float (&L)[KP], float& invd, int la
 }
 
 // Solves L L^T x = r with the register factor; lane a holds r_a and gets x_a.
+// Both substitutions are column sweeps: step j broadcasts one solved entry and
+// every later (forward) or earlier (backward) lane updates its own entry. The
+// backward sweep reads L^T from Ls (row a = row a of L, stride KP + 1), and
+// ivd holds 1 / L_jj; both are in shared memory.
 template <int KP>
-__device__ __forceinline__ float reg_chol_solve(const float (&L)[KP], float invd, float r, int lane)
+__device__ __forceinline__ float reg_chol_solve(const float (&L)[KP], const float* Ls, const float* ivd, float r,
+                                                int lane)
 {
     float y = r;
 #pragma unroll
     for (int j = 0; j < KP; ++j)
     {
-        const float yj = __shfl_sync(0xffffffffu, y, j) * __shfl_sync(0xffffffffu, invd, j);
+        const float yj = __shfl_sync(0xffffffffu, y, j) * ivd[j];
         if (lane == j)
             y = yj;
         else if (lane > j)
             y = fmaf(-L[j], yj, y);
     }
-    float x = 0.f;
 #pragma unroll
     for (int j = KP - 1; j >= 0; --j)
     {
-        float s = (lane > j && lane < KP) ? L[j] * x : 0.f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            s += __shfl_xor_sync(0xffffffffu, s, o);
+        const float lji = (lane < j) ? Ls[j * (KP + 1) + lane] : 0.f;
+        const float xj = __shfl_sync(0xffffffffu, y, j) * ivd[j];
         if (lane == j)
-            x = (y - s) * invd;
+            y = xj;
+        else if (lane < j)
+            y = fmaf(-lji, xj, y);
     }
-    return x;
+    return y;
 }
 
 __device__ __forceinline__ float ld_f(const void* X, int dtype, int64_t off)
@@ -175,6 +180,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     LleSmem<KP>& S = reinterpret_cast<LleSmem<KP>*>(smem_raw)[wib];
+    const ff ks = ff{(float)klle_shift, (float)(klle_shift - (double)(float)klle_shift)};
     const int64_t warp = (int64_t)blockIdx.x * WARPS + wib;
     const int64_t nwarps = (int64_t)gridDim.x * WARPS;
 
@@ -366,8 +372,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         }
         __syncwarp();
         float trace = 0.f;
-        for (int a = 0; a < k; ++a)
+        for (int a = lane; a < k; a += 32)
             trace += S.C[a][a];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            trace += __shfl_xor_sync(0xffffffffu, trace, o);
         __syncwarp();
         const float shift = (float)klle_shift * trace;
         for (int a = lane; a < KP; a += 32)
@@ -389,7 +398,18 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
             for (int c = 0; c < KP; ++c)
                 Lr[c] = (lane < KP && c <= lane) ? S.C[lane][c] : 0.f;
             reg_cholesky<KP>(Lr, invd, lane);
-            const float x = reg_chol_solve<KP>(Lr, invd, lane < KP ? S.r[lane] : 0.f, lane);
+            // the factor's rows and reciprocal diagonal, for the backward sweeps
+            __syncwarp();
+            if (lane < KP)
+            {
+#pragma unroll
+                for (int c = 0; c < KP; ++c)
+                    if (c <= lane)
+                        S.C[lane][c] = Lr[c];
+                S.ivd[lane] = invd;
+            }
+            __syncwarp();
+            const float x = reg_chol_solve<KP>(Lr, &S.C[0][0], S.ivd, lane < KP ? S.r[lane] : 0.f, lane);
             __syncwarp();
             if (lane < KP)
                 S.w[lane] = (lane < k) ? x : 0.f;
@@ -484,13 +504,27 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
                     else
                         part[0] = ff_add(part[0], ff_shfl_xor(part[0], o));  // pairs hold the same index
                 }
-                // part[0] of lane l is (C w)_a for a = KR == 32 ? l : (l >> 1)
+                // part[0] of lane l is (C w)_a for a = KR == 32 ? l : (l >> 1);
+                // r_a = rhs_a - (C w)_a - klle_shift trace w_a in float-float
                 const int a_own = (KR == 32) ? lane : (lane >> 1);
-                const double shift_true = klle_shift * (double)trace;
                 if ((KR == 32 || (lane & 1) == 0) && a_own < KP)
-                    S.r[a_own] = (a_own < k) ? (float)((rhs ? rhs[g * k + a_own] : 1.0) - ff_to_double(part[0]) -
-                                                       shift_true * (double)S.w[a_own])
-                                             : 0.f;
+                {
+                    float ra = 0.f;
+                    if (a_own < k)
+                    {
+                        const ff sw = ff_mul(ff_mul(ks, ff{trace, 0.f}), ff{S.w[a_own], 0.f});
+                        ff b = ff{1.f, 0.f};
+                        if (rhs)
+                        {
+                            const double rb = rhs[g * k + a_own];
+                            b.hi = (float)rb;
+                            b.lo = (float)(rb - (double)b.hi);
+                        }
+                        const ff rr = ff_add(ff_add(b, ff_neg(part[0])), ff_neg(sw));
+                        ra = rr.hi + rr.lo;
+                    }
+                    S.r[a_own] = ra;
+                }
                 __syncwarp();
             }
             else
@@ -558,7 +592,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
             }
             if constexpr (KP <= 32)
             {
-                const float x = reg_chol_solve<KP>(Lr, invd, lane < KP ? S.r[lane] : 0.f, lane);
+                const float x = reg_chol_solve<KP>(Lr, &S.C[0][0], S.ivd, lane < KP ? S.r[lane] : 0.f, lane);
                 __syncwarp();
                 if (lane < k)
                     S.w[lane] += x;
