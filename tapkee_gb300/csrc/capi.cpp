@@ -195,7 +195,7 @@ int64_t knn_device(tk_ctx* ctx, const void* Xd, int dtype, int64_t N, int D, int
     float* cand_val = (float*)ctx->scratch.get("knn.cand_val", sizeof(float) * (size_t)P.Npad * kc);
     TK_CUDA(cudaEventRecord(ctx->ev[8], ctx->stream));
     if (tensor)
-        screen_tensor(ctx, P, kc, cand_idx, cand_val);
+        screen_tensor(ctx, P, kc, k, cand_idx, cand_val);
     else
         screen_fp32(ctx, P, kc, cand_idx, cand_val);
     TK_CUDA(cudaEventRecord(ctx->ev[9], ctx->stream));

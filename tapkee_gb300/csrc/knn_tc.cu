@@ -999,7 +999,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // (valid rows only; radius -1 for a block without valid rows). One CTA per block.
 template <int ROWS>
 __global__ void __launch_bounds__(256) k_spheres(const float* __restrict__ xc, int64_t N, int Dp, float* ctr,
-                                                 float* rad)
+                                                 float* rad, float* ctrT)
 {
     __shared__ float part[256];
     __shared__ float c_s[128];
@@ -1022,6 +1022,8 @@ __global__ void __launch_bounds__(256) k_spheres(const float* __restrict__ xc, i
             tot += part[q * Dp + t];
         c_s[t] = nvalid > 0 ? tot / (float)nvalid : 0.f;
         ctr[(int64_t)blockIdx.x * Dp + t] = c_s[t];
+        if (ctrT)
+            ctrT[(int64_t)t * gridDim.x + blockIdx.x] = c_s[t];  // dimension-major copy
     }
     __syncthreads();
     const int lane = t & 31, w = t >> 5;
@@ -1052,50 +1054,135 @@ __global__ void __launch_bounds__(256) k_spheres(const float* __restrict__ xc, i
     }
 }
 
-// near_bits[b][t] = 1 when candidate tile t may hold one of the k nearest
-// neighbours of a query of block b. A query x of a block with at least 40 valid
-// rows has 39 other rows within 2 r_b, so its k-th neighbour distance e_k is at
-// most (2 r_b)^2 for every k of the 32-entry lists. Every point of a far tile
-// lies at least the sphere gap g away, and its screened value is at least
-// g^2 - eps_far(b); the re-rank certifies x when e_k < far_val - eps_far, which
-// g^2 >= (2 r_b)^2 + 2 eps_far(b) guarantees (eps_far(b) uses the largest |x| of
-// the block, so it covers every row's own bound). tau_b carries 1 % for the FP32
-// rounding of the gap. Any value of tau is safe: a row that fails certification
-// is rescanned exactly; tau only decides how many tiles get the full fp16 split.
-__global__ void k_classify(const float* __restrict__ qc, const float* __restrict__ qr, const float* __restrict__ tc,
-                           const float* __restrict__ tr, int nq, int nt, int nwords, int Dp, int64_t N,
-                           const float* rmax, float c1, float c2f, uint32_t* near_bits)
+// Upper bound of the k-th neighbour distance of every query of a 128-row block:
+// the largest, over the block's rows, of the k-th smallest squared distance to
+// the block's other rows (direct FP32 differences), or +inf when the block has
+// at most k valid rows. The block-mates are a subset of all points, so each
+// row's true k-th neighbour distance e_k is at most this. One CTA per block,
+// one thread per row.
+template <int DP>
+__global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ xc, int64_t N, int k, float* Tb)
 {
-    const int64_t total = (int64_t)nq * nwords;
-    const float R = rmax[0];
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    __shared__ __align__(16) float xs[128][DP];
+    __shared__ float wmax[4];
+    const int t = threadIdx.x;
+    const int64_t r0 = (int64_t)blockIdx.x * 128;
+    const int nvalid = (int)max((int64_t)0, min((int64_t)128, N - r0));
+    for (int e = t; e < 128 * DP; e += 128)
     {
-        const int b = (int)(e / nwords), wd = (int)(e % nwords);
-        const float rb = qr[b];
-        float cn2 = 0.f;
-        for (int d = 0; d < Dp; ++d)
-            cn2 = fmaf(qc[(int64_t)b * Dp + d], qc[(int64_t)b * Dp + d], cn2);
-        const float xm = sqrtf(cn2) + fmaxf(rb, 0.f);  // bound of |x| over the block
-        const float eps_far = c1 * (xm * xm + R * R) + c2f * xm * R;
-        const int64_t nvalid = N - (int64_t)b * 128;  // rows of the block (at most 128)
-        const float tau = nvalid >= 40 ? 1.01f * (4.f * rb * rb + 2.f * eps_far) : __int_as_float(0x7f800000);
-        uint32_t word = 0u;
-        for (int j = 0; j < 32; ++j)
+        const int r = e / DP, d = e % DP;
+        xs[r][d] = (r < nvalid) ? xc[(r0 + r) * DP + d] : 0.f;
+    }
+    __syncthreads();
+    float xr[DP];  // this thread's row
+#pragma unroll
+    for (int q = 0; q < DP / 4; ++q)
+    {
+        const float4 v = reinterpret_cast<const float4*>(&xs[t][0])[q];
+        xr[4 * q] = v.x;
+        xr[4 * q + 1] = v.y;
+        xr[4 * q + 2] = v.z;
+        xr[4 * q + 3] = v.w;
+    }
+    float L[32];  // the k smallest distances so far, ascending (k <= 32)
+#pragma unroll
+    for (int s = 0; s < 32; ++s)
+        L[s] = __int_as_float(0x7f800000);
+    for (int c = 0; c < nvalid; ++c)
+    {
+        // every lane reads the same row c: broadcast loads
+        const float4* y4 = reinterpret_cast<const float4*>(&xs[c][0]);
+        float d2a = 0.f, d2b = 0.f;
+#pragma unroll
+        for (int q = 0; q < DP / 4; q += 2)
         {
-            const int t = wd * 32 + j;
-            if (t >= nt || rb < 0.f || tr[t] < 0.f)
-                continue;
+            const float4 ya = y4[q], yb = y4[q + 1];
+            float z;
+            z = xr[4 * q] - ya.x;      d2a = fmaf(z, z, d2a);
+            z = xr[4 * q + 1] - ya.y;  d2a = fmaf(z, z, d2a);
+            z = xr[4 * q + 2] - ya.z;  d2a = fmaf(z, z, d2a);
+            z = xr[4 * q + 3] - ya.w;  d2a = fmaf(z, z, d2a);
+            z = xr[4 * q + 4] - yb.x;  d2b = fmaf(z, z, d2b);
+            z = xr[4 * q + 5] - yb.y;  d2b = fmaf(z, z, d2b);
+            z = xr[4 * q + 6] - yb.z;  d2b = fmaf(z, z, d2b);
+            z = xr[4 * q + 7] - yb.w;  d2b = fmaf(z, z, d2b);
+        }
+        const float d2 = d2a + d2b;
+        if (c != t && t < nvalid && d2 < L[31])
+        {
+#pragma unroll
+            for (int s = 31; s > 0; --s)
+            {
+                const bool sh = d2 < L[s - 1];
+                L[s] = sh ? L[s - 1] : (d2 < L[s] ? d2 : L[s]);
+            }
+            L[0] = fminf(L[0], d2);
+        }
+    }
+    // L is ascending, so its k-th entry is the largest of the first k (a max
+    // rather than an indexed read keeps L in registers)
+    float mine = 0.f;
+#pragma unroll
+    for (int s = 0; s < 32; ++s)
+        mine = fmaxf(mine, (s < k && t < nvalid) ? L[s] : 0.f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        mine = fmaxf(mine, __shfl_xor_sync(0xffffffffu, mine, o));
+    if ((t & 31) == 0)
+        wmax[t >> 5] = mine;
+    __syncthreads();
+    if (t == 0)
+        Tb[blockIdx.x] = fmaxf(fmaxf(wmax[0], wmax[1]), fmaxf(wmax[2], wmax[3]));
+}
+
+// near_bits[b][t] = 1 when candidate tile t may hold one of the k nearest
+// neighbours of a query of block b. Every point of a far tile lies at least
+// the sphere gap g away, and its screened value is at least g^2 - eps_far(b);
+// the re-rank certifies a query x when e_k < far_val - eps_far, which
+// g^2 >= T_b + 2 eps_far(b) guarantees, T_b bounding e_k for the block
+// (k_blockmate) and eps_far(b) using the largest |x| of the block, so that it
+// covers every row's own bound. tau_b carries 1 % for the FP32 rounding of the
+// gap and of T_b. Any value of tau is safe: a row that fails certification is
+// rescanned exactly; tau only decides how many tiles get the full fp16 split.
+// One CTA per query block; thread t takes tiles t, t + 256, ...; the tile
+// centres are read dimension-major (tcT[d * nt + tile]), so a warp's loads of
+// one dimension are contiguous, and a warp ballot forms each 32-tile word.
+__global__ void __launch_bounds__(256) k_classify(const float* __restrict__ qc, const float* __restrict__ qr,
+                                                  const float* __restrict__ tcT, const float* __restrict__ tr,
+                                                  const float* __restrict__ Tb, int nt, int nwords, int Dp,
+                                                  const float* rmax, float c1, float c2f, uint32_t* near_bits)
+{
+    __shared__ float cb[128];
+    const int b = blockIdx.x, t = threadIdx.x, lane = t & 31;
+    if (t < Dp)
+        cb[t] = qc[(int64_t)b * Dp + t];
+    __syncthreads();
+    const float R = rmax[0];
+    const float rb = qr[b];
+    float cn2 = 0.f;
+    for (int d = 0; d < Dp; ++d)
+        cn2 = fmaf(cb[d], cb[d], cn2);
+    const float xm = sqrtf(cn2) + fmaxf(rb, 0.f);  // bound of |x| over the block
+    const float eps_far = c1 * (xm * xm + R * R) + c2f * xm * R;
+    const float tau = 1.01f * (Tb[b] + 2.f * eps_far);  // +inf for a block of at most k rows
+    for (int w0 = 0; w0 < nwords * 32; w0 += 256)
+    {
+        const int tile = w0 + t;
+        bool near = false;
+        if (tile < nt && rb >= 0.f && tr[tile] >= 0.f)
+        {
             float d2 = 0.f;
             for (int d = 0; d < Dp; ++d)
             {
-                const float z = qc[(int64_t)b * Dp + d] - tc[(int64_t)t * Dp + d];
+                const float z = cb[d] - tcT[(int64_t)d * nt + tile];
                 d2 = fmaf(z, z, d2);
             }
-            const float gap = fmaxf(0.f, sqrtf(d2) - rb - tr[t]);
-            if (gap * gap < tau)
-                word |= 1u << j;
+            const float gap = fmaxf(0.f, sqrtf(d2) - rb - tr[tile]);
+            near = gap * gap < tau;
         }
-        near_bits[e] = word;
+        const unsigned word = __ballot_sync(0xffffffffu, near);
+        if (lane == 0 && (tile >> 5) < nwords)
+            near_bits[(int64_t)b * nwords + (tile >> 5)] = word;
     }
 }
 
@@ -1146,7 +1233,7 @@ void launch(tk_ctx* ctx, const uint16_t* xh, const uint16_t* xl, const uint16_t*
     TK_CHECK_LAUNCH();
 }
 
-void launch_wide(tk_ctx* ctx, Prepared& P, int32_t* cand_idx, float* cand_val)
+void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand_val)
 {
     cudaStream_t st = ctx->stream;
     const int nq = (int)(P.Npad / TC_M), nt = (int)(P.Npad / TW_N);
@@ -1154,18 +1241,22 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int32_t* cand_idx, float* cand_val)
     float* qc = (float*)ctx->scratch.get("tw.qc", sizeof(float) * (size_t)nq * P.Dp);
     float* qr = (float*)ctx->scratch.get("tw.qr", sizeof(float) * (size_t)nq);
     float* tc = (float*)ctx->scratch.get("tw.tc", sizeof(float) * (size_t)nt * P.Dp);
+    float* tcT = (float*)ctx->scratch.get("tw.tcT", sizeof(float) * (size_t)nt * P.Dp);
     float* tr = (float*)ctx->scratch.get("tw.tr", sizeof(float) * (size_t)nt);
     uint32_t* bits = (uint32_t*)ctx->scratch.get("tw.bits", sizeof(uint32_t) * (size_t)nq * nwords);
+    float* Tb = (float*)ctx->scratch.get("tw.tb", sizeof(float) * (size_t)nq);
     P.far_val = (float*)ctx->scratch.get("tw.far", sizeof(float) * (size_t)P.Npad);
     float c1, c2, c2f;
     screen_error_model(TK_SCREEN_TENSOR, P.Dp, &c1, &c2);
     screen_error_model_far(P.Dp, &c2f);
     P.c2_far = c2f;
-    k_spheres<TC_M><<<nq, 256, 0, st>>>(P.xc, P.N, P.Dp, qc, qr);
+    k_spheres<TC_M><<<nq, 256, 0, st>>>(P.xc, P.N, P.Dp, qc, qr, nullptr);
     TK_CHECK_LAUNCH();
-    k_spheres<TW_N><<<nt, 256, 0, st>>>(P.xc, P.N, P.Dp, tc, tr);
+    k_spheres<TW_N><<<nt, 256, 0, st>>>(P.xc, P.N, P.Dp, tc, tr, tcT);
     TK_CHECK_LAUNCH();
-    k_classify<<<2 * ctx->num_sms, 256, 0, st>>>(qc, qr, tc, tr, nq, nt, nwords, P.Dp, P.N, P.rmax, c1, c2f, bits);
+    k_blockmate<64><<<nq, 128, 0, st>>>(P.xc, P.N, k, Tb);
+    TK_CHECK_LAUNCH();
+    k_classify<<<nq, 256, 0, st>>>(qc, qr, tcT, tr, Tb, nt, nwords, P.Dp, P.rmax, c1, c2f, bits);
     TK_CHECK_LAUNCH();
     CUtensorMap ah, al, bh, bl, bn;
     make_map(&ah, P.xh, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, 128);
@@ -1191,14 +1282,14 @@ void launch_single(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* can
 
 bool tensor_screen_supported(int Dp) { return Dp == 64 || Dp == 128; }
 
-void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
+void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int k, int32_t* cand_idx, float* cand_val)
 {
     if (!P.xh || !P.xl || !P.xn)
         throw Error(TK_ERR_INTERNAL, "tensor screen needs the fp16 split layout");
     if (P.Dp == 64)
     {
         if (kc == 32)
-            launch_wide(ctx, P, cand_idx, cand_val);
+            launch_wide(ctx, P, k, cand_idx, cand_val);
         else
             launch_single<64, 64>(ctx, P, cand_idx, cand_val);
     }

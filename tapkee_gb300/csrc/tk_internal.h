@@ -122,7 +122,7 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
 // knn_simt.cu / knn_tc.cu: screening, K candidates per row (sorted-space indices).
 constexpr int KCAND_MAX = 64;
 void screen_fp32(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
-void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int32_t* cand_idx, float* cand_val);
+void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int k, int32_t* cand_idx, float* cand_val);
 
 // ---- batches of independent problems -----------------------------------------
 
