@@ -14,7 +14,7 @@
 //     source is one lane-parallel batch and every (row, col) sum is formed in
 //     the reference's serial triplet order;
 //   * the table is compacted, sorted by column (bitonic, in registers) and
-//     written to a per-row scratch of RCAP entries together with its count.
+//     written to a per-row scratch (128 or 256 entries) together with its count.
 // One pass over the rows (k_rows_fused), then an exclusive scan of the counts
 // and a copy of every row into the CSR (k_compact). The contributions of a
 // round of sources are loaded into shared memory together before they are
@@ -35,11 +35,14 @@
 namespace tk {
 namespace {
 
-constexpr int HC = 256;         // hash slots per warp (normal rows)
-constexpr int HC_BIG = 8192;    // hash slots for rows that overflow HC
+constexpr int HC = 256;         // hash slots of the big kernel's first attempt
+constexpr int HC_BIG = 8192;    // hash slots for rows that overflow the fused pass
 constexpr int ROW_WARPS = 8;
-constexpr int RCAP = 128;       // entries per row in the row scratch
 constexpr int STAGE = 256;      // staged (column, value) contributions per warp
+// fused pass: (hash slots, row scratch entries) -- rows of LLE with k <= 24
+// hold ~3.5 k distinct columns; LTSA and larger k take the wider table
+constexpr int HC_S = 256, RCAP_S = 128;
+constexpr int HC_L = 512, RCAP_L = 256;
 
 __global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, int* cnt, unsigned* err)
 {
@@ -419,19 +422,20 @@ __device__ void table_emit(RowTable<CAP>& T, int lane, int64_t base, int32_t* co
 // ---------------------------------------------------------------------------
 // Fused row pass: one warp per row, contributions staged per round of sources.
 
+template <int HCT>
 struct FusedSmem
 {
-    int keys[HC];
-    double vals[HC];
+    int keys[HCT];
+    double vals[HCT];
     int scol[STAGE];
-    double sval[STAGE];  // reused for the 64-bit sort keys of the emission
+    double sval[STAGE];  // reused for the 64-bit sort keys of the emission (at most STAGE)
 };
 
 // Bitonic sort of 32 * NK 64-bit keys held NK per lane (element i = e * 32 + lane).
 template <int NK>
 __device__ __forceinline__ void warp_bitonic(unsigned long long (&key)[NK], int lane)
 {
-    constexpr int LOGP = 5 + (NK == 4 ? 2 : (NK == 2 ? 1 : 0));
+    constexpr int LOGP = 5 + (NK == 8 ? 3 : (NK == 4 ? 2 : (NK == 2 ? 1 : 0)));
 #pragma unroll
     for (int ls = 1; ls <= LOGP; ++ls)
     {
@@ -475,8 +479,8 @@ __device__ __forceinline__ void warp_bitonic(unsigned long long (&key)[NK], int 
 }
 
 // Sorts the n occupied slots (keys in F.sval, padded) and writes the row.
-template <int NK>
-__device__ __forceinline__ void emit_sorted(FusedSmem& F, int lane, int n, int32_t* out_col, double* out_val)
+template <int NK, class Smem>
+__device__ __forceinline__ void emit_sorted(Smem& F, int lane, int n, int32_t* out_col, double* out_val)
 {
     const unsigned long long* sk = reinterpret_cast<const unsigned long long*>(F.sval);
     unsigned long long key[NK];
@@ -493,8 +497,8 @@ __device__ __forceinline__ void emit_sorted(FusedSmem& F, int lane, int n, int32
         const int i = e * 32 + lane;
         if (i < n)
         {
-            out_col[i] = (int32_t)(key[e] >> 8);
-            out_val[i] = F.vals[key[e] & 0xffull];
+            out_col[i] = (int32_t)(key[e] >> 10);
+            out_val[i] = F.vals[key[e] & 0x3ffull];
         }
     }
 }
@@ -502,7 +506,8 @@ __device__ __forceinline__ void emit_sorted(FusedSmem& F, int lane, int n, int32
 // Row j in one pass: table of (column, sum) in the serial triplet order, then
 // sorted into the row scratch (scol_out/sval_out, RCAP entries per row). Rows
 // that do not fit are listed for the large-table kernel.
-__global__ void __launch_bounds__(ROW_WARPS * 32, 4)
+template <int HCT, int RCAP>
+__global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
     k_rows_fused(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx,
                  const double* __restrict__ wts, double shift, const int64_t* __restrict__ rptr,
                  const int32_t* __restrict__ rev, int* row_nnz, int32_t* scol_out, double* sval_out,
@@ -510,7 +515,8 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    FusedSmem& F = reinterpret_cast<FusedSmem*>(smem_raw)[wib];
+    FusedSmem<HCT>& F = reinterpret_cast<FusedSmem<HCT>*>(smem_raw)[wib];
+    static_assert(RCAP <= STAGE && HCT <= 1024, "sort keys live in sval; slot ids take 10 bits");
     const int KS = k + 1;          // contributions per source
     const int S = STAGE / KS;      // sources per round (0 when k >= STAGE: every row takes the large table)
     const int64_t nw = (int64_t)gridDim.x * ROW_WARPS;
@@ -524,7 +530,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
         bool ok = S > 0 && row_bound(method, k, deg) <= (int64_t)HC_BIG;
         if (ok)
         {
-            for (int h = lane; h < HC; h += 32)
+            for (int h = lane; h < HCT; h += 32)
             {
                 F.keys[h] = -1;
                 F.vals[h] = 0.0;
@@ -611,13 +617,13 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
                     if (!lle)
                     {
                         if (lane == 0 && F.scol[base] >= 0)
-                            ok &= table_add<HC, true>(F, F.scol[base], F.sval[base]);
+                            ok &= table_add<HCT, true>(F, F.scol[base], F.sval[base]);
                         __syncwarp();
                         for (int t0 = 1; t0 < KS; t0 += 32)
                         {
                             const int t = t0 + lane;
                             const bool valid = t < KS && F.scol[base + t] >= 0;
-                            ok &= warp_add<HC, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
+                            ok &= warp_add<HCT, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
                                                      valid ? F.sval[base + t] : 0.0);
                         }
                     }
@@ -627,7 +633,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
                         {
                             const int t = t0 + lane;
                             const bool valid = t < KS;
-                            ok &= warp_add<HC, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
+                            ok &= warp_add<HCT, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
                                                      valid ? F.sval[base + t] : 0.0);
                         }
                     }
@@ -642,14 +648,14 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
             // compact the occupied slots into 64-bit sort keys (column << 8 | slot)
             __syncwarp();
             unsigned long long* sk = reinterpret_cast<unsigned long long*>(F.sval);
-            for (int h0 = 0; h0 < HC; h0 += 32)
+            for (int h0 = 0; h0 < HCT; h0 += 32)
             {
                 const int h = h0 + lane;
                 const bool occ = F.keys[h] != -1;
                 const unsigned m = __ballot_sync(0xffffffffu, occ);
                 if (occ && n + __popc(m & ((1u << lane) - 1u)) < RCAP)
                     sk[n + __popc(m & ((1u << lane) - 1u))] =
-                        ((unsigned long long)(unsigned)F.keys[h] << 8) | (unsigned)h;
+                        ((unsigned long long)(unsigned)F.keys[h] << 10) | (unsigned)h;
                 n += __popc(m);
             }
             __syncwarp();
@@ -669,18 +675,22 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
         double* ov = sval_out + j * RCAP;
         if (n <= 64)
             emit_sorted<2>(F, lane, n, oc, ov);
-        else
+        else if (RCAP <= 128 || n <= 128)
             emit_sorted<4>(F, lane, n, oc, ov);
+        else
+            emit_sorted<8>(F, lane, n, oc, ov);
         if (lane == 0)
             row_nnz[j] = n;
         __syncwarp();
     }
 }
 
-// Copies every row that the fused pass kept from the row scratch into the CSR.
-__global__ void k_compact(int64_t N, const int* __restrict__ row_nnz, const unsigned char* __restrict__ row_big,
-                          const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ scol,
-                          const double* __restrict__ sval, int32_t* col_idx, double* vals)
+// Copies every row that the fused pass kept from the row scratch (rcap entries
+// per row) into the CSR.
+__global__ void k_compact(int64_t N, int rcap, const int* __restrict__ row_nnz,
+                          const unsigned char* __restrict__ row_big, const int64_t* __restrict__ row_ptr,
+                          const int32_t* __restrict__ scol, const double* __restrict__ sval, int32_t* col_idx,
+                          double* vals)
 {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -692,8 +702,8 @@ __global__ void k_compact(int64_t N, const int* __restrict__ row_nnz, const unsi
         const int64_t dst = row_ptr[j];
         for (int i = lane; i < n; i += 32)
         {
-            col_idx[dst + i] = scol[j * RCAP + i];
-            vals[dst + i] = sval[j * RCAP + i];
+            col_idx[dst + i] = scol[j * rcap + i];
+            vals[dst + i] = sval[j * rcap + i];
         }
     }
 }
@@ -745,9 +755,13 @@ struct AsmState
     unsigned char* row_big;
     int32_t* scol;
     double* sval;
+    int rcap;
 };
 
-AsmState asm_state(tk_ctx* ctx, int64_t N, int k)
+// the wide fused-pass table for LTSA and for LLE with k > 24
+bool wide_rows(int method, int k) { return method != TK_METHOD_KLLE || k > 24; }
+
+AsmState asm_state(tk_ctx* ctx, int method, int64_t N, int k)
 {
     const int64_t nk = N * (int64_t)k;
     AsmState a;
@@ -757,16 +771,19 @@ AsmState asm_state(tk_ctx* ctx, int64_t N, int k)
     a.big = (int32_t*)ctx->scratch.get("asm.big", sizeof(int32_t) * (size_t)N);
     a.nbig = (unsigned*)ctx->scratch.get("asm.nbig", 16);
     a.row_big = (unsigned char*)ctx->scratch.get("asm.rowbig", (size_t)N);
-    a.scol = (int32_t*)ctx->scratch.get("asm.scol", sizeof(int32_t) * (size_t)N * RCAP);
-    a.sval = (double*)ctx->scratch.get("asm.sval", sizeof(double) * (size_t)N * RCAP);
+    a.rcap = wide_rows(method, k) ? RCAP_L : RCAP_S;
+    a.scol = (int32_t*)ctx->scratch.get("asm.scol", sizeof(int32_t) * (size_t)N * a.rcap);
+    a.sval = (double*)ctx->scratch.get("asm.sval", sizeof(double) * (size_t)N * a.rcap);
     return a;
 }
 
 void set_smem_limits()
 {
-    const size_t smem = sizeof(FusedSmem) * ROW_WARPS;
     const size_t smem_big = sizeof(RowTable<HC_BIG>);
-    TK_CUDA(cudaFuncSetAttribute(k_rows_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TK_CUDA(cudaFuncSetAttribute(k_rows_fused<HC_S, RCAP_S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(FusedSmem<HC_S>) * ROW_WARPS)));
+    TK_CUDA(cudaFuncSetAttribute(k_rows_fused<HC_L, RCAP_L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(FusedSmem<HC_L>) * ROW_WARPS)));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
 }
@@ -785,7 +802,7 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     const int64_t nk = N * (int64_t)k;
     if (nk >= (int64_t)1 << 31)
         throw Error(TK_ERR_UNSUPPORTED, "assembly supports N*k < 2^31");
-    AsmState a = asm_state(ctx, N, k);
+    AsmState a = asm_state(ctx, method, N, k);
     int* cnt = (int*)ctx->scratch.get("asm.cnt", sizeof(int) * (size_t)N * 2);
     int* fillc = cnt + N;
     const int g = 4 * ctx->num_sms;
@@ -800,8 +817,14 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     k_sort_rev<<<g, 256, 0, st>>>(N, a.rptr, a.rev);
     TK_CHECK_LAUNCH();
     set_smem_limits();
-    k_rows_fused<<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem) * ROW_WARPS, st>>>(
-        method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig, a.row_big);
+    if (wide_rows(method, k))
+        k_rows_fused<HC_L, RCAP_L><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem<HC_L>) * ROW_WARPS, st>>>(
+            method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig,
+            a.row_big);
+    else
+        k_rows_fused<HC_S, RCAP_S><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem<HC_S>) * ROW_WARPS, st>>>(
+            method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig,
+            a.row_big);
     TK_CHECK_LAUNCH();
     k_rows_big<false><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, nullptr, 0.0,
                                                                            a.rptr, a.rev, a.row_nnz, nullptr,
@@ -824,11 +847,11 @@ void assemble_write(tk_ctx* ctx, int method, int64_t N, int k, int td, const int
                     double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals)
 {
     cudaStream_t st = ctx->stream;
-    AsmState a = asm_state(ctx, N, k);
+    AsmState a = asm_state(ctx, method, N, k);
     set_smem_limits();
     const int64_t warps = std::min<int64_t>(N, (int64_t)ctx->num_sms * 64);
-    k_compact<<<(int)((warps + 7) / 8), 256, 0, st>>>(N, a.row_nnz, a.row_big, row_ptr, a.scol, a.sval, col_idx,
-                                                       vals);
+    k_compact<<<(int)((warps + 7) / 8), 256, 0, st>>>(N, a.rcap, a.row_nnz, a.row_big, row_ptr, a.scol, a.sval,
+                                                       col_idx, vals);
     TK_CHECK_LAUNCH();
     k_rows_big<true><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, weights, shift,
                                                                           a.rptr, a.rev, a.row_nnz, row_ptr, col_idx,
