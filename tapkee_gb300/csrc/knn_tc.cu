@@ -680,7 +680,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                      const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
                      int64_t Npad, const uint32_t* __restrict__ near_bits, int nwords,
                      int32_t* __restrict__ cand_idx, float* __restrict__ cand_val, float* __restrict__ far_val,
-                     const float* __restrict__ nrm, unsigned* err)
+                     const float* __restrict__ nrm, int full_blocks, int parts, int32_t* __restrict__ part_idx,
+                     float* __restrict__ part_val, float* __restrict__ part_far, unsigned* err)
 {
     using C = TwCfg;
     constexpr int KC = TW_KC;
@@ -699,10 +700,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ntiles = (int)(Npad / TW_N);
-    const int64_t q0 = (int64_t)blockIdx.x * TC_M;
+    // Work item: CTAs below full_blocks take their whole query block; the blocks
+    // after them (the last, partial wave) are split into `parts` items over
+    // consecutive stretches of the block's tile order, whose lists k_merge_parts
+    // combines.
+    int blk = (int)blockIdx.x, part = 0, nparts = 1;
+    if (blk >= full_blocks)
+    {
+        const int e = blk - full_blocks;
+        blk = full_blocks + e / parts;
+        part = e % parts;
+        nparts = parts;
+    }
+    const int it0 = (int)((int64_t)ntiles * part / nparts);
+    const int nit = (int)((int64_t)ntiles * (part + 1) / nparts) - it0;
+    const int64_t q0 = (int64_t)blk * TC_M;
     // near (full fp16 split) or far (high parts only) pair of this query block and
     // a tile; the block's bits are staged in shared memory when they fit
-    const uint32_t* nb_row = near_bits + (int64_t)blockIdx.x * nwords;
+    const uint32_t* nb_row = near_bits + (int64_t)blk * nwords;
     uint32_t* nb_s = reinterpret_cast<uint32_t*>(gbase + C::OFF_NB);
     const bool nb_staged = nwords <= C::NB_WORDS;
     if (nb_staged)
@@ -752,8 +767,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tma_load_2d(A_s, &tmA_hi, 0, (int)q0, afull);
             tma_load_2d(A_s + C::A_ATOM, &tmA_lo, 0, (int)q0, afull);
             ZigZag zz((int)(q0 / TW_N), ntiles);
+            for (int s = 0; s < it0; ++s)
+                zz.next();
             int issued = 0;
-            for (int it = 0; it < ntiles; ++it)
+            for (int it = 0; it < nit; ++it)
             {
                 const int tile = zz.next();
                 const int slot = it % C::STAGES;
@@ -799,7 +816,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
             const uint64_t bx0 = umma_desc_sw32(B_s + 2 * C::B_ATOM);
             ZigZag zz((int)(q0 / TW_N), ntiles);
-            for (int it = 0; ok && it < ntiles; ++it)
+            for (int s = 0; s < it0; ++s)
+                zz.next();
+            for (int it = 0; ok && it < nit; ++it)
             {
                 const bool nr = is_near(zz.next());
                 const int slot = it % C::STAGES;
@@ -859,8 +878,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         float thr = -__int_as_float(0x7f800000);
         float far_max = -__int_as_float(0x7f800000);  // largest accumulator over far tiles
         ZigZag zz((int)(q0 / TW_N), ntiles);
+        for (int s = 0; s < it0; ++s)
+            zz.next();
         bool alive = true;
-        for (int it = 0; it < ntiles; ++it)
+        for (int it = 0; it < nit; ++it)
         {
             const int tile = zz.next();
             const int buf = it & 1;
@@ -974,15 +995,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
             }
             const float nq = nrm[q];
+            // a whole block writes its rows' lists; a part writes its own slot
+            const int64_t pr = (nparts == 1) ? -1 : ((int64_t)(blk - full_blocks) * TC_M + row) * nparts + part;
+            int32_t* oi = (nparts == 1) ? cand_idx + q * KC : part_idx + pr * KC;
+            float* ov = (nparts == 1) ? cand_val + q * KC : part_val + pr * KC;
 #pragma unroll
             for (int s = 0; s < KC; ++s)
             {
-                cand_idx[q * KC + s] = Ix[s];
-                cand_val[q * KC + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+                oi[s] = Ix[s];
+                ov[s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
             }
             // smallest screened value over far tiles (high-part products only)
             const float fm = fmaxf(far_max, merge_far[row]);
-            far_val[q] = (fm > -FLT_MAX) ? m2 * fm + nq : FLT_MAX;
+            const float fv = (fm > -FLT_MAX) ? m2 * fm + nq : FLT_MAX;
+            if (nparts == 1)
+                far_val[q] = fv;
+            else
+                part_far[pr] = fv;
         }
     }
 
@@ -1052,6 +1081,58 @@ __global__ void __launch_bounds__(256) k_spheres(const float* __restrict__ xc, i
         // FP32 rounding of the centre and of the squares: widen by a relative 1e-5
         rad[blockIdx.x] = nvalid > 0 ? sqrtf(m) * 1.00001f + 1e-6f : -1.f;
     }
+}
+
+// Combines the partial lists of the split blocks: per row, the 32 smallest of
+// the parts' sorted lists (ties to the earlier part, so the result does not
+// depend on timing) and the smallest far value. One thread per row.
+__global__ void k_merge_parts(int64_t row0, int64_t rows, int parts, const int32_t* __restrict__ part_idx,
+                              const float* __restrict__ part_val, const float* __restrict__ part_far,
+                              int32_t* cand_idx, float* cand_val, float* far_val)
+{
+    constexpr int KC = TW_KC;
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows)
+        return;
+    int head[8];
+    float hv[8];
+    float fv = FLT_MAX;
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+    {
+        head[p] = 0;
+        hv[p] = (p < parts) ? part_val[(r * parts + p) * KC] : FLT_MAX;
+        if (p < parts)
+            fv = fminf(fv, part_far[r * parts + p]);
+    }
+    const int64_t q = row0 + r;
+    for (int s = 0; s < KC; ++s)
+    {
+        int best = 0;
+        float bv = hv[0];
+#pragma unroll
+        for (int p = 1; p < 8; ++p)
+            if (hv[p] < bv)
+            {
+                bv = hv[p];
+                best = p;
+            }
+        int bh = 0;
+#pragma unroll
+        for (int p = 0; p < 8; ++p)
+            if (p == best)
+                bh = head[p];
+        cand_idx[q * KC + s] = (bv < FLT_MAX) ? part_idx[(r * parts + best) * KC + bh] : -1;
+        cand_val[q * KC + s] = bv;
+#pragma unroll
+        for (int p = 0; p < 8; ++p)
+            if (p == best)
+            {
+                head[p] = bh + 1;
+                hv[p] = (bh + 1 < KC) ? part_val[(r * parts + p) * KC + bh + 1] : FLT_MAX;
+            }
+    }
+    far_val[q] = fv;
 }
 
 // Upper bound of the k-th neighbour distance of every query of a 128-row block:
@@ -1264,10 +1345,37 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     make_map(&bh, P.xh, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, TW_N);
     make_map(&bl, P.xl, P.Npad, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B, TW_N);
     make_map(&bn, P.xn, P.Npad, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B, TW_N);
+    // One CTA per query block fills whole waves of one CTA per SM; the blocks of
+    // the last, partial wave are split into `parts` CTAs each (at most one wave),
+    // so the kernel does not wait on a few whole blocks at its end.
+    const int sms = std::max(1, ctx->num_sms);
+    const int tail = nq % sms;
+    int parts = (tail > 0 && nq > sms) ? std::min(8, std::min(sms / tail, nt)) : 1;
+    if (parts < 2)
+        parts = 1;
+    const int full_blocks = (parts == 1) ? nq : nq - tail;
+    const int grid = full_blocks + (nq - full_blocks) * parts;
+    const int64_t split_rows = (int64_t)(nq - full_blocks) * TC_M;
+    int32_t* part_idx = nullptr;
+    float *part_val = nullptr, *part_far = nullptr;
+    if (parts > 1)
+    {
+        part_idx = (int32_t*)ctx->scratch.get("tw.pidx", sizeof(int32_t) * (size_t)split_rows * parts * TW_KC);
+        part_val = (float*)ctx->scratch.get("tw.pval", sizeof(float) * (size_t)split_rows * parts * TW_KC);
+        part_far = (float*)ctx->scratch.get("tw.pfar", sizeof(float) * (size_t)split_rows * parts);
+    }
     TK_CUDA(cudaFuncSetAttribute(k_screen_tc_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TwCfg::SMEM));
-    k_screen_tc_wide<<<nq, TC_THREADS, TwCfg::SMEM, st>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad, bits, nwords,
-                                                          cand_idx, cand_val, P.far_val, P.nrm, ctx->dev_err);
+    k_screen_tc_wide<<<grid, TC_THREADS, TwCfg::SMEM, st>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad, bits, nwords,
+                                                           cand_idx, cand_val, P.far_val, P.nrm, full_blocks, parts,
+                                                           part_idx, part_val, part_far, ctx->dev_err);
     TK_CHECK_LAUNCH();
+    if (parts > 1)
+    {
+        k_merge_parts<<<(int)((split_rows + 127) / 128), 128, 0, st>>>((int64_t)full_blocks * TC_M, split_rows, parts,
+                                                                       part_idx, part_val, part_far, cand_idx,
+                                                                       cand_val, P.far_val);
+        TK_CHECK_LAUNCH();
+    }
 }
 
 template <int DP, int KC>

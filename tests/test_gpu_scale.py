@@ -58,3 +58,15 @@ def test_lle_lifted_roll_200k(ctx):
     assert np.abs(op.weights[rows] - W_ref).max() / np.abs(W_ref).max() < 1e-5
     np.testing.assert_allclose(op.weights.sum(1), 1.0, atol=1e-9)
     _csr_checks(op, 1e-9, 1e-6)
+
+
+@pytest.mark.parametrize("n", [25_000, 200_000])
+def test_lle_tensor_screen_equals_fp32_screen(ctx, n):
+    # both screens are certified exact, so the neighbour tables agree row for
+    # row; at these sizes the last, partial wave of query blocks is split into
+    # parts whose lists are merged (25000 points: 196 blocks, 44 split in 3)
+    X = datasets.lifted_swiss_roll(n, 64, seed=1)
+    a = ctx.local_operator(X, "lle", num_neighbors=16, klle_shift=1e-3, check_connectivity=False)
+    b = ctx.local_operator(X, "lle", num_neighbors=16, klle_shift=1e-3, check_connectivity=False, screen="fp32")
+    assert a.rows_uncertified == 0
+    assert np.array_equal(a.idx, b.idx)
