@@ -34,11 +34,6 @@ __device__ __forceinline__ float ldx_f(const void* X, int dtype, int64_t off)
     return dtype == TK_F64 ? (float)reinterpret_cast<const double*>(X)[off] : reinterpret_cast<const float*>(X)[off];
 }
 
-__device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
-{
-    return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
-}
-
 __device__ __forceinline__ float warp_sum_f(float v)
 {
 #pragma unroll
@@ -60,36 +55,55 @@ __device__ __forceinline__ float ord2f(unsigned u)
 
 // 1. column sums: block b sums rows [b*rpb, (b+1)*rpb) for all columns.
 __global__ void k_colsum_partial(const void* X, int dtype, int64_t N, int D, int64_t ldx, int64_t rpb,
-                                 double* partial)
+                                 float* partial)
 {
-    __shared__ double red[4][64];
+    // FP32 sums in a fixed order: the mean only centres the screening
+    // coordinates (the exact distances and the weights use X itself), so its
+    // rounding affects no result
+    __shared__ float red[4][64];
     const int lane64 = threadIdx.x & 63, grp = threadIdx.x >> 6;  // 4 row groups of 64 columns
     const int64_t r0 = (int64_t)blockIdx.x * rpb;
     const int64_t r1 = min(N, r0 + rpb);
     for (int c0 = 0; c0 < D; c0 += 64)
     {
         const int c = c0 + lane64;
-        double s = 0.0;
+        float s0 = 0.f, s1 = 0.f;
         if (c < D)
-            for (int64_t r = r0 + grp; r < r1; r += 4)
-                s += ldx_elem(X, dtype, r * ldx + c);
-        red[grp][lane64] = s;
+        {
+            int64_t r = r0 + grp;
+            for (; r + 4 < r1; r += 8)
+            {
+                s0 += ldx_f(X, dtype, r * ldx + c);
+                s1 += ldx_f(X, dtype, (r + 4) * ldx + c);
+            }
+            if (r < r1)
+                s0 += ldx_f(X, dtype, r * ldx + c);
+        }
+        red[grp][lane64] = s0 + s1;
         __syncthreads();
         if (grp == 0 && c < D)
             partial[(int64_t)blockIdx.x * D + c] = ((red[0][lane64] + red[1][lane64]) + red[2][lane64]) + red[3][lane64];
         __syncthreads();
     }
 }
-
-__global__ void k_colsum_final(const double* partial, int nblk, int D, int64_t N, float* meanf)
+// One block per column: a fixed-shape tree over the block partials.
+__global__ void k_colsum_final(const float* partial, int nblk, int D, int64_t N, float* meanf)
 {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < D; c += gridDim.x * blockDim.x)
+    __shared__ float red[256];
+    const int c = blockIdx.x, t = threadIdx.x;
+    float acc = 0.f;
+    for (int b = t; b < nblk; b += 256)
+        acc += partial[(int64_t)b * D + c];
+    red[t] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1)
     {
-        double s = 0.0;
-        for (int b = 0; b < nblk; ++b)
-            s += partial[(int64_t)b * D + c];
-        meanf[c] = (float)(s / (double)N);
+        if (t < o)
+            red[t] += red[t + o];
+        __syncthreads();
     }
+    if (t == 0)
+        meanf[c] = red[0] / (float)N;
 }
 
 // deterministic pseudo-random sketch matrix entry in [-1, 1)
@@ -199,9 +213,18 @@ __global__ void k_pca3(const float* cov_partial, int nblk, int D, float* H)
     const int t = threadIdx.x;
     for (int p = t; p < 136; p += blockDim.x)
     {
-        float s = 0.f;
-        for (int w = 0; w < nblk; ++w)
-            s += cov_partial[(int64_t)w * 136 + p];
+        // eight independent chains keep the loads of the partials in flight
+        float s8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        int w = 0;
+        for (; w + 8 <= nblk; w += 8)
+        {
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                s8[u] += cov_partial[(int64_t)(w + u) * 136 + p];
+        }
+        for (; w < nblk; ++w)
+            s8[0] += cov_partial[(int64_t)w * 136 + p];
+        const float s = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
         int a = 0, rem = p;
         while (rem >= SKETCH - a)
         {
@@ -264,33 +287,54 @@ __global__ void k_pca3(const float* cov_partial, int nblk, int D, float* H)
 __global__ void k_project(const void* X, int dtype, int64_t N, int D, int64_t ldx, const float* meanf,
                           const float* H, float* proj, unsigned* bbox /* 6: min x3, max x3 */, unsigned* rest_ord)
 {
+    // four rows per iteration: their loads are in flight together
+    constexpr int RW = 4;
     float rloc = 0.f;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    for (int64_t i = warp; i < N; i += nwarps)
+    for (int64_t i0 = warp * RW; i0 < N; i0 += nwarps * RW)
     {
-        float p[3] = {0.f, 0.f, 0.f};
-        float r2 = 0.f;
+        float p[RW][3], r2[RW];
+#pragma unroll
+        for (int u = 0; u < RW; ++u)
+        {
+            p[u][0] = p[u][1] = p[u][2] = 0.f;
+            r2[u] = 0.f;
+        }
         for (int d = lane; d < D; d += 32)
         {
-            const float v = ldx_f(X, dtype, i * ldx + d) - meanf[d];
-            r2 = fmaf(v, v, r2);
-            p[0] = fmaf(H[d * 3 + 0], v, p[0]);
-            p[1] = fmaf(H[d * 3 + 1], v, p[1]);
-            p[2] = fmaf(H[d * 3 + 2], v, p[2]);
+            const float m = meanf[d], h0 = H[d * 3 + 0], h1 = H[d * 3 + 1], h2 = H[d * 3 + 2];
+            float v[RW];
+#pragma unroll
+            for (int u = 0; u < RW; ++u)
+                v[u] = (i0 + u < N) ? ldx_f(X, dtype, (i0 + u) * ldx + d) - m : 0.f;
+#pragma unroll
+            for (int u = 0; u < RW; ++u)
+            {
+                r2[u] = fmaf(v[u], v[u], r2[u]);
+                p[u][0] = fmaf(h0, v[u], p[u][0]);
+                p[u][1] = fmaf(h1, v[u], p[u][1]);
+                p[u][2] = fmaf(h2, v[u], p[u][2]);
+            }
         }
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
+        for (int u = 0; u < RW; ++u)
         {
-            p[c] = warp_sum_f(p[c]);
-            mn[c] = fminf(mn[c], p[c]);
-            mx[c] = fmaxf(mx[c], p[c]);
+            if (i0 + u >= N)
+                break;
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+            {
+                p[u][c] = warp_sum_f(p[u][c]);
+                mn[c] = fminf(mn[c], p[u][c]);
+                mx[c] = fmaxf(mx[c], p[u][c]);
+            }
+            if (lane < 3)
+                proj[(i0 + u) * 3 + lane] = lane == 0 ? p[u][0] : (lane == 1 ? p[u][1] : p[u][2]);
+            rloc = fmaxf(rloc, sqrtf(warp_sum_f(r2[u])));
         }
-        if (lane < 3)
-            proj[i * 3 + lane] = lane == 0 ? p[0] : (lane == 1 ? p[1] : p[2]);
-        rloc = fmaxf(rloc, sqrtf(warp_sum_f(r2)));
     }
     if (lane == 0 && rloc > 0.f)
         atomicMax(rest_ord, f2ord(rloc));
@@ -363,51 +407,76 @@ __global__ void k_layout(const void* X, int dtype, int64_t N, int64_t Npad, int 
     if (warp == 0 && lane == 0 && scale_out)
         *scale_out = (float)s;
     float rloc = 0.f;
-    for (int64_t p = warp; p < Npad; p += nwarps)
+    // two rows per iteration: their gathers are in flight together
+    constexpr int RW = 2;
+    for (int64_t p0 = warp * RW; p0 < Npad; p0 += nwarps * RW)
     {
-        const bool valid = p < N;
-        const int64_t i = valid ? perm[p] : 0;
-        ff n2 = ff_zero();
+        int64_t src[RW];
+        bool valid[RW];
+#pragma unroll
+        for (int u = 0; u < RW; ++u)
+        {
+            valid[u] = p0 + u < N;
+            src[u] = valid[u] ? perm[p0 + u] : 0;
+        }
+        ff n2[RW];
+#pragma unroll
+        for (int u = 0; u < RW; ++u)
+            n2[u] = ff_zero();
         for (int d = lane; d < Dp; d += 32)
         {
-            float v = 0.f;
-            if (valid && d < D)
+            float v[RW];
+#pragma unroll
+            for (int u = 0; u < RW; ++u)
+                v[u] = (valid[u] && d < D) ? ldx_f(X, dtype, src[u] * ldx + d) - meanf[d] : 0.f;
+#pragma unroll
+            for (int u = 0; u < RW; ++u)
             {
-                v = ldx_f(X, dtype, i * ldx + d) - meanf[d];
-                n2 = ff_add(n2, two_prod(v, v));
-            }
-            xc[p * Dp + d] = v;
-            if (xh)
-            {
-                const float vs = v * scale;
-                const __half h = __float2half_rn(vs);
-                const __half l = __float2half_rn(vs - __half2float(h));
-                xh[p * Dp + d] = h;
-                xl[p * Dp + d] = l;
+                const int64_t p = p0 + u;
+                if (p >= Npad)
+                    break;
+                n2[u] = ff_add(n2[u], two_prod(v[u], v[u]));
+                xc[p * Dp + d] = v[u];
+                if (xh)
+                {
+                    const float vs = v[u] * scale;
+                    const __half h = __float2half_rn(vs);
+                    const __half l = __float2half_rn(vs - __half2float(h));
+                    xh[p * Dp + d] = h;
+                    xl[p * Dp + d] = l;
+                }
             }
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            n2 = ff_add(n2, ff_shfl_xor(n2, o));
-        const double n2d = ff_to_double(n2);
-        if (valid)
-            rloc = fmaxf(rloc, (float)sqrt(n2d) * 1.000001f);
-        if (lane == 0)
-            nrm[p] = valid ? (float)n2d : __int_as_float(0x7f800000);
-        if (xn && lane < 16)
+        for (int u = 0; u < RW; ++u)
         {
-            // -|2^s xc|^2 / 2^14 as fp16 hi + lo: the tensor screen adds 2^13 (h + l)
-            // = -|2^s y|^2 / 2 to every dot product through one extra K=16 step.
-            // Padding rows stay 0 (the screen skips their indices).
-            __half v = __float2half_rn(0.f);
-            if (valid && lane < 2)
+            const int64_t p = p0 + u;
+            if (p >= Npad)
+                break;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                n2[u] = ff_add(n2[u], ff_shfl_xor(n2[u], o));
+            // n2 is normalised, so hi is |xc|^2 rounded to FP32; sqrtf is within an
+            // ulp, which the 1e-6 margin covers
+            if (valid[u])
+                rloc = fmaxf(rloc, sqrtf(n2[u].hi) * 1.000001f);
+            if (lane == 0)
+                nrm[p] = valid[u] ? n2[u].hi : __int_as_float(0x7f800000);
+            if (xn && lane < 16)
             {
-                const float f = ldexpf(1.f, 2 * s - 14);
-                const float t_hi = -n2.hi * f, t_lo = -n2.lo * f;
-                const __half h = __float2half_rn(t_hi);
-                v = (lane == 0) ? h : __float2half_rn((t_hi - __half2float(h)) + t_lo);
+                // -|2^s xc|^2 / 2^14 as fp16 hi + lo: the tensor screen adds 2^13 (h + l)
+                // = -|2^s y|^2 / 2 to every dot product through one extra K=16 step.
+                // Padding rows stay 0 (the screen skips their indices).
+                __half hv = __float2half_rn(0.f);
+                if (valid[u] && lane < 2)
+                {
+                    const float f = ldexpf(1.f, 2 * s - 14);
+                    const float t_hi = -n2[u].hi * f, t_lo = -n2[u].lo * f;
+                    const __half h = __float2half_rn(t_hi);
+                    hv = (lane == 0) ? h : __float2half_rn((t_hi - __half2float(h)) + t_lo);
+                }
+                xn[p * 16 + lane] = hv;
             }
-            xn[p * 16 + lane] = v;
         }
     }
     if (lane == 0 && rloc > 0.f)
@@ -434,11 +503,11 @@ void prepare_points(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int
     // 1. mean
     const int nblk = (int)std::min<int64_t>(4 * sms, std::max<int64_t>(1, (N + 63) / 64));
     const int64_t rpb = (N + nblk - 1) / nblk;
-    double* partial = (double*)ctx->scratch.get("prep.partial", sizeof(double) * (size_t)nblk * D);
+    float* partial = (float*)ctx->scratch.get("prep.partial", sizeof(float) * (size_t)nblk * D);
     float* meanf = (float*)ctx->scratch.get("prep.mean", sizeof(float) * D);
     k_colsum_partial<<<nblk, 256, 0, st>>>(X, dtype, N, D, ldx, rpb, partial);
     TK_CHECK_LAUNCH();
-    k_colsum_final<<<(D + 255) / 256, 256, 0, st>>>(partial, nblk, D, N, meanf);
+    k_colsum_final<<<D, 256, 0, st>>>(partial, nblk, D, N, meanf);
     TK_CHECK_LAUNCH();
 
     // 2. sketch covariance (subsample)
