@@ -321,28 +321,34 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
             }
         }
         // e_k: an upper bound of the exact k-th distance, from the lane holding
-        // rank k-1
+        // rank k-1, rounded up to FP32 (exact pair: hi + lo rounded up; FP32
+        // value: f (1 + gam) rounded up)
         unsigned own = 0u;
-        double ek_own = 0.0;
+        float ek_own = 0.f;
 #pragma unroll
         for (int s = 0; s < PER; ++s)
             if (rank[s] == k - 1)
             {
                 own = 1u;
-                ek_own = exact[s] ? (double)kh[s] + (double)kl[s] : (double)kh[s] * (1.0 + (double)gam);
+                ek_own = exact[s] ? __fadd_ru(kh[s], kl[s]) : __fmul_ru(kh[s], __fadd_ru(1.f, gam));
             }
         const unsigned holder = __ballot_sync(0xffffffffu, own != 0u);
-        const double ek = __shfl_sync(0xffffffffu, ek_own, holder ? __ffs(holder) - 1 : 0);
+        const float ek = __shfl_sync(0xffffffffu, ek_own, holder ? __ffs(holder) - 1 : 0);
         bool certified = true;
         if (lane == 0)
         {
+            // the bounds eps are rounded up and T - eps down, so every comparison
+            // is at least as strict as in exact arithmetic (FP32 throughout: no
+            // FP64 square root per row)
+            const float R = V.R;
+            const float nx = nrm[p];
+            const float base = __fmul_ru(c1, __fadd_ru(nx, __fmul_ru(R, R)));
+            const float sr = __fmul_ru(__fsqrt_ru(nx), R);
             const float T = cand_val[p * KC + KC - 1];
             if (T < FLT_MAX)  // a full list: points outside it are bounded below
             {
-                const double R = (double)V.R;
-                const double nx = (double)nrm[p];
-                const double eps = (double)c1 * (nx + R * R) + (double)c2 * sqrt(nx) * R;
-                certified = ek < (double)T - eps;
+                const float eps = __fadd_ru(base, __fmul_ru(c2, sr));
+                certified = ek < __fsub_rd(T, eps);
             }
             if (RS.far_val)
             {
@@ -351,10 +357,8 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                 const float A = RS.far_val[p];
                 if (A < FLT_MAX)
                 {
-                    const double R = (double)V.R;
-                    const double nx = (double)nrm[p];
-                    const double eps_far = (double)c1 * (nx + R * R) + (double)RS.c2_far * sqrt(nx) * R;
-                    certified = certified && ek < (double)A - eps_far;
+                    const float eps_far = __fadd_ru(base, __fmul_ru(RS.c2_far, sr));
+                    certified = certified && ek < __fsub_rd(A, eps_far);
                 }
             }
         }
@@ -374,7 +378,7 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
         {
             const unsigned fidx = atomicAdd(nfailed, 1u);
             failed[fidx] = (int32_t)p;
-            failed_ub[fidx] = ek;
+            failed_ub[fidx] = (double)ek;
         }
     }
 }
