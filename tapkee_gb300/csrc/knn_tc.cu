@@ -206,6 +206,13 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // Branchless sorted insertion into a register list (ascending).
 template <int KC>
 __device__ __forceinline__ void reg_insert(float (&L)[KC], int32_t (&I)[KC], float v, int32_t id)
@@ -496,7 +503,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int quad = warp & 3;
         const int qt = warp >> 2;
         const int row = quad * 32 + lane;
-        float* stash = stash_all + (warp * 32 + lane) * (C::STASH + 1);
         int gi = 0;
         bool alive = true;
         for (int j = j_first; alive && j < j_end; j += j_step)
@@ -552,38 +558,49 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         if (lane == 0)
                             mbar_arrive(smem_u32(&Bar.tempty[buf][qt]));
                     }
+                    // largest value of each group of 8 columns (3-input max) and of
+                    // the round: one branch per round when nothing passes
+                    constexpr int NG = CPW / 8;
+                    float gm[NG];
 #pragma unroll
-                    for (int s32 = 0; s32 < CPW / 32; ++s32)
+                    for (int g = 0; g < NG; ++g)
                     {
-                        float gm[4];
+                        const float* w = v + g * 8;
+                        gm[g] = fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7]));
+                    }
+                    float gall = gm[0];
 #pragma unroll
-                        for (int g = 0; g < 4; ++g)
-                        {
-                            const float* w = v + s32 * 32 + g * 8;
-                            gm[g] = fmaxf(fmaxf(fmaxf(w[0], w[1]), fmaxf(w[2], w[3])),
-                                          fmaxf(fmaxf(w[4], w[5]), fmaxf(w[6], w[7])));
-                        }
-                        if (fmaxf(fmaxf(gm[0], gm[1]), fmaxf(gm[2], gm[3])) > thr)
-                        {
+                    for (int g = 1; g < NG; ++g)
+                        gall = fmaxf(gall, gm[g]);
+                    if (gall > thr)
+                    {
 #pragma unroll
-                            for (int g = 0; g < 4; ++g)
+                        for (int g = 0; g < NG; ++g)
+                        {
+                            if (gm[g] > thr)
                             {
-                                if (gm[g] > thr)
-                                {
+                                // columns of the group that pass, then one insertion each
+                                const float* w = v + g * 8;
+                                unsigned msk = 0u;
 #pragma unroll
-                                    for (int e = 0; e < 8; ++e)
-                                        stash[e] = v[s32 * 32 + g * 8 + e];
-                                    const int64_t cb = c0 + h * CPW + s32 * 32 + g * 8;
+                                for (int e = 0; e < 8; ++e)
+                                    msk |= (w[e] > thr) ? (1u << e) : 0u;
+                                const int64_t cb = c0 + h * CPW + g * 8;
 #pragma unroll 1
-                                    for (int e = 0; e < 8; ++e)
+                                while (msk)
+                                {
+                                    const int e = __ffs(msk) - 1;
+                                    msk &= msk - 1u;
+                                    float x = w[0];
+#pragma unroll
+                                    for (int e2 = 1; e2 < 8; ++e2)
+                                        x = (e == e2) ? w[e2] : x;
+                                    const float t = m2 * x;
+                                    if (t < cmp && cb + e < I.n)
                                     {
-                                        const float t = m2 * stash[e];
-                                        if (t < cmp && cb + e < I.n)
-                                        {
-                                            reg_insert<KC>(L, Ix, t, (int32_t)(cb + e));
-                                            cmp = L[KC - 1];
-                                            thr = cmp * inv_m2;
-                                        }
+                                        reg_insert<KC>(L, Ix, t, (int32_t)(cb + e));
+                                        cmp = L[KC - 1];
+                                        thr = cmp * inv_m2;
                                     }
                                 }
                             }
@@ -665,13 +682,6 @@ __device__ __forceinline__ void umma_f16_w(uint32_t dtmem, uint64_t adesc, uint6
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
             dtmem),
         "l"(adesc), "l"(bdesc), "r"(IDESC_W), "r"(accumulate));
-}
-
-__device__ __forceinline__ float fmax3(float a, float b, float c)
-{
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
