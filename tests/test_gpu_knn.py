@@ -97,3 +97,22 @@ def test_device_resident_inputs(ctx):
     assert idx_d.is_cuda
     idx_h = ctx.knn_brute(X, 16)
     assert np.array_equal(idx_d.cpu().numpy(), idx_h)
+
+
+@pytest.mark.parametrize("n", [1290, 1300, 1345, 1353])
+def test_wide_screen_short_last_block(ctx, n):
+    # the last 128-query block holds 10, 20, 65 and 73 rows: the block-mate
+    # bound of its k-th neighbour distance is infinite (every tile near), taken
+    # over all of its rows, or over a 64-row window
+    X = datasets.lifted_swiss_roll(n, 64, seed=n)
+    idx = ctx.knn_brute(X, 16, screen="tensor")
+    ref, _, _ = oracle.knn_brute(X, 16)
+    assert np.array_equal(idx, _ordered(X, ref)[0])
+
+
+def test_wide_screen_tail_blocks_split_in_eight(ctx):
+    # 19600 points: 154 query blocks, the 2 after the first 152 split in 8 parts
+    X = datasets.lifted_swiss_roll(19_600, 64, seed=5)
+    a = ctx.knn_brute(X, 16, screen="tensor")
+    b = ctx.knn_brute(X, 16, screen="fp32")
+    assert np.array_equal(a, b)
