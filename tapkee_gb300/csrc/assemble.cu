@@ -44,7 +44,8 @@ constexpr int STAGE = 256;      // staged (column, value) contributions per warp
 constexpr int HC_S = 256, RCAP_S = 128;
 constexpr int HC_L = 512, RCAP_L = 256;
 
-__global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, int* cnt, unsigned* err)
+__global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, int k, int* cnt, unsigned* repeats,
+                        unsigned* err)
 {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x)
     {
@@ -55,6 +56,13 @@ __global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, 
             continue;
         }
         atomicAdd(&cnt[j], 1);
+        // a point listed as its own neighbour, or twice in one list
+        const int64_t r = e / k, a = e - r * k;
+        bool rep = (j == r);
+        for (int b = 0; b < a && !rep; ++b)
+            rep = idx[r * k + b] == j;
+        if (rep)
+            atomicOr(repeats, 1u);
     }
 }
 
@@ -245,6 +253,24 @@ __device__ __forceinline__ bool warp_add(Table& T, int lane, bool valid, int col
     }
     return ok;
 }
+
+// n / d for 0 <= n < 2^31 and a divisor fixed per launch: one multiply-high by
+// m = ceil(2^32 / d) (2^32 - 1 for d = 1) gives floor(n / d) or one more or
+// less, and the remainder fixes it.
+struct FastDiv
+{
+    int d;
+    unsigned m;
+    __host__ __device__ explicit FastDiv(int dd)
+        : d(dd), m(dd <= 1 ? 0xffffffffu : (unsigned)((0x100000000ull + (unsigned)dd - 1) / (unsigned)dd)) {}
+    __device__ __forceinline__ int div(int n) const
+    {
+        int q = (int)__umulhi((unsigned)n, m);
+        const int r = n - q * d;
+        q += (r < 0) ? -1 : ((r >= d) ? 1 : 0);
+        return q;
+    }
+};
 
 // Upper bound of the number of distinct columns in row j.
 __device__ __forceinline__ int64_t row_bound(int method, int k, int64_t deg)
@@ -511,7 +537,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
     k_rows_fused(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx,
                  const double* __restrict__ wts, double shift, const int64_t* __restrict__ rptr,
                  const int32_t* __restrict__ rev, int* row_nnz, int32_t* scol_out, double* sval_out,
-                 int32_t* big_rows, unsigned* nbig, unsigned char* row_big)
+                 int32_t* big_rows, unsigned* nbig, unsigned char* row_big, const unsigned* repeats)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -522,6 +548,10 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
     const int64_t nw = (int64_t)gridDim.x * ROW_WARPS;
     const bool lle = method == TK_METHOD_KLLE;
     const double inv_k = 1.0 / k;
+    const FastDiv div_k(k), div_ks(KS);
+    // no point lists itself or a neighbour twice (always so for kNN output):
+    // a source's contributions then have distinct columns and add in one step
+    const bool distinct = *repeats == 0u;
     for (int64_t j = (int64_t)blockIdx.x * ROW_WARPS + wib; j < N; j += nw)
     {
         __syncwarp();
@@ -541,7 +571,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
             for (int64_t p0 = b; p0 < e; p0 += 32)
             {
                 const int64_t p = p0 + lane;
-                const bool lt = p < e && (int64_t)(rev[p] / k) <= j;
+                const bool lt = p < e && (int64_t)div_k.div(rev[p]) <= j;
                 pos_j += __popc(__ballot_sync(0xffffffffu, lt));
             }
             const int total = (int)deg + 1;
@@ -552,14 +582,14 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
                 // stage the round's contributions: item it = (source s, entry t)
                 for (int it = lane; it < ns * KS; it += 32)
                 {
-                    const int s = it / KS, t = it - s * KS;
+                    const int s = div_ks.div(it), t = it - s * KS;
                     const int p = r0 + s;
                     int64_t src = j;
                     int slot = -1;
                     if (p != pos_j)
                     {
                         const int32_t eid = rev[b + (p < pos_j ? p : p - 1)];
-                        src = eid / k;
+                        src = div_k.div(eid);
                         slot = eid - (int32_t)src * k;
                     }
                     int col = -1;
@@ -623,8 +653,14 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
                         {
                             const int t = t0 + lane;
                             const bool valid = t < KS && F.scol[base + t] >= 0;
-                            ok &= warp_add<HCT, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
-                                                     valid ? F.sval[base + t] : 0.0);
+                            if (distinct)
+                            {
+                                if (valid)
+                                    ok &= table_add<HCT, true>(F, F.scol[base + t], F.sval[base + t]);
+                            }
+                            else
+                                ok &= warp_add<HCT, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
+                                                         valid ? F.sval[base + t] : 0.0);
                         }
                     }
                     else
@@ -633,8 +669,14 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
                         {
                             const int t = t0 + lane;
                             const bool valid = t < KS;
-                            ok &= warp_add<HCT, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
-                                                     valid ? F.sval[base + t] : 0.0);
+                            if (distinct)
+                            {
+                                if (valid)
+                                    ok &= table_add<HCT, true>(F, F.scol[base + t], F.sval[base + t]);
+                            }
+                            else
+                                ok &= warp_add<HCT, true>(F, lane, valid, valid ? F.scol[base + t] : 0,
+                                                         valid ? F.sval[base + t] : 0.0);
                         }
                     }
                     __syncwarp();
@@ -809,7 +851,9 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     TK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)N * 2, st));
     TK_CUDA(cudaMemsetAsync(a.nbig, 0, 16, st));
     TK_CUDA(cudaMemsetAsync(a.row_big, 0, (size_t)N, st));
-    k_indeg<<<g, 256, 0, st>>>(idx, nk, N, cnt, ctx->dev_err);
+    unsigned* repeats = (unsigned*)ctx->scratch.get("asm.repeats", 16);
+    TK_CUDA(cudaMemsetAsync(repeats, 0, 16, st));
+    k_indeg<<<g, 256, 0, st>>>(idx, nk, N, k, cnt, repeats, ctx->dev_err);
     TK_CHECK_LAUNCH();
     scan_to_offsets(ctx, cnt, N, a.rptr);
     k_fill_rev<<<g, 256, 0, st>>>(idx, nk, a.rptr, fillc, a.rev);
@@ -820,11 +864,11 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     if (wide_rows(method, k))
         k_rows_fused<HC_L, RCAP_L><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem<HC_L>) * ROW_WARPS, st>>>(
             method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig,
-            a.row_big);
+            a.row_big, repeats);
     else
         k_rows_fused<HC_S, RCAP_S><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem<HC_S>) * ROW_WARPS, st>>>(
             method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig,
-            a.row_big);
+            a.row_big, repeats);
     TK_CHECK_LAUNCH();
     k_rows_big<false><<<ctx->num_sms, 32, sizeof(RowTable<HC_BIG>), st>>>(method, N, k, td, idx, nullptr, 0.0,
                                                                            a.rptr, a.rev, a.row_nnz, nullptr,
