@@ -206,6 +206,24 @@ int tk_ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64
 int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
                 double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, int64_t* nnz_io);
 
+/* The dense eigenproblem pair of NPE (kind TK_PAIR_NPE, from the KLLE matrix M)
+ * or LLTSA (kind TK_PAIR_LLTSA, from the KLTSA matrix M) for the linear
+ * kernel: replaces construct_neighborhood_preserving_eigenproblem and
+ * construct_lltsa_eigenproblem (routines/locally_linear.hpp:257-338). X is
+ * points-major (N rows of D, row stride ldx), M is the CSR of tk_assemble /
+ * tk_operator_copy (row_ptr: N + 1; col_idx, vals: row_ptr[N]). lhs and rhs are
+ * D x D, column-major, written exactly as the reference leaves them:
+ *   rhs = (U + U^T) / 2, U the upper triangle of sum_i x_i x_i^T (LLTSA: minus
+ *         s s^T / N, s = sum_i x_i) -- off-diagonal entries halved;
+ *   lhs = upper triangle of sum over nonzeros (i, j) of M_ij (x_i x_j^T + x_j
+ *         x_i^T) (LLTSA: minus s s^T / N), lower triangle zero.
+ * All pointers may be host or device memory. FP64 sums over fixed row blocks. */
+#define TK_PAIR_NPE 0
+#define TK_PAIR_LLTSA 1
+int tk_eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_t N, int D, int64_t ldx,
+                         const int64_t* row_ptr, const int32_t* col_idx, const double* vals, double* lhs,
+                         double* rhs);
+
 /* The whole stage of KernelLocallyLinearEmbeddingImplementation::embed /
  * KernelLocalTangentSpaceAlignmentImplementation::embed up to the eigensolver
  * (methods/kernel_locally_linear_embedding.hpp:22-30,

@@ -55,6 +55,8 @@ def lib():
         L.oracle_ltsa_basis.restype = i32
         L.oracle_assemble.argtypes = [i32, i64, i32, i32, iptr, dptr, ctypes.c_double, dptr, dptr, dptr, i64]
         L.oracle_assemble.restype = i64
+        L.oracle_eigenproblem_pair.argtypes = [i32, i64, i32, dptr, dptr, iptr, dptr, dptr, dptr]
+        L.oracle_eigenproblem_pair.restype = None
         _lib = L
     return _lib
 
@@ -165,6 +167,22 @@ def assemble(method, idx, weights, shift):
                                 row_ptr.ctypes.data, col.ctypes.data, vals.ctypes.data, nnz)
     assert got == nnz
     return row_ptr, col, vals
+
+
+def eigenproblem_pair(kind, X, row_ptr, col, vals):
+    """The NPE (kind 0) or LLTSA (kind 1) dense eigenproblem pair (lhs, rhs), D x D,
+    built as routines/locally_linear.hpp:257-338 builds them for the linear
+    kernel (X points-major, N x D; M in CSR)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    N, D = X.shape
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    ci = np.ascontiguousarray(col, dtype=np.int32)
+    v = np.ascontiguousarray(vals, dtype=np.float64)
+    lhs = np.zeros((D, D), np.float64, order="F")
+    rhs = np.zeros((D, D), np.float64, order="F")
+    lib().oracle_eigenproblem_pair(int(kind), N, D, X.ctypes.data, rp.ctypes.data, ci.ctypes.data, v.ctypes.data,
+                                   lhs.ctypes.data, rhs.ctypes.data)
+    return lhs, rhs
 
 
 def dense_embedding(row_ptr, col, vals, td):

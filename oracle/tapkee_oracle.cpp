@@ -508,4 +508,57 @@ int64_t oracle_assemble(int method, int64_t N, int k, int td, const int32_t* idx
     return nnz;
 }
 
+
+// construct_neighborhood_preserving_eigenproblem (kind 0) and
+// construct_lltsa_eigenproblem (kind 1), routines/locally_linear.hpp:257-338,
+// for the linear kernel's feature vectors (the rows of X, points-major). The
+// sparse matrix is given in CSR; it is symmetric, so its CSR arrays are also the
+// CSC arrays the reference's InnerIterator walks, and the loops below visit
+// the nonzeros in that order. lhs and rhs are D x D column-major:
+//   rhs: upper triangle of sum_i x_i x_i^T (LLTSA: minus s s^T / N, s = sum_i
+//        x_i), then rhs = (rhs + rhs^T) / 2 -- the lower triangle enters as
+//        zero, so off-diagonal entries end halved, as in the reference;
+//   lhs: upper triangle of sum over nonzeros (i, j) of v (x_i x_j^T + x_j x_i^T)
+//        (LLTSA: minus s s^T / N); the lower triangle stays zero.
+void oracle_eigenproblem_pair(int kind, int64_t N, int D, const double* X, const int64_t* row_ptr,
+                              const int32_t* col_idx, const double* vals, double* lhs, double* rhs)
+{
+    std::vector<double> L((size_t)D * D, 0.0), R((size_t)D * D, 0.0), s(D, 0.0);
+    auto at = [D](std::vector<double>& M, int a, int b) -> double& { return M[(size_t)b * D + a]; };
+    for (int64_t i = 0; i < N; ++i)
+    {
+        const double* x = X + i * D;
+        for (int a = 0; a < D; ++a)
+            s[a] += x[a];
+        for (int b = 0; b < D; ++b)
+            for (int a = 0; a <= b; ++a)
+                at(R, a, b) += x[a] * x[b];
+    }
+    if (kind == 1)
+        for (int b = 0; b < D; ++b)
+            for (int a = 0; a <= b; ++a)
+                at(R, a, b) += -1.0 / (double)N * s[a] * s[b];
+    for (int64_t c = 0; c < N; ++c)  // outer index (column of the CSC view)
+        for (int64_t p = row_ptr[c]; p < row_ptr[c + 1]; ++p)
+        {
+            const int64_t r = col_idx[p];  // it.row()
+            const double v = vals[p];
+            const double* xi = X + r * D;
+            const double* xj = X + c * D;
+            for (int b = 0; b < D; ++b)
+                for (int a = 0; a <= b; ++a)
+                    at(L, a, b) += v * xi[a] * xj[b] + v * xj[a] * xi[b];
+        }
+    if (kind == 1)
+        for (int b = 0; b < D; ++b)
+            for (int a = 0; a <= b; ++a)
+                at(L, a, b) += -1.0 / (double)N * s[a] * s[b];
+    for (int b = 0; b < D; ++b)
+        for (int a = 0; a < D; ++a)
+        {
+            lhs[(size_t)b * D + a] = L[(size_t)b * D + a];
+            rhs[(size_t)b * D + a] = (R[(size_t)b * D + a] + R[(size_t)a * D + b]) / 2.0;
+        }
+}
+
 } // extern "C"

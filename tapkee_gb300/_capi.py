@@ -21,6 +21,8 @@ TK_ERR_CANCELLED = 6
 TK_ERR_BUFFER_TOO_SMALL = 7
 TK_ERR_UNSUPPORTED = 8
 TK_ERR_NO_DEVICE = 9
+TK_PAIR_NPE = 0
+TK_PAIR_LLTSA = 1
 TK_ERR_INTERNAL = 10
 
 TK_F32, TK_F64 = 0, 1
@@ -91,6 +93,7 @@ SIGNATURES = {
     "tk_lle_weights_grad": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P, _P, _P]),
     "tk_ltsa_basis": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _I, _P]),
     "tk_assemble": (_I, [_P, _I, _I64, _I, _I, _P, _P, _D, _P, _P, _P, ctypes.POINTER(_I64)]),
+    "tk_eigenproblem_pair": (_I, [_P, _I, _P, _I, _I64, _I, _I64, _P, _P, _P, _P, _P]),
     "tk_local_operator": (_I, [_P, ctypes.POINTER(tk_params), _P, _I, _I64, _I, _I64,
                                ctypes.POINTER(tk_operator_info)]),
     "tk_operator_copy": (_I, [_P, _P, _P, _P, _P, _P]),

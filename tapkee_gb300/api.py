@@ -290,6 +290,27 @@ class Context:
                                          val.ptr, ctypes.byref(nnz)))
         return rp.arr, col.arr, val.arr
 
+    def eigenproblem_pair(self, kind, X, row_ptr, col_idx, vals):
+        """The NPE ("npe", from the LLE matrix M) or LLTSA ("lltsa", from the LTSA
+        matrix M) dense pair (lhs, rhs), D x D, as
+        routines/locally_linear.hpp:257-338 leaves them: lhs on its upper
+        triangle (lower zero), rhs symmetric with halved off-diagonal entries."""
+        k = {"npe": C.TK_PAIR_NPE, "lltsa": C.TK_PAIR_LLTSA}[kind] if isinstance(kind, str) else int(kind)
+        xb, dt = _as_points(X)
+        if xb.arr.ndim != 2:
+            raise WrongParameterError("X must be 2-D (points x features)")
+        N, D = xb.arr.shape
+        rp = _Buf(np.ascontiguousarray(np.asarray(row_ptr, dtype=np.int64)), "np") if not _is_torch(row_ptr) \
+            else _Buf(row_ptr.to(_torch().int64).contiguous(), "torch")
+        ci = _as_index(col_idx, xb)
+        vb = _as_f64(vals)
+        lhs = np.zeros(D * D, np.float64)
+        rhs = np.zeros(D * D, np.float64)
+        self._check(self.lib.tk_eigenproblem_pair(self.ptr, k, xb.ptr, dt, N, D, D, rp.ptr, ci.ptr, vb.ptr,
+                                                  lhs.ctypes.data, rhs.ctypes.data))
+        # column-major D x D -> [a, b]
+        return lhs.reshape(D, D).T.copy(), rhs.reshape(D, D).T.copy()
+
     def local_operator(self, X, method="lle", num_neighbors=5, target_dimension=2, klle_shift=1e-3,
                        nullspace_shift=1e-9, check_connectivity=True, screen="tensor", cancel_function=None,
                        copy_out=True):

@@ -498,6 +498,48 @@ int tk_ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64
     });
 }
 
+int tk_eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_t N, int D, int64_t ldx,
+                         const int64_t* row_ptr, const int32_t* col_idx, const double* vals, double* lhs,
+                         double* rhs)
+{
+    return guarded(ctx, [&] {
+        if (N <= 0)
+            throw Error(TK_ERR_NO_DATA, "No data");
+        if (kind != TK_PAIR_NPE && kind != TK_PAIR_LLTSA)
+            throw Error(TK_ERR_UNSUPPORTED, "unsupported eigenproblem kind");
+        if (!X || !row_ptr || !col_idx || !vals || !lhs || !rhs || D < 1 || ldx < D)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        check_dtype(dtype);
+        int64_t ldd = 0;
+        const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "io.X");
+        int64_t nnz = 0;
+        if (is_device_ptr(row_ptr))
+        {
+            TK_CUDA(cudaMemcpyAsync(ctx->host_i64, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            TK_CUDA(cudaStreamSynchronize(ctx->stream));
+            nnz = ctx->host_i64[0];
+        }
+        else
+            nnz = row_ptr[N];
+        if (nnz < 0)
+            throw Error(TK_ERR_INVALID_ARG, "row_ptr[N] < 0");
+        const int64_t* rp_d = device_array(ctx, row_ptr, (size_t)N + 1, "io.pair_rp");
+        const int32_t* c_d = device_array(ctx, col_idx, (size_t)std::max<int64_t>(nnz, 1), "io.pair_col");
+        const double* v_d = device_array(ctx, vals, (size_t)std::max<int64_t>(nnz, 1), "io.pair_val");
+        bool lh = false, rh = false;
+        double* l_d = device_out(ctx, lhs, (size_t)D * D, "io.pair_lhs", &lh);
+        double* r_d = device_out(ctx, rhs, (size_t)D * D, "io.pair_rhs", &rh);
+        eigenproblem_pair(ctx, kind, Xd, dtype, N, D, ldd, rp_d, c_d, v_d, l_d, r_d);
+        check_device_errors(ctx);
+        if (lh)
+            copy_back(ctx, lhs, l_d, (size_t)D * D);
+        if (rh)
+            copy_back(ctx, rhs, r_d, (size_t)D * D);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
                 double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, int64_t* nnz_io)
 {

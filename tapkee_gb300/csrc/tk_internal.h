@@ -229,6 +229,10 @@ int64_t assemble_rows(tk_ctx* ctx, int method, int64_t N, int k, int td, const i
 void assemble_write(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
                     double shift, const int64_t* row_ptr, int32_t* col_idx, double* vals);
 
+// pair.cu: the NPE / LLTSA dense eigenproblem pair (device pointers).
+void eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_t N, int D, int64_t ldx,
+                       const int64_t* row_ptr, const int32_t* col_idx, const double* vals, double* lhs, double* rhs);
+
 // Screening error model (see rerank.cu): |approx - exact| <= c1 (|x|^2 + R^2) + c2 |x| R.
 void screen_error_model(int screen, int Dp, float* c1, float* c2);
 // Relative error constant c2 of screened values formed from the fp16 high parts
