@@ -53,18 +53,16 @@ struct TcCfg
     static constexpr int B_OPER_BYTES = 2 * KATOMS * ATOM_BYTES;        // hi + lo
     static constexpr int B_STAGE_BYTES = B_OPER_BYTES + EXTRA_BYTES;    // + norm column
     // as many candidate stages as fit in 227 KB next to the A tiles, the norm
-    // slice, the barriers and the stash (at most 6)
-    static constexpr int FIXED_BYTES = EXTRA_BYTES + 256 + 8 * 32 * (8 + 1) * 4 + 1024;
+    // slice and the barriers (at most 6)
+    static constexpr int FIXED_BYTES = EXTRA_BYTES + 256 + 1024;
     static constexpr int STAGES_FIT = (227 * 1024 - A_BYTES - FIXED_BYTES) / B_STAGE_BYTES;
     static constexpr int STAGES = STAGES_FIT > 6 ? 6 : STAGES_FIT;
     static constexpr int ACC_COLS = QT * TC_N;
     static constexpr int TMEM_COLS = 2 * ACC_COLS;  // 512 or 256, power of two
     static constexpr int EPI_WARPS = 4 * QT;
-    static constexpr int STASH = 8;                 // values per lane in the slow path
     static constexpr size_t OFF_AX = (size_t)A_BYTES + (size_t)STAGES * B_STAGE_BYTES;
     static constexpr size_t OFF_BAR = OFF_AX + EXTRA_BYTES;
-    static constexpr size_t OFF_STASH = OFF_BAR + 256;
-    static constexpr size_t SMEM = OFF_STASH + (size_t)8 * 32 * (STASH + 1) * 4 + 1024 /*align*/;
+    static constexpr size_t SMEM = OFF_BAR + 256 + 1024 /*align*/;
     static_assert(STAGES >= 2, "at least two candidate stages");
 };
 
@@ -173,20 +171,6 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
 
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int t = 0; t < 16; ++t)
-        v[t] = __uint_as_float(r[t]);
-}
 
 __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float* v)
 {
@@ -303,7 +287,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t B_s = base + C::A_BYTES;
     const uint32_t AX_s = base + (uint32_t)C::OFF_AX;
     TcBarriers& Bar = *reinterpret_cast<TcBarriers*>(gbase + C::OFF_BAR);
-    float* stash_all = reinterpret_cast<float*>(gbase + C::OFF_STASH);
     volatile int* abort = &Bar.abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
