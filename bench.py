@@ -142,6 +142,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16000)
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-ltsa", action="store_true")
+    ap.add_argument("--no-eigen", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--check-connectivity", type=int, default=0)
@@ -291,6 +292,31 @@ def main():
                 "nnz": int(linf[-1].nnz)}
         del Xl
 
+    # eigensolver on the operator (row (f)): the smallest eigenpairs of the LLE
+    # matrix M of the lifted roll at N=20000 (D=64, k=16), the embedding step that
+    # follows the stage. A host-driven loop of block products, so it is timed by
+    # wall clock around the call (the call synchronises before it returns).
+    eigen = None
+    if not args.no_eigen:
+        Xe = torch.from_numpy(datasets.lifted_swiss_roll(20_000, 64, seed=1)).cuda()
+        ope = ctx.local_operator(Xe, "lle", num_neighbors=16, klle_shift=1e-3, check_connectivity=False)
+        rp_d, col_d, val_d = ope.row_ptr, ope.col_idx, ope.vals  # device tensors (X is on the device)
+        ctx.smallest_eigenvectors(rp_d, col_d, val_d, 2, 1)  # warm-up
+        et, einf = [], None
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, lam_e, einf = ctx.smallest_eigenvectors(rp_d, col_d, val_d, 2, 1, return_info=True)
+            et.append((time.perf_counter() - t0) * 1e3)
+        ems = float(np.mean(et))
+        eigen = {"workload": "smallest 2 eigenpairs after skip 1 of the LLE M, lifted roll N=20000 D=64 k=16",
+                 "ms": ems, "block_products": int(einf["matvecs"]), "rounds": int(einf["iterations"]),
+                 "block": int(einf["block"]), "us_per_block_product": 1e3 * ems / max(1, einf["matvecs"]),
+                 "max_residual": einf["max_residual"], "spectrum_bound": einf["spectrum_bound"],
+                 "eigenvalues": [float(v) for v in np.asarray(lam_e.cpu() if hasattr(lam_e, "cpu") else lam_e)],
+                 "nnz": int(rp_d[-1].item())}
+        del Xe, ope
+
     # batched uneven problems: one captured CUDA graph vs one launch sequence per
     # problem through the single-problem entry point (same GPU, same screen)
     batch = None
@@ -370,7 +396,7 @@ def main():
             "vs_baseline": None, "dtype": "fp16x3-split screen / f32+float-float re-rank and weights",
             "data": "synthetic (seeded lifted Swiss roll)", "config": workload, "stage_ms": stage,
             "rows_uncertified": int(info.rows_uncertified), "nnz": nnz, "k_used": kk,
-            "fp32_path": fp32, "ltsa": ltsa, "batch": batch, "roofline": roofline,
+            "fp32_path": fp32, "ltsa": ltsa, "eigen": eigen, "batch": batch, "roofline": roofline,
             "e2e": {"value": args.n / (e2e_ms / 1000.0), "unit": "points/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clocks, "gpu_launches": int(launches)}

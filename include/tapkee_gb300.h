@@ -46,7 +46,9 @@ typedef enum tk_status
     TK_ERR_BUFFER_TOO_SMALL = 7, /* output capacity below the required size       */
     TK_ERR_UNSUPPORTED = 8,      /* unsupported_method_error                       */
     TK_ERR_NO_DEVICE = 9,        /* no usable sm_103a device                       */
-    TK_ERR_INTERNAL = 10         /* an internal consistency check failed           */
+    TK_ERR_INTERNAL = 10,        /* an internal consistency check failed           */
+    TK_ERR_NOT_CONVERGED = 11    /* eigendecomposition_error (the eigensolver did
+                                    not reach its tolerance)                       */
 } tk_status;
 
 typedef enum tk_dtype
@@ -223,6 +225,37 @@ int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t
 int tk_eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_t N, int D, int64_t ldx,
                          const int64_t* row_ptr, const int32_t* col_idx, const double* vals, double* lhs,
                          double* rhs);
+
+/* Result summary of tk_smallest_eigenvectors. */
+typedef struct tk_eig_info
+{
+    int32_t iterations;     /* filter + Rayleigh-Ritz rounds                      */
+    int32_t block;          /* subspace width (32)                                 */
+    int64_t matvecs;        /* block products with M                               */
+    double spectrum_bound;  /* upper bound B of the spectrum used by the filter    */
+    double max_residual;    /* max over returned pairs of ||M v - lambda v||       */
+    int32_t converged;      /* 1 when every wanted pair met tol * B                */
+    float ms;               /* wall time of the call                               */
+} tk_eig_info;
+
+/* The target_dimension smallest eigenpairs of the symmetric positive
+ * semi-definite CSR matrix M after skipping the `skip` smallest: replaces
+ * eigendecomposition(Arpack, SmallestEigenvalues, M, td) with skip = 1, the
+ * last step of KLLE / KLTSA embed() (routines/eigendecomposition.hpp:31-50,
+ * 252-266, 330-345; methods/kernel_locally_linear_embedding.hpp:27). M is the
+ * CSR of tk_assemble / tk_operator_copy (row_ptr N + 1, col_idx and vals
+ * row_ptr[N]); it must be symmetric (both triangles stored). Chebyshev-filtered
+ * subspace iteration on the GPU; stops when every wanted pair has
+ * ||M v - lambda v|| <= tol * B (tol <= 0: 1e-12), B an upper bound of the
+ * spectrum, or after max_matvecs block products (<= 0: 200000), returning
+ * TK_ERR_NOT_CONVERGED with the current iterate written. vectors is N x td
+ * column-major (the reference's DenseMatrix), each vector's entry of largest
+ * magnitude positive; values (td) ascending. Needs td + skip <= 14 and
+ * N >= 128 (four block widths); smaller problems belong to a dense solver.
+ * All pointers may be host or device memory; info may be NULL. */
+int tk_smallest_eigenvectors(tk_ctx* ctx, int64_t N, const int64_t* row_ptr, const int32_t* col_idx,
+                             const double* vals, int target_dimension, int skip, double tol, int64_t max_matvecs,
+                             double* vectors, double* values, tk_eig_info* info);
 
 /* The whole stage of KernelLocallyLinearEmbeddingImplementation::embed /
  * KernelLocalTangentSpaceAlignmentImplementation::embed up to the eigensolver

@@ -24,6 +24,7 @@ TK_ERR_NO_DEVICE = 9
 TK_PAIR_NPE = 0
 TK_PAIR_LLTSA = 1
 TK_ERR_INTERNAL = 10
+TK_ERR_NOT_CONVERGED = 11
 
 TK_F32, TK_F64 = 0, 1
 TK_NOALLOC_MAX_POINTS = 2097152
@@ -73,6 +74,18 @@ class tk_operator_info(ctypes.Structure):
     ]
 
 
+class tk_eig_info(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int32),
+        ("block", ctypes.c_int32),
+        ("matvecs", ctypes.c_int64),
+        ("spectrum_bound", ctypes.c_double),
+        ("max_residual", ctypes.c_double),
+        ("converged", ctypes.c_int32),
+        ("ms", ctypes.c_float),
+    ]
+
+
 # Every symbol the header declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -94,6 +107,8 @@ SIGNATURES = {
     "tk_ltsa_basis": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _I, _P]),
     "tk_assemble": (_I, [_P, _I, _I64, _I, _I, _P, _P, _D, _P, _P, _P, ctypes.POINTER(_I64)]),
     "tk_eigenproblem_pair": (_I, [_P, _I, _P, _I, _I64, _I, _I64, _P, _P, _P, _P, _P]),
+    "tk_smallest_eigenvectors": (_I, [_P, _I64, _P, _P, _P, _I, _I, _D, _I64, _P, _P,
+                                      ctypes.POINTER(tk_eig_info)]),
     "tk_local_operator": (_I, [_P, ctypes.POINTER(tk_params), _P, _I, _I64, _I, _I64,
                                ctypes.POINTER(tk_operator_info)]),
     "tk_operator_copy": (_I, [_P, _P, _P, _P, _P, _P]),

@@ -76,6 +76,7 @@ _STATUS_EXC = {
     C.TK_ERR_UNSUPPORTED: UnsupportedMethodError,
     C.TK_ERR_NO_DEVICE: DeviceError,
     C.TK_ERR_INTERNAL: DeviceError,
+    C.TK_ERR_NOT_CONVERGED: EigendecompositionError,
 }
 
 METHODS = {
@@ -311,6 +312,33 @@ class Context:
         # column-major D x D -> [a, b]
         return lhs.reshape(D, D).T.copy(), rhs.reshape(D, D).T.copy()
 
+    def smallest_eigenvectors(self, row_ptr, col_idx, vals, target_dimension, skip=1, tol=None, max_matvecs=None,
+                              return_info=False):
+        """The target_dimension smallest eigenpairs of the symmetric CSR matrix M
+        after skipping `skip` (eigendecomposition(Arpack, SmallestEigenvalues, M, td),
+        routines/eigendecomposition.hpp:31-50,252-266): Chebyshev-filtered subspace
+        iteration on the GPU. Returns (vectors N x td, values td), each vector's
+        entry of largest magnitude positive; raises EigendecompositionError when the
+        residual does not reach tol * B within max_matvecs block products."""
+        rp = _Buf(np.ascontiguousarray(np.asarray(row_ptr, dtype=np.int64)), "np") if not _is_torch(row_ptr) \
+            else _Buf(row_ptr.to(_torch().int64).contiguous(), "torch")
+        N = int(rp.arr.shape[0]) - 1
+        ci = _as_index(col_idx, rp)
+        vb = _as_f64(vals)
+        td = int(target_dimension)
+        vec = _empty((td, N), np.float64, rp)
+        lam = _empty((td,), np.float64, rp)
+        info = C.tk_eig_info()
+        self._check(self.lib.tk_smallest_eigenvectors(self.ptr, N, rp.ptr, ci.ptr, vb.ptr, td, int(skip),
+                                                      float(tol or 0.0), int(max_matvecs or 0), vec.ptr, lam.ptr,
+                                                      ctypes.byref(info)))
+        out = (vec.arr.T, lam.arr)
+        if return_info:
+            return out + ({"iterations": info.iterations, "block": info.block, "matvecs": info.matvecs,
+                           "spectrum_bound": info.spectrum_bound, "max_residual": info.max_residual,
+                           "converged": bool(info.converged), "ms": info.ms},)
+        return out
+
     def local_operator(self, X, method="lle", num_neighbors=5, target_dimension=2, klle_shift=1e-3,
                        nullspace_shift=1e-9, check_connectivity=True, screen="tensor", cancel_function=None,
                        copy_out=True):
@@ -367,15 +395,28 @@ def default_context() -> Context:
 # ---------------------------------------------------------------- eigensolver
 
 
-def smallest_eigenvectors(op: LocalOperator, target_dimension: int, skip: int = 1, eigen_method: str = "dense"):
-    """Consumes the CSR of M unchanged: the eigenvectors of the target_dimension
-    smallest eigenvalues after skipping `skip` (routines/eigendecomposition.hpp:56-87,
-    dense path: symmetrise, self-adjoint solve, columns skip..skip+td). Runs on
-    the GPU in FP64."""
-    torch = _torch()
-    if eigen_method != "dense":
-        raise UnsupportedMethodError(f"eigen_method {eigen_method!r} is not provided (use 'dense')")
+def smallest_eigenvectors(op: LocalOperator, target_dimension: int, skip: int = 1, eigen_method: str = "arpack",
+                          context=None):
+    """Consumes the CSR of M unchanged and returns (vectors N x td, values td) as
+    numpy arrays: the eigenvectors of the target_dimension smallest eigenvalues
+    after skipping `skip`.
+    - "arpack", the reference default (defines/methods.hpp:198): the GPU
+      Chebyshev-filtered subspace iteration of tk_smallest_eigenvectors
+      (routines/eigendecomposition.hpp:31-50,252-266). Problems smaller than four
+      block widths go to the dense solver below.
+    - "dense" (routines/eigendecomposition.hpp:56-87): symmetrise, self-adjoint
+      solve of the dense N x N matrix on the GPU in FP64, columns skip..skip+td."""
+    if eigen_method not in ("arpack", "dense"):
+        raise UnsupportedMethodError(f"eigen_method {eigen_method!r} is not provided (use 'arpack' or 'dense')")
     n = len(op.row_ptr) - 1
+    if eigen_method == "arpack":
+        if n >= 128 and target_dimension + skip <= 14:
+            ctx = context or default_context()
+            E, w = ctx.smallest_eigenvectors(op.row_ptr, op.col_idx, op.vals, target_dimension, skip)
+            if _is_torch(E):
+                E, w = E.cpu().numpy(), w.cpu().numpy()
+            return np.ascontiguousarray(E), np.asarray(w)
+    torch = _torch()
     dev = "cuda"
     rp = torch.as_tensor(np.asarray(op.row_ptr.cpu() if _is_torch(op.row_ptr) else op.row_ptr)).to(dev)
     ci = torch.as_tensor(np.asarray(op.col_idx.cpu() if _is_torch(op.col_idx) else op.col_idx)).to(dev)
@@ -386,7 +427,7 @@ def smallest_eigenvectors(op: LocalOperator, target_dimension: int, skip: int = 
         w, V = torch.linalg.eigh(M)
     except Exception as e:  # pragma: no cover
         raise EigendecompositionError(str(e))
-    return V[:, skip:skip + target_dimension], w[skip:skip + target_dimension]
+    return V[:, skip:skip + target_dimension].cpu().numpy(), w[skip:skip + target_dimension].cpu().numpy()
 
 
 # ---------------------------------------------------------------- reference-shaped entry points
@@ -417,8 +458,8 @@ def embed(data, method="lle", neighbors_method=None, eigen_method=None, num_neig
                             nullspace_shift=1e-9 if nullspace_shift is None else nullspace_shift,
                             check_connectivity=True if check_connectivity is None else bool(check_connectivity),
                             screen=screen)
-    E, _ = smallest_eigenvectors(op, td, 1, eigen_method or "dense")
-    return E.cpu().numpy()
+    E, _ = smallest_eigenvectors(op, td, 1, eigen_method or "arpack", ctx)
+    return E
 
 
 @dataclass
@@ -447,8 +488,8 @@ class ParametersInitializedState:
                                 nullspace_shift=p.get("nullspace_shift", 1e-9),
                                 check_connectivity=p.get("check_connectivity", True),
                                 screen=p.get("screen", "tensor"), cancel_function=p.get("cancel_function"))
-        E, _ = smallest_eigenvectors(op, td, 1, p.get("eigen_method", "dense"))
-        return TapkeeOutput(E.cpu().numpy(), op)
+        E, _ = smallest_eigenvectors(op, td, 1, p.get("eigen_method", "arpack"), ctx)
+        return TapkeeOutput(E, op)
 
     embedUsing = embed_using
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -537,6 +538,60 @@ int tk_eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_
         if (rh)
             copy_back(ctx, rhs, r_d, (size_t)D * D);
         TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int tk_smallest_eigenvectors(tk_ctx* ctx, int64_t N, const int64_t* row_ptr, const int32_t* col_idx,
+                             const double* vals, int target_dimension, int skip, double tol, int64_t max_matvecs,
+                             double* vectors, double* values, tk_eig_info* info)
+{
+    return guarded(ctx, [&] {
+        if (N <= 0)
+            throw Error(TK_ERR_NO_DATA, "No data");
+        if (!row_ptr || !col_idx || !vals || !vectors || !values || target_dimension < 1 || skip < 0)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        const int bw = eigen_block_width(target_dimension, skip);
+        if (bw == 0)
+            throw Error(TK_ERR_UNSUPPORTED, "the sparse eigensolver takes target_dimension + skip <= 14");
+        if (N < 4 * (int64_t)bw)
+            throw Error(TK_ERR_INVALID_ARG, "the sparse eigensolver needs N >= " + std::to_string(4 * bw) +
+                                                " points; use a dense eigensolver");
+        const auto t0 = std::chrono::steady_clock::now();
+        int64_t nnz = 0;
+        if (is_device_ptr(row_ptr))
+        {
+            TK_CUDA(cudaMemcpyAsync(ctx->host_i64, row_ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            TK_CUDA(cudaStreamSynchronize(ctx->stream));
+            nnz = ctx->host_i64[0];
+        }
+        else
+            nnz = row_ptr[N];
+        if (nnz < 0)
+            throw Error(TK_ERR_INVALID_ARG, "row_ptr[N] < 0");
+        const int64_t* rp_d = device_array(ctx, row_ptr, (size_t)N + 1, "io.eig_rp");
+        const int32_t* c_d = device_array(ctx, col_idx, (size_t)std::max<int64_t>(nnz, 1), "io.eig_col");
+        const double* v_d = device_array(ctx, vals, (size_t)std::max<int64_t>(nnz, 1), "io.eig_val");
+        bool vh = false, lh = false;
+        double* vec_d = device_out(ctx, vectors, (size_t)N * target_dimension, "io.eig_vec", &vh);
+        double* val_d = device_out(ctx, values, (size_t)target_dimension, "io.eig_lam", &lh);
+        tk_eig_info inf{};
+        smallest_eigenvectors(ctx, N, nnz, rp_d, c_d, v_d, target_dimension, skip, tol > 0 ? tol : 1e-12,
+                              max_matvecs > 0 ? max_matvecs : 200000, vec_d, val_d, &inf);
+        check_device_errors(ctx);
+        if (vh)
+            copy_back(ctx, vectors, vec_d, (size_t)N * target_dimension);
+        if (lh)
+            copy_back(ctx, values, val_d, (size_t)target_dimension);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+        inf.ms = (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (info)
+            *info = inf;
+        log(ctx, TK_LOG_INFO,
+            "eigensolver: " + std::to_string(inf.iterations) + " rounds, " + std::to_string(inf.matvecs) +
+                " block products, residual " + std::to_string(inf.max_residual));
+        if (!inf.converged)
+            throw Error(TK_ERR_NOT_CONVERGED, "eigendecomposition failed: the residual stayed above tol * B");
     });
 }
 

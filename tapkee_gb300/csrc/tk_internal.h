@@ -233,6 +233,14 @@ void assemble_write(tk_ctx* ctx, int method, int64_t N, int k, int td, const int
 void eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_t N, int D, int64_t ldx,
                        const int64_t* row_ptr, const int32_t* col_idx, const double* vals, double* lhs, double* rhs);
 
+// eigen.cu: smallest eigenpairs of a symmetric CSR matrix (device pointers;
+// vectors N x td column-major, values td). eigen_block_width gives the subspace
+// width for td + skip, 0 when unsupported.
+int eigen_block_width(int td, int skip);
+void smallest_eigenvectors(tk_ctx* ctx, int64_t N, int64_t nnz, const int64_t* row_ptr, const int32_t* col_idx,
+                           const double* vals, int td, int skip, double tol, int64_t max_matvecs, double* vectors,
+                           double* values, tk_eig_info* info);
+
 // Screening error model (see rerank.cu): |approx - exact| <= c1 (|x|^2 + R^2) + c2 |x| R.
 void screen_error_model(int screen, int Dp, float* c1, float* c2);
 // Relative error constant c2 of screened values formed from the fp16 high parts
