@@ -11,10 +11,11 @@
  * It mirrors tapkee::with(ParametersSet) / ParametersInitializedState
  * (chain_interface.hpp:401-480) and the keywords of defines/keywords.hpp for the
  * parameters this stage reads, with the reference's exception types
- * (exceptions.hpp:14-91). Where the reference's embedUsing(DenseMatrix) goes on
- * to the eigensolver, buildOperatorUsing stops at the sparse alignment matrix M
- * (CSR, symmetric) and hands it back with the neighbours and weights, so the
- * caller's own eigensolver consumes it unchanged.
+ * (exceptions.hpp:14-91). embedUsing(X, D, N) runs the whole of the reference's
+ * embedUsing(DenseMatrix) for these methods, eigensolver included (the GPU
+ * solver of tk_smallest_eigenvectors in place of ARPACK). buildOperatorUsing
+ * stops at the sparse alignment matrix M (CSR, symmetric) and hands it back with
+ * the neighbours and weights, for a caller with its own eigensolver.
  *
  * Header-only; link against libtapkee_gb300.so.
  */
@@ -68,6 +69,11 @@ class multiple_parameter_error : public std::runtime_error
 public:
     explicit multiple_parameter_error(const std::string& m) : std::runtime_error(m) {}
 };
+class eigendecomposition_error : public std::runtime_error
+{
+public:
+    explicit eigendecomposition_error(const std::string& m) : std::runtime_error(m) {}
+};
 /* No counterpart in the reference: the GPU, its driver or a bounded device wait failed. */
 class device_error : public std::runtime_error
 {
@@ -93,6 +99,8 @@ inline void throw_status(int status, const std::string& message)
         throw cancelled_exception();
     case TK_ERR_UNSUPPORTED:
         throw unsupported_method_error(message);
+    case TK_ERR_NOT_CONVERGED:
+        throw eigendecomposition_error(message);
     default:
         throw device_error(std::string(tk_status_string(status)) + ": " + message);
     }
@@ -245,6 +253,19 @@ struct LocalOperator
     tk_operator_info info{};
 };
 
+/* embedUsing's result, the embedding part of the reference's TapkeeOutput
+ * (defines/types.hpp): N x target_dimension, column-major like its DenseMatrix,
+ * with the eigenvalues of M for those columns. */
+struct TapkeeOutput
+{
+    int64_t n = 0;
+    int target_dimension = 0;
+    std::vector<double> embedding;
+    std::vector<double> eigenvalues;
+    tk_operator_info info{};
+    tk_eig_info eigen{};
+};
+
 /* ---- context and chain -------------------------------------------------------- */
 
 /* One GPU context (stream + scratch); reused by every call made through it. */
@@ -288,8 +309,16 @@ public:
     LocalOperator buildOperatorUsing(const double* X, int64_t D, int64_t N) const { return run(X, TK_F64, D, N); }
     LocalOperator buildOperatorUsing(const float* X, int64_t D, int64_t N) const { return run(X, TK_F32, D, N); }
 
+    /* embedUsing(DenseMatrix) (chain_interface.hpp:471-480) for these methods: the
+     * operator, then the target_dimension smallest eigenvectors of M after the
+     * first (eigendecomposition(SmallestEigenvalues, M, td),
+     * methods/kernel_locally_linear_embedding.hpp:27) with the GPU eigensolver,
+     * reading M where the operator left it on the device. */
+    TapkeeOutput embedUsing(const double* X, int64_t D, int64_t N) const { return embed(X, TK_F64, D, N); }
+    TapkeeOutput embedUsing(const float* X, int64_t D, int64_t N) const { return embed(X, TK_F32, D, N); }
+
 private:
-    LocalOperator run(const void* X, int dtype, int64_t D, int64_t N) const
+    std::shared_ptr<Context> checked_context(int64_t D) const
     {
         if (!(params_.given & detail::P_METHOD))
             throw unsupported_method_error("only KernelLocallyLinearEmbedding and "
@@ -298,7 +327,30 @@ private:
             throw unsupported_method_error("only the Brute neighbours method runs on this path");
         if (D < 1 || D > 0x7fffffff)
             throw wrong_parameter_error("feature dimension out of range");
-        std::shared_ptr<Context> c = ctx_ ? ctx_ : std::make_shared<Context>(0);
+        return ctx_ ? ctx_ : std::make_shared<Context>(0);
+    }
+
+    TapkeeOutput embed(const void* X, int dtype, int64_t D, int64_t N) const
+    {
+        std::shared_ptr<Context> c = checked_context(D);
+        TapkeeOutput out;
+        c->check(tk_local_operator(c->get(), &params_.values, X, dtype, N, (int)D, D, &out.info));
+        const int64_t* rp = nullptr;
+        const int32_t* col = nullptr;
+        const double* vals = nullptr;
+        c->check(tk_operator_device_views(c->get(), nullptr, nullptr, &rp, &col, &vals));
+        out.n = out.info.n;
+        out.target_dimension = params_.values.target_dimension;
+        out.embedding.resize((size_t)out.n * (size_t)out.target_dimension);
+        out.eigenvalues.resize((size_t)out.target_dimension);
+        c->check(tk_smallest_eigenvectors(c->get(), out.n, rp, col, vals, out.target_dimension, 1, 0.0, 0,
+                                          out.embedding.data(), out.eigenvalues.data(), &out.eigen));
+        return out;
+    }
+
+    LocalOperator run(const void* X, int dtype, int64_t D, int64_t N) const
+    {
+        std::shared_ptr<Context> c = checked_context(D);
         LocalOperator op;
         c->check(tk_local_operator(c->get(), &params_.values, X, dtype, N, (int)D, D, &op.info));
         op.n = op.info.n;

@@ -111,6 +111,14 @@ int gpu_run(const char* xpath, long long N, int D, const std::string& prefix)
     CHECK(throws<no_data_error>([&] {
         with((method = KernelLocallyLinearEmbedding, num_neighbors = 5)).onContext(ctx).buildOperatorUsing(X.data(), D, 0);
     }));
+    // embedUsing: the operator and the GPU eigensolver (2 columns after the first)
+    TapkeeOutput emb = with((method = KernelLocallyLinearEmbedding, neighbors_method = Brute, num_neighbors = 12,
+                             klle_shift = 1e-3))
+                           .onContext(ctx)
+                           .embedUsing(X.data(), D, N);
+    CHECK(emb.n == N && emb.target_dimension == 2 && emb.embedding.size() == (size_t)N * 2);
+    CHECK(emb.eigen.converged == 1 && emb.eigenvalues[0] <= emb.eigenvalues[1]);
+    dump(prefix + "embedding.bin", emb.embedding);
     // LTSA through the same chain
     LocalOperator lt = with((method = KernelLocalTangentSpaceAlignment, num_neighbors = 12, target_dimension = 2))
                            .onContext(ctx)

@@ -58,3 +58,8 @@ def test_facade_lle_c1_matches_oracle(facade_bin, golden, tmp_path):
     rp_ref, col_ref, vals_ref = oracle.assemble(0, idx, W_ref, 1e-9)
     assert np.array_equal(rp, rp_ref) and np.array_equal(col, col_ref)
     assert np.abs(vals - vals_ref).max() / np.abs(vals_ref).max() < 1e-5
+    # embedUsing: N x 2 column-major embedding, the golden dense-oracle subspace
+    E = np.fromfile(prefix + "embedding.bin", np.float64).reshape(2, 2000).T
+    qa, _ = np.linalg.qr(E)
+    qb, _ = np.linalg.qr(golden["lle_embedding"])
+    assert np.arccos(np.clip(np.linalg.svd(qa.T @ qb, compute_uv=False), -1, 1)).max() < 1e-4
