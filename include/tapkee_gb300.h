@@ -281,6 +281,13 @@ int tk_operator_device_views(tk_ctx* ctx, const int32_t** idx, const double** we
 /* Information about the operator held by ctx. */
 int tk_operator_get_info(const tk_ctx* ctx, tk_operator_info* info);
 
+/* Failure-path self-test: one CTA waits, with the distance screen's own bounded
+ * mbarrier wait (2 s limit), on a barrier that nothing arrives at. The wait
+ * expires, the kernel records the device-side timeout and returns, and the call
+ * returns TK_ERR_TIMEOUT with *outcome = 1 (2 would mean the wait completed).
+ * The context stays usable. No counterpart in the reference. */
+int tk_selftest_bounded_wait(tk_ctx* ctx, int* outcome);
+
 /* Waits for all work queued on the context's stream. */
 int tk_ctx_synchronize(tk_ctx* ctx);
 

@@ -226,7 +226,13 @@ class Context:
             self._check(self.lib.tk_set_log_callback(self.ptr, C.LOG_FN(), None))
             return
         self._log_cb = C.LOG_FN(lambda lvl, msg, user: fn(lvl, msg.decode()))
+        self._log_fn = fn
         self._check(self.lib.tk_set_log_callback(self.ptr, self._log_cb, None))
+
+    def _log(self, level, message):
+        fn = getattr(self, "_log_fn", None)
+        if fn is not None:
+            fn(level, message)
 
     # -- stages ---------------------------------------------------------------
     def knn_brute(self, X, k, screen="tensor", return_distances=False, return_stats=False):
@@ -245,6 +251,38 @@ class Context:
         if return_stats:
             out.append({"rows_uncertified": st.rows_uncertified, "candidates": st.candidates})
         return out[0] if len(out) == 1 else tuple(out)
+
+    def find_neighbors(self, X, k, check_connectivity=True, screen="tensor", return_distances=False):
+        """find_neighbors with neighbors_method=Brute (neighbors/neighbors.hpp:173-213)
+        for any caller of the brute kNN, including the plain-distance ones (Isomap,
+        Laplacian Eigenmaps, LPP, SPE, Manifold Sculpting; callbacks/eigen_callbacks.hpp:52-64):
+        k above N - 1 is clamped with a warning, and while the graph is not connected
+        (is_connected, neighbors/connected.hpp:19-62) the search is redone with 2k.
+        The ranking is by the exact squared Euclidean distance, which orders both the
+        kernel-trick and the plain distance. Returns (idx N x k_used, k_used) or, with
+        return_distances, (idx, distances N x k_used = sqrt(d2), k_used)."""
+        xb, _ = _as_points(X)
+        N = int(xb.arr.shape[0])
+        if N < 2:
+            raise WrongParameterError("at least 2 points are needed to find neighbours")
+        k = int(k)
+        if k < 1:
+            raise WrongParameterError(f"num_neighbors {k} must be at least 1")
+        if k > N - 1:
+            self._log(1, "Number of neighbors is greater than number of objects to embed. "
+                         "Using greatest possible number of neighbors.")
+            k = N - 1
+        while True:
+            idx, d2 = self.knn_brute(X, k, screen=screen, return_distances=True)
+            if not check_connectivity or self.check_connected(idx) or k >= N - 1:
+                break
+            self._log(1, f"The neighborhood graph with {k} neighbors is not connected. "
+                         f"Recomputing with a larger number of neighbors {min(2 * k, N - 1)}.")
+            k = min(2 * k, N - 1)
+        if return_distances:
+            dist = d2.sqrt() if _is_torch(d2) else np.sqrt(d2)
+            return idx, dist, k
+        return idx, k
 
     def check_connected(self, idx):
         """Reachability of all vertices from vertex 0 (neighbors/connected.hpp:19-62)."""

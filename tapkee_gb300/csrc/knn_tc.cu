@@ -1388,6 +1388,41 @@ void launch_single(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* can
 
 } // namespace
 
+namespace {
+
+// Self-test of the bounded wait: thread 0 waits, with the screen's own mbar_wait
+// and limit, on a shared-memory mbarrier that expects one arrival nobody makes.
+// After WAIT_LIMIT_NS the wait gives up, raises DEV_ERR_TIMEOUT and the kernel
+// returns; *outcome is 1 for that and 2 if the phase had completed (it cannot).
+// No copy, MMA or TMEM allocation is involved, so nothing is left to drain.
+__global__ void k_wait_selftest(unsigned* err, int* outcome)
+{
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x != 0)
+        return;
+    abort_flag = 0;
+    const uint32_t b = smem_u32(&bar);
+    mbar_init(b, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const bool done = mbar_wait(b, 0, &abort_flag, err);
+    *outcome = done ? 2 : 1;
+}
+
+} // namespace
+
+int wait_selftest(tk_ctx* ctx)
+{
+    int* d = (int*)ctx->scratch.get("selftest.outcome", sizeof(int));
+    TK_CUDA(cudaMemsetAsync(d, 0, sizeof(int), ctx->stream));
+    k_wait_selftest<<<1, 32, 0, ctx->stream>>>(ctx->dev_err, d);
+    TK_CHECK_LAUNCH();
+    int h = 0;
+    TK_CUDA(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return h;
+}
+
 bool tensor_screen_supported(int Dp) { return Dp == 64 || Dp == 128; }
 
 void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int k, int32_t* cand_idx, float* cand_val)

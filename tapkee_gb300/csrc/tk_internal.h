@@ -233,6 +233,10 @@ void assemble_write(tk_ctx* ctx, int method, int64_t N, int k, int td, const int
 void eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_t N, int D, int64_t ldx,
                        const int64_t* row_ptr, const int32_t* col_idx, const double* vals, double* lhs, double* rhs);
 
+// knn_tc.cu: one bounded mbarrier wait that nothing satisfies (the screen's wait
+// helper); returns 1 when it expired as designed, 2 if it completed.
+int wait_selftest(tk_ctx* ctx);
+
 // eigen.cu: smallest eigenpairs of a symmetric CSR matrix (device pointers;
 // vectors N x td column-major, values td). eigen_block_width gives the subspace
 // width for td + skip, 0 when unsupported.

@@ -1,0 +1,34 @@
+"""The failure path of the bounded device waits, made to run out on purpose
+without faulting the GPU: one CTA waits with the distance screen's own wait
+helper on an mbarrier that nothing arrives at. The wait gives up after its
+limit, the kernel records the timeout and returns, the host reads TK_ERR_TIMEOUT,
+and the context keeps working afterwards."""
+import ctypes
+import time
+
+import numpy as np
+import pytest
+
+import tapkee_gb300 as tk
+from tapkee_gb300 import _capi as C
+from tapkee_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+
+
+def test_bounded_wait_expires_and_context_survives(ctx, golden):
+    outcome = ctypes.c_int(0)
+    t0 = time.perf_counter()
+    st = ctx.lib.tk_selftest_bounded_wait(ctx.ptr, ctypes.byref(outcome))
+    elapsed = time.perf_counter() - t0
+    assert st == C.TK_ERR_TIMEOUT
+    assert outcome.value == 1  # the wait expired; it did not complete
+    assert "bounded wait expired" in ctx.lib.tk_last_error(ctx.ptr).decode()
+    assert 1.5 < elapsed < 30.0  # the 2 s limit, not a hang
+    # the error word was cleared and the context still computes the right thing
+    X = datasets.swiss_roll(2000, seed=0)
+    op = ctx.local_operator(X, "lle", num_neighbors=12, klle_shift=1e-3)
+    assert np.array_equal(op.idx, golden["lle_idx"])
+    # and through the Python error mapping
+    with pytest.raises(tk.DeviceError, match="bounded wait expired"):
+        ctx._check(ctx.lib.tk_selftest_bounded_wait(ctx.ptr, None))

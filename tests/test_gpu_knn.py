@@ -116,3 +116,28 @@ def test_wide_screen_tail_blocks_split_in_eight(ctx):
     a = ctx.knn_brute(X, 16, screen="tensor")
     b = ctx.knn_brute(X, 16, screen="fp32")
     assert np.array_equal(a, b)
+
+
+def test_find_neighbors_for_plain_distance_callers(ctx):
+    """find_neighbors (neighbors/neighbors.hpp:173-213) as the plain-distance
+    callers (Isomap, Laplacian Eigenmaps, LPP, SPE, Manifold Sculpting) use it:
+    the connectivity retry and the k clamp of the reference, and distances equal
+    to eigen_distance_callback's (x_a - x_b).norm() (callbacks/eigen_callbacks.hpp:52-64)."""
+    rng = np.random.default_rng(0)
+    X = np.concatenate([rng.normal(size=(60, 2)), rng.normal(size=(60, 2)) + 100.0])
+    msgs = []
+    ctx.set_logger(lambda lvl, m: msgs.append((lvl, m)))
+    try:
+        idx, dist, k = ctx.find_neighbors(X, 5, return_distances=True)
+        idx_small, k_small = ctx.find_neighbors(X[:8], 20)
+    finally:
+        ctx.set_logger(None)
+    ref_idx, k_ref = oracle.find_neighbors(X, 5)
+    assert k == k_ref == 80
+    assert all(set(a) == set(b) for a, b in zip(idx.tolist(), ref_idx.tolist()))
+    plain = np.linalg.norm(X[:, None, :] - X[idx], axis=2)
+    assert np.allclose(dist, plain, rtol=1e-12, atol=1e-12)
+    assert np.all(np.diff(dist, axis=1) >= 0)
+    assert k_small == 7 and idx_small.shape == (8, 7)
+    assert any("not connected" in m for _, m in msgs)
+    assert any("greater than number of objects" in m for _, m in msgs)
