@@ -190,6 +190,19 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// 64 accumulator columns of this thread's TMEM lane together with their largest
+// value: the .red form of tcgen05.ld reduces over the loaded columns on the way
+// out of TMEM, so the filter's common case (nothing in the 64 columns passes)
+// needs no max tree. Values and maximum are valid after tmem_wait_ld().
+__device__ __forceinline__ float tmem_ld64_max_nowait(uint32_t taddr, float* v)
+{
+    float m;
+    asm volatile("tcgen05.ld.red.sync.aligned.32x32b.x64.max.f32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, %64, [%65];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]), "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]), "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31]), "=f"(v[32]), "=f"(v[33]), "=f"(v[34]), "=f"(v[35]), "=f"(v[36]), "=f"(v[37]), "=f"(v[38]), "=f"(v[39]), "=f"(v[40]), "=f"(v[41]), "=f"(v[42]), "=f"(v[43]), "=f"(v[44]), "=f"(v[45]), "=f"(v[46]), "=f"(v[47]), "=f"(v[48]), "=f"(v[49]), "=f"(v[50]), "=f"(v[51]), "=f"(v[52]), "=f"(v[53]), "=f"(v[54]), "=f"(v[55]), "=f"(v[56]), "=f"(v[57]), "=f"(v[58]), "=f"(v[59]), "=f"(v[60]), "=f"(v[61]), "=f"(v[62]), "=f"(v[63]), "=f"(m)
+                 : "r"(taddr));
+    return m;
+}
+
 __device__ __forceinline__ float fmax3(float a, float b, float c)
 {
     float r;
@@ -617,7 +630,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // instructions of two N = 128 MMAs and half the shared-memory reads of the A
 // operand per output), two 256-column accumulators double-buffered in TMEM.
 // The epilogue splits each tile's 256 columns between warps 0-3 (columns
-// 0-127) and warps 4-7 (128-255); each keeps its own top-32 per row, and the
+// 0-127) and warps 4-7 (128-255), reading 64 columns per TMEM load with the
+// load's own max reduction as the pass filter; each keeps its own top-32 per row, and the
 // two lists of a row are merged before they are written. Both half lists hold
 // their half's 32 smallest values, so the merged list is the top 32 of the
 // union and its last value bounds every candidate outside it, as the
@@ -894,8 +908,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (int h = 0; h < 2; ++h)
             {
                 float v[64];
-                tmem_ld32_nowait(tacc + h * 64, v);
-                tmem_ld32_nowait(tacc + h * 64 + 32, v + 32);
+                // the 64 columns and their largest value, from one TMEM load:
+                // one branch per 64 columns in the common case (nothing passes)
+                const float g64 = tmem_ld64_max_nowait(tacc + h * 64, v);
                 tmem_wait_ld();
                 if (h == 1)
                 {
@@ -904,17 +919,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     if (lane == 0)
                         mbar_arrive(smem_u32(&Bar.tempty[buf]));
                 }
-                // largest value of each group of 8 columns and of all 64: one
-                // branch per 64 columns in the common case (nothing passes)
-                float gm[8];
-#pragma unroll
-                for (int g = 0; g < 8; ++g)
-                {
-                    const float* w = v + g * 8;
-                    gm[g] = fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7]));
-                }
-                const float g64 =
-                    fmax3(fmax3(gm[0], gm[1], gm[2]), fmax3(gm[3], gm[4], gm[5]), fmaxf(gm[6], gm[7]));
                 if (far_tile)
                 {
                     if (!ragged)
@@ -932,10 +936,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                     for (int g = 0; g < 8; ++g)
                     {
-                        if (gm[g] > thr)
+                        const float* w = v + g * 8;
+                        if (fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7])) > thr)
                         {
                             // columns of the group that pass, then one insertion each
-                            const float* w = v + g * 8;
                             unsigned msk = 0u;
 #pragma unroll
                             for (int e = 0; e < 8; ++e)
