@@ -190,6 +190,16 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// The same for 32 columns.
+__device__ __forceinline__ float tmem_ld32_max_nowait(uint32_t taddr, float* v)
+{
+    float m;
+    asm volatile("tcgen05.ld.red.sync.aligned.32x32b.x32.max.f32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, %32, [%33];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]), "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]), "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31]), "=f"(m)
+                 : "r"(taddr));
+    return m;
+}
+
 // 64 accumulator columns of this thread's TMEM lane together with their largest
 // value: the .red form of tcgen05.ld reduces over the loaded columns on the way
 // out of TMEM, so the filter's common case (nothing in the 64 columns passes)
@@ -541,10 +551,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll 1
                 for (int h = 0; h < TC_N / CPW; ++h)
                 {
+                    // the round's columns and their largest value from one reducing
+                    // TMEM load: one branch per round when nothing passes
                     float v[CPW];
-                    tmem_ld32_nowait(tacc + h * CPW, v);
-                    if (CPW == 64)
-                        tmem_ld32_nowait(tacc + h * CPW + 32, v + 32);
+                    float gall;
+                    if constexpr (CPW == 64)
+                        gall = tmem_ld64_max_nowait(tacc + h * CPW, v);
+                    else
+                        gall = tmem_ld32_max_nowait(tacc + h * CPW, v);
                     tmem_wait_ld();
                     if (h == TC_N / CPW - 1)
                     {
@@ -554,29 +568,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         if (lane == 0)
                             mbar_arrive(smem_u32(&Bar.tempty[buf][qt]));
                     }
-                    // largest value of each group of 8 columns (3-input max) and of
-                    // the round: one branch per round when nothing passes
                     constexpr int NG = CPW / 8;
-                    float gm[NG];
-#pragma unroll
-                    for (int g = 0; g < NG; ++g)
-                    {
-                        const float* w = v + g * 8;
-                        gm[g] = fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7]));
-                    }
-                    float gall = gm[0];
-#pragma unroll
-                    for (int g = 1; g < NG; ++g)
-                        gall = fmaxf(gall, gm[g]);
                     if (gall > thr)
                     {
 #pragma unroll
                         for (int g = 0; g < NG; ++g)
                         {
-                            if (gm[g] > thr)
+                            const float* w = v + g * 8;
+                            if (fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7])) > thr)
                             {
                                 // columns of the group that pass, then one insertion each
-                                const float* w = v + g * 8;
                                 unsigned msk = 0u;
 #pragma unroll
                                 for (int e = 0; e < 8; ++e)
