@@ -79,6 +79,26 @@ def test_oracle_lle_embedding_vs_sklearn_fixture(golden):
     assert _angles(E, golden["lle_embedding_sklearn"]).max() < 1e-4
 
 
+def test_oracle_dense_eigen_path_vs_shift_invert_lanczos(golden):
+    """The eigen step of the oracle (the reference's dense path,
+    routines/eigendecomposition.hpp:56-87) on the C1 operator: the golden embedding,
+    and the same subspace as scipy's shift-invert Lanczos (ARPACK "SM" through a
+    sparse LU, the family of the reference's default Arpack path)."""
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    sp = pytest.importorskip("scipy.sparse")
+    X = datasets.swiss_roll(2000, seed=0)
+    idx = golden["lle_idx"]
+    W = oracle.lle_weights(X, idx, 1e-3)
+    rp, col, vals = oracle.assemble(0, idx, W, 1e-9)
+    E, lam = oracle.dense_embedding(rp, col, vals, 2)
+    assert _angles(E, golden["lle_embedding"]).max() < 1e-6
+    M = sp.csr_matrix((vals, col, rp), shape=(2000, 2000))
+    w, V = sla.eigsh(M, k=3, sigma=0, which="LM")
+    o = np.argsort(w)
+    assert _angles(E, V[:, o[1:3]]).max() < 1e-4
+    assert np.allclose(lam, w[o[1:3]], rtol=1e-6, atol=1e-15)
+
+
 def test_oracle_ltsa_vs_sklearn_fixture(golden):
     Xs = datasets.lifted_s_curve(1500, d=8, seed=11, noise=0.02, dtype=np.float64)
     idx = golden["ltsa_idx_oracle_order"]
