@@ -528,6 +528,8 @@ int tk_eigenproblem_pair(tk_ctx* ctx, int kind, const void* X, int dtype, int64_
         const int64_t* rp_d = device_array(ctx, row_ptr, (size_t)N + 1, "io.pair_rp");
         const int32_t* c_d = device_array(ctx, col_idx, (size_t)std::max<int64_t>(nnz, 1), "io.pair_col");
         const double* v_d = device_array(ctx, vals, (size_t)std::max<int64_t>(nnz, 1), "io.pair_val");
+        check_csr_rows(ctx, N, rp_d, nnz);
+        check_device_errors(ctx);
         bool lh = false, rh = false;
         double* l_d = device_out(ctx, lhs, (size_t)D * D, "io.pair_lhs", &lh);
         double* r_d = device_out(ctx, rhs, (size_t)D * D, "io.pair_rhs", &rh);
@@ -582,6 +584,8 @@ int tk_smallest_eigenvectors(tk_ctx* ctx, int64_t N, const int64_t* row_ptr, con
         const int64_t* rp_d = device_array(ctx, row_ptr, (size_t)N + 1, "io.eig_rp");
         const int32_t* c_d = device_array(ctx, col_idx, (size_t)std::max<int64_t>(nnz, 1), "io.eig_col");
         const double* v_d = device_array(ctx, vals, (size_t)std::max<int64_t>(nnz, 1), "io.eig_val");
+        check_csr_rows(ctx, N, rp_d, nnz);
+        check_device_errors(ctx);
         bool vh = false, lh = false;
         double* vec_d = device_out(ctx, vectors, (size_t)N * target_dimension, "io.eig_vec", &vh);
         double* val_d = device_out(ctx, values, (size_t)target_dimension, "io.eig_lam", &lh);

@@ -60,6 +60,22 @@ __device__ __forceinline__ double ff_d(float2 a)
     return (double)a.x + (double)a.y;
 }
 
+// A caller's CSR row pointers: every entry in [0, nnz] and non-decreasing, so
+// that no row range reaches outside the column and value arrays. A violation
+// raises DEV_ERR_BOUNDS (reads only rp[0..N]).
+__global__ void k_check_rows(int64_t N, const int64_t* __restrict__ rp, int64_t nnz, unsigned* err)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r <= N; r += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t a = rp[r];
+        bool bad = a < 0 || a > nnz;
+        if (r < N)
+            bad = bad || rp[r + 1] < a;
+        if (bad)
+            atomicOr(err, DEV_ERR_BOUNDS);
+    }
+}
+
 __global__ void k_vals_split(int64_t nnz, const double* __restrict__ v, float2* __restrict__ out)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x)
@@ -702,6 +718,13 @@ void run_solver(tk_ctx* ctx, const Csr& A, double bound, int td, int skip, doubl
 }
 
 } // namespace
+
+void check_csr_rows(tk_ctx* ctx, int64_t N, const int64_t* row_ptr, int64_t nnz)
+{
+    k_check_rows<<<(int)std::max<int64_t>(1, std::min<int64_t>((N + 256) / 256, 4096)), 256, 0, ctx->stream>>>(
+        N, row_ptr, nnz, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+}
 
 int eigen_block_width(int td, int skip)
 {

@@ -241,6 +241,9 @@ int wait_selftest(tk_ctx* ctx);
 // vectors N x td column-major, values td). eigen_block_width gives the subspace
 // width for td + skip, 0 when unsupported.
 int eigen_block_width(int td, int skip);
+// Checks a caller's CSR row pointers (N + 1 entries, device) against nnz: entries in
+// [0, nnz], non-decreasing; a violation raises DEV_ERR_BOUNDS for check_device_errors.
+void check_csr_rows(tk_ctx* ctx, int64_t N, const int64_t* row_ptr, int64_t nnz);
 void smallest_eigenvectors(tk_ctx* ctx, int64_t N, int64_t nnz, const int64_t* row_ptr, const int32_t* col_idx,
                            const double* vals, int td, int skip, double tol, int64_t max_matvecs, double* vectors,
                            double* values, tk_eig_info* info);

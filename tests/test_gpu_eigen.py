@@ -108,6 +108,15 @@ def test_argument_errors_and_non_convergence(ctx):
     bad[5] = len(op.row_ptr) + 3
     with pytest.raises(tk.WrongParameterError, match="index out of range"):
         ctx.smallest_eigenvectors(op.row_ptr, bad, op.vals, 2, 1)
+    # row pointers that go backwards or past row_ptr[N] are rejected before any gather
+    rp_bad = op.row_ptr.copy()
+    rp_bad[10], rp_bad[11] = rp_bad[11], rp_bad[10]
+    with pytest.raises(tk.WrongParameterError, match="index out of range"):
+        ctx.smallest_eigenvectors(rp_bad, op.col_idx, op.vals, 2, 1)
+    rp_bad = op.row_ptr.copy()
+    rp_bad[7] = rp_bad[-1] + 100
+    with pytest.raises(tk.WrongParameterError, match="index out of range"):
+        ctx.smallest_eigenvectors(rp_bad, op.col_idx, op.vals, 2, 1)
     # the context stays usable
     E, _ = ctx.smallest_eigenvectors(op.row_ptr, op.col_idx, op.vals, 2, 1)
     assert E.shape == (600, 2)

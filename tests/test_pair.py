@@ -74,3 +74,16 @@ def test_gpu_pair_device_inputs_and_wide_d(ctx):
     Lr, Rr = oracle.eigenproblem_pair(0, X.astype(np.float64), op.row_ptr, op.col_idx, op.vals)
     assert np.abs(L - Lr).max() <= 1e-10 * np.abs(Lr).max()
     assert np.abs(R - Rr).max() <= 1e-10 * np.abs(Rr).max()
+
+
+@pytest.mark.gpu
+def test_gpu_pair_rejects_bad_row_pointers(ctx):
+    import tapkee_gb300 as tk
+    X = datasets.swiss_roll(500, seed=3)
+    op = ctx.local_operator(X, "lle", num_neighbors=8, klle_shift=1e-3)
+    rp_bad = op.row_ptr.copy()
+    rp_bad[20], rp_bad[21] = rp_bad[21], rp_bad[20]
+    with pytest.raises(tk.WrongParameterError, match="index out of range"):
+        ctx.eigenproblem_pair("npe", X, rp_bad, op.col_idx, op.vals)
+    L, _ = ctx.eigenproblem_pair("npe", X, op.row_ptr, op.col_idx, op.vals)  # the context stays usable
+    assert L.shape == (3, 3)
