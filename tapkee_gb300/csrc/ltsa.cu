@@ -365,7 +365,7 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
 template <int M, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, int64_t N, int D, int64_t ldx,
                                               const int32_t* __restrict__ idx, int k, int td, double* V,
-                                              int32_t* refine, unsigned* nrefine)
+                                              int32_t* refine, unsigned* nrefine, unsigned* err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -375,7 +375,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, i
     for (int64_t i = (int64_t)blockIdx.x * WARPS + wib; i < N; i += nw)
     {
         for (int a = lane; a < k; a += 32)
-            nb_s[wib][a] = idx[i * k + a];
+        {
+            // a neighbour index outside [0, N) is reported and read as the point itself
+            int nb = idx[i * k + a];
+            if (nb < 0 || (int64_t)nb >= N)
+            {
+                atomicOr(err, DEV_ERR_BOUNDS);
+                nb = (int)i;
+            }
+            nb_s[wib][a] = nb;
+        }
         __syncwarp();
         centred_gram<M, float>(S, lane, X, dtype, ldx, D, nb_s[wib], k);
         warp_jacobi<M, float>(S, lane, 30);
@@ -448,7 +457,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, i
 template <int M>
 __global__ void __launch_bounds__(32) k_ltsa_fp64(const void* X, int dtype, int64_t N, int D, int64_t ldx,
                                                   const int32_t* __restrict__ idx, int k, int td, double* V,
-                                                  const int32_t* refine, const unsigned* nrefine)
+                                                  const int32_t* refine, const unsigned* nrefine, unsigned* err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     JacobiSmem<M, double>& S = *reinterpret_cast<JacobiSmem<M, double>*>(smem_raw);
@@ -460,7 +469,15 @@ __global__ void __launch_bounds__(32) k_ltsa_fp64(const void* X, int dtype, int6
     {
         const int64_t i = refine[r];
         for (int a = lane; a < k; a += 32)
-            nb_s[a] = idx[i * k + a];
+        {
+            int nb = idx[i * k + a];
+            if (nb < 0 || (int64_t)nb >= N)
+            {
+                atomicOr(err, DEV_ERR_BOUNDS);
+                nb = (int)i;
+            }
+            nb_s[a] = nb;
+        }
         __syncwarp();
         centred_gram<M, double>(S, lane, X, dtype, ldx, D, nb_s, k);
         warp_jacobi<M, double>(S, lane, 60);
@@ -509,11 +526,13 @@ void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx
     static_assert(sizeof(JacobiSmem<M, float>) * WARPS <= 200 * 1024, "shared memory budget");
     TK_CUDA(cudaFuncSetAttribute(k_ltsa<M, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<int64_t>((N + WARPS - 1) / WARPS, (int64_t)ctx->num_sms * 16);
-    k_ltsa<M, WARPS><<<grid, WARPS * 32, smem, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine);
+    k_ltsa<M, WARPS><<<grid, WARPS * 32, smem, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine,
+                                                     ctx->dev_err);
     TK_CHECK_LAUNCH();
     const size_t smem64 = sizeof(JacobiSmem<M, double>);
     TK_CUDA(cudaFuncSetAttribute(k_ltsa_fp64<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem64));
-    k_ltsa_fp64<M><<<ctx->num_sms * 4, 32, smem64, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine);
+    k_ltsa_fp64<M><<<ctx->num_sms * 4, 32, smem64, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine,
+                                                          ctx->dev_err);
     TK_CHECK_LAUNCH();
 }
 

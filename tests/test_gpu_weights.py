@@ -47,3 +47,20 @@ def test_ltsa_basis(ctx, n, d, k, td):
     assert _rel(_P(V, k), _P(ref, k)) < TOL
     # orthonormal columns
     assert np.abs(np.einsum("nat,nas->nts", V, V) - np.eye(td)).max() < 1e-5
+
+
+def test_out_of_range_neighbours_are_reported(ctx):
+    """A neighbour index outside [0, N) in a caller's list is reported as a bad
+    argument by both weight routines, never read."""
+    import tapkee_gb300 as tk
+    X = datasets.lifted_s_curve(800, 8, seed=5, noise=0.02)
+    idx, _, _ = oracle.knn_brute(X, 12)
+    bad = idx.copy()
+    bad[17, 3] = 800
+    bad[400, 0] = -5
+    with pytest.raises(tk.WrongParameterError, match="index out of range"):
+        ctx.ltsa_basis(X, bad, 2)
+    with pytest.raises(tk.WrongParameterError, match="index out of range"):
+        ctx.lle_weights(X, bad)
+    V = ctx.ltsa_basis(X, idx, 2)  # the context stays usable
+    assert V.shape == (800, 12, 2)
