@@ -99,6 +99,21 @@ def test_oracle_dense_eigen_path_vs_shift_invert_lanczos(golden):
     assert np.allclose(lam, w[o[1:3]], rtol=1e-6, atol=1e-15)
 
 
+def test_oracle_dense_eigen_known_answer():
+    """The reference's sparse smallest-eigenvector known answer
+    (test/unit/eigendecomposition.cpp:30-50): M = diag(1, 2, 3) from triplets,
+    SmallestEigenvalues with one vector after the skipped one gives the
+    eigenvalue 2 and a vector v with |M v - 2 v| ~ 0."""
+    rp = np.array([0, 1, 2, 3], np.int64)
+    col = np.array([0, 1, 2], np.int32)
+    vals = np.array([1.0, 2.0, 3.0])
+    E, lam = oracle.dense_embedding(rp, col, vals, 1)
+    assert E.shape == (3, 1) and lam.shape == (1,)
+    assert abs(lam[0] - 2.0) < 1e-7
+    M = np.diag(vals)
+    assert np.linalg.norm(M @ E[:, 0] - lam[0] * E[:, 0]) < 1e-7
+
+
 def test_oracle_ltsa_vs_sklearn_fixture(golden):
     Xs = datasets.lifted_s_curve(1500, d=8, seed=11, noise=0.02, dtype=np.float64)
     idx = golden["ltsa_idx_oracle_order"]
