@@ -10,7 +10,9 @@ LLE weights (routines/locally_linear.hpp:90-159), LTSA tangent basis
 (routines/locally_linear.hpp:20-88) and triplet assembly (utils/sparse.hpp:16-21).
 Parity status: kNN sets pinned by the reference's 1-D line known-answer test;
 W / M / LTSA values unpinned by the reference (it has no golden values for them)
-and cross-checked against scikit-learn fixtures in tests/golden/.
+and cross-checked against scikit-learn fixtures in tests/golden/. The dense
+eigen step (dense_embedding) reproduces the reference's sparse
+smallest-eigenvector known answer (test/unit/eigendecomposition.cpp:30-50).
 """
 from __future__ import annotations
 
