@@ -7,7 +7,8 @@ baseline / reference arm may import this module. The product path
 The oracle restates, in FP64, the reference's brute kNN
 (neighbors/neighbors.hpp:119-149), connectivity DFS (neighbors/connected.hpp:19-62),
 LLE weights (routines/locally_linear.hpp:90-159), LTSA tangent basis
-(routines/locally_linear.hpp:20-88) and triplet assembly (utils/sparse.hpp:16-21).
+(routines/locally_linear.hpp:20-88), Hessian LLE blocks
+(routines/locally_linear.hpp:161-255) and triplet assembly (utils/sparse.hpp:16-21).
 Parity status: kNN sets pinned by the reference's 1-D line known-answer test;
 W / M / LTSA values unpinned by the reference (it has no golden values for them)
 and cross-checked against scikit-learn fixtures in tests/golden/. The dense
@@ -55,6 +56,8 @@ def lib():
         L.oracle_lle_weights_rows.restype = i32
         L.oracle_ltsa_basis.argtypes = [dptr, i64, i64, iptr, i32, i32, dptr, dptr, i32]
         L.oracle_ltsa_basis.restype = i32
+        L.oracle_hessian_blocks.argtypes = [dptr, i64, i64, iptr, i32, i32, dptr, i32]
+        L.oracle_hessian_blocks.restype = i32
         L.oracle_assemble.argtypes = [i32, i64, i32, i32, iptr, dptr, ctypes.c_double, dptr, dptr, dptr, i64]
         L.oracle_assemble.restype = i64
         L.oracle_eigenproblem_pair.argtypes = [i32, i64, i32, dptr, dptr, iptr, dptr, dptr, dptr]
@@ -152,8 +155,25 @@ def ltsa_basis(X, idx, td=2, nthreads=None, return_evals=False):
     return (V, ev) if return_evals else V
 
 
+def hessian_blocks(X, idx, td=2, nthreads=None):
+    """Per-neighbourhood Hessian LLE blocks B (rows x k x k) of
+    hessian_weight_matrix (routines/locally_linear.hpp:161-255); td is 1 or 2
+    (the reference's product-column placement is defined for those only)."""
+    X = _X64(X)
+    D = X.shape[1]
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    rows, k = idx.shape
+    B = np.zeros((rows, k, k), np.float64)
+    rc = lib().oracle_hessian_blocks(X.ctypes.data, rows, D, idx.ctypes.data, k, int(td), B.ctypes.data,
+                                     _threads(nthreads))
+    if rc != 0:
+        raise ValueError("the Hessian blocks are defined for target_dimension 1 or 2")
+    return B
+
+
 def assemble(method, idx, weights, shift):
-    """method 0 = LLE (weights = W, N x k), 1 = LTSA (weights = V, N x k x td).
+    """method 0 = LLE (weights = W, N x k), 1 = LTSA (weights = V, N x k x td),
+    2 = Hessian (weights = B, N x k x k; shift unused).
     Returns (row_ptr int64, col_idx int32, vals float64)."""
     idx = np.ascontiguousarray(idx, dtype=np.int32)
     N, k = idx.shape

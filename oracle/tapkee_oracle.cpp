@@ -370,10 +370,46 @@ static void jacobi_eigen(double* A, int n, double* evals, double* V)
     std::memcpy(V, Vs.data(), sizeof(double) * n * n);
 }
 
+// Centred neighbour Gram and its top eigenvectors, shared by the LTSA basis
+// (routines/locally_linear.hpp:45-63) and the Hessian weights (:188-204): the
+// Gram of the neighbours only, K_ab = k(n_a,n_b) (:47-55 / :188-196), double
+// centring centerMatrix (utils/matrix.hpp:12-19), and the eigenvectors of the td
+// largest eigenvalues in ascending order, rightCols(td) (:60-61 / :200-204).
+// top is k x td row-major; ev receives the k ascending eigenvalues. G, V and cm
+// are caller scratch of k*k, k*k and k doubles.
+static void local_top_basis(const double* X, int64_t D, const int32_t* nb, int k, int td, double* G, double* V,
+                            double* cm, double* ev, double* top)
+{
+    for (int a = 0; a < k; ++a)
+        for (int b = a; b < k; ++b)
+        {
+            double v = kernel_dot(X, D, nb[a], nb[b]);
+            G[a * k + b] = v;
+            G[b * k + a] = v;
+        }
+    // centerMatrix: K + mean(K) - colmean (row-wise) - colmean (col-wise)
+    double grand = 0.0;
+    for (int b = 0; b < k; ++b)
+    {
+        double s = 0.0;
+        for (int a = 0; a < k; ++a)
+            s += G[a * k + b];
+        cm[b] = s / k;
+    }
+    for (int t = 0; t < k * k; ++t)
+        grand += G[t];
+    grand /= (double)k * k;
+    for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b)
+            G[a * k + b] = G[a * k + b] + grand - cm[b] - cm[a];
+    jacobi_eigen(G, k, ev, V);
+    for (int a = 0; a < k; ++a)
+        for (int t = 0; t < td; ++t)
+            top[a * td + t] = V[a * k + (k - td + t)];
+}
+
 // LTSA local tangent basis: routines/locally_linear.hpp:20-88 (per point,
-// :45-63). Gram of the neighbours only, K_ab = k(n_a,n_b) (:47-55), double
-// centring centerMatrix (utils/matrix.hpp:12-19), eigenvectors of the td
-// largest eigenvalues (:60-61). V_out is N x k x td (row-major); the
+// :45-63), the basis of local_top_basis. V_out is N x k x td (row-major); the
 // alignment block is P = (1/k) 1 1^T + V V^T (G = [1/sqrt(k) 1, V], :36-37,63).
 // evals_out (optional) receives the k ascending eigenvalues per point.
 int oracle_ltsa_basis(const double* X, int64_t N, int64_t D, const int32_t* idx, int k, int td, double* V_out,
@@ -385,36 +421,95 @@ int oracle_ltsa_basis(const double* X, int64_t N, int64_t D, const int32_t* idx,
 #pragma omp for schedule(static)
         for (int64_t i = 0; i < N; ++i)
         {
-            const int32_t* nb = idx + i * k;
-            for (int a = 0; a < k; ++a)
-                for (int b = a; b < k; ++b)
-                {
-                    double v = kernel_dot(X, D, nb[a], nb[b]);
-                    G[a * k + b] = v;
-                    G[b * k + a] = v;
-                }
-            // centerMatrix: K + mean(K) - colmean (row-wise) - colmean (col-wise)
-            double grand = 0.0;
-            for (int b = 0; b < k; ++b)
-            {
-                double s = 0.0;
-                for (int a = 0; a < k; ++a)
-                    s += G[a * k + b];
-                cm[b] = s / k;
-            }
-            for (int t = 0; t < k * k; ++t)
-                grand += G[t];
-            grand /= (double)k * k;
-            for (int a = 0; a < k; ++a)
-                for (int b = 0; b < k; ++b)
-                    G[a * k + b] = G[a * k + b] + grand - cm[b] - cm[a];
-            jacobi_eigen(G.data(), k, ev.data(), V.data());
-            for (int a = 0; a < k; ++a)
-                for (int t = 0; t < td; ++t)
-                    V_out[(i * k + a) * td + t] = V[a * k + (k - td + t)];
+            local_top_basis(X, D, idx + i * k, k, td, G.data(), V.data(), cm.data(), ev.data(),
+                            V_out + i * (int64_t)k * td);
             if (evals_out)
                 for (int a = 0; a < k; ++a)
                     evals_out[i * k + a] = ev[a];
+        }
+    }
+    return 0;
+}
+
+// Hessian LLE weights: routines/locally_linear.hpp:161-255 (per point,
+// :184-243). With the tangent basis V (k x td) of local_top_basis:
+//   Yi = [1, V, products V_j * V_{j+p}]                          (:203-214)
+//   Gram-Schmidt over the columns of Yi in order, each column normalised (:216-225)
+//   a product column is divided by its sum when the sum exceeds 1e-4 (:226-231)
+//   B = Yr Yr^T with Yr the dp = td (td + 1) / 2 product columns    (:234)
+// B_out is N x k x k (row-major); the point's triplets are (n_a, n_b, B_ab) for
+// all a, b (:236-243). The reference places the product columns with
+// ct += ct + td - j (:213), which matches the ordered pairs j <= j + p only for
+// td <= 2; for td >= 3 it writes past the dp columns of Yi. This restatement
+// therefore accepts td <= 2 and returns -1 otherwise.
+int oracle_hessian_blocks(const double* X, int64_t N, int64_t D, const int32_t* idx, int k, int td, double* B_out,
+                          int nthreads)
+{
+    if (td < 1 || td > 2)
+        return -1;
+    const int dp = td * (td + 1) / 2;
+    const int ncol = 1 + td + dp;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+    {
+        std::vector<double> G(k * k), V(k * k), ev(k), cm(k), top(k * td), Y((size_t)k * ncol);
+        auto col = [&](int c) { return Y.data() + (size_t)c * k; };  // column-major Yi
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < N; ++i)
+        {
+            local_top_basis(X, D, idx + i * k, k, td, G.data(), V.data(), cm.data(), ev.data(), top.data());
+            for (int a = 0; a < k; ++a)
+            {
+                col(0)[a] = 1.0;
+                for (int t = 0; t < td; ++t)
+                    col(1 + t)[a] = top[a * td + t];
+            }
+            int ct = 0;
+            for (int j = 0; j < td; ++j)
+            {
+                for (int p = 0; p < td - j; ++p)
+                    for (int a = 0; a < k; ++a)
+                        col(ct + p + 1 + td)[a] = col(j + 1)[a] * col(j + p + 1)[a];
+                ct += ct + td - j;
+            }
+            for (int c = 0; c < ncol; ++c)
+            {
+                double* yc = col(c);
+                for (int j = 0; j < c; ++j)
+                {
+                    const double* yj = col(j);
+                    double r = 0.0;
+                    for (int a = 0; a < k; ++a)
+                        r += yc[a] * yj[a];
+                    for (int a = 0; a < k; ++a)
+                        yc[a] -= r * yj[a];
+                }
+                double nrm = 0.0;
+                for (int a = 0; a < k; ++a)
+                    nrm += yc[a] * yc[a];
+                // (1.f / norm) in the reference: the float 1 promotes to double
+                const double inv = 1.0f / std::sqrt(nrm);
+                for (int a = 0; a < k; ++a)
+                    yc[a] *= inv;
+            }
+            for (int q = 0; q < dp; ++q)
+            {
+                double* yc = col(1 + td + q);
+                double s = 0.0;
+                for (int a = 0; a < k; ++a)
+                    s += yc[a];
+                if (s > 1e-4)
+                    for (int a = 0; a < k; ++a)
+                        yc[a] /= s;
+            }
+            double* B = B_out + i * (int64_t)k * k;
+            for (int a = 0; a < k; ++a)
+                for (int b = 0; b < k; ++b)
+                {
+                    double s = 0.0;
+                    for (int q = 0; q < dp; ++q)
+                        s += col(1 + td + q)[a] * col(1 + td + q)[b];
+                    B[a * k + b] = s;
+                }
         }
     }
     return 0;
@@ -428,7 +523,10 @@ int oracle_ltsa_basis(const double* X, int64_t N, int64_t D, const int32_t* idx,
 //        (i,i,1+shift), then per a: (n_a,i,-w_a), (i,n_a,-w_a), (n_a,n_b,w_a w_b) for b
 //   LTSA (routines/locally_linear.hpp:65-77):
 //        (i,i,shift), then per a: (n_a,n_a,1), (n_a,n_b,-P_ab) for b, P = (1/k)11^T + V V^T
-// method: 0 = LLE (weights = W, N x k), 1 = LTSA (weights = V, N x k x td).
+//   HLLE (routines/locally_linear.hpp:236-243):
+//        per a: (n_a,n_b,B_ab) for b; no diagonal shift
+// method: 0 = LLE (weights = W, N x k), 1 = LTSA (weights = V, N x k x td),
+// 2 = Hessian (weights = B, N x k x k; td and shift unused).
 // Returns nnz, or -1 if cap is too small (row_ptr is filled in any case).
 int64_t oracle_assemble(int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,
                         double shift, int64_t* row_ptr, int32_t* col_idx, double* vals, int64_t cap)
@@ -455,6 +553,13 @@ int64_t oracle_assemble(int method, int64_t N, int k, int td, const int32_t* idx
                 for (int b = 0; b < k; ++b)
                     trips.push_back({nb[a], nb[b], w[a] * w[b]});
             }
+        }
+        else if (method == 2)
+        {
+            const double* B = weights + i * (int64_t)k * k;
+            for (int a = 0; a < k; ++a)
+                for (int b = 0; b < k; ++b)
+                    trips.push_back({nb[a], nb[b], B[a * k + b]});
         }
         else
         {

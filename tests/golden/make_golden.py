@@ -15,6 +15,13 @@ scikit-learn's independent implementations of the same published formulas:
 * LTSA embedding -- sklearn LocallyLinearEmbedding(method="ltsa", dense eigh);
                     its alignment update equals routines/locally_linear.hpp:65-77
                     without the (i,i,shift) triplet.
+* HLLE blocks    -- hlle_blocks_numpy below, the Donoho-Grimes estimator with
+                    an SVD tangent basis and a Householder QR (the oracle uses a
+                    Jacobi eigenbasis and Gram-Schmidt). scikit-learn's
+                    method="hessian" is no cross-check here: it keeps every
+                    column of a full QR past 1 + td, so its block is
+                    I - P[1, V], the LTSA block, and its embedding equals its
+                    LTSA embedding.
 
 The scikit-learn outputs are stored next to the oracle's so the cross-check can
 be replayed where scikit-learn is not installed.
@@ -47,6 +54,26 @@ def principal_angles(A, B):
     qb, _ = np.linalg.qr(B)
     s = np.linalg.svd(qa.T @ qb, compute_uv=False)
     return np.arccos(np.clip(s, -1, 1))
+
+
+def hlle_blocks_numpy(X, idx, td):
+    """Hessian blocks B_i = H H^T, H the dp product columns of the reduced QR of
+    [1, U, U_j U_l] (U: top-td left singular vectors of the centred neighbours),
+    a product column divided by its sum when that sum exceeds 1e-4."""
+    k = idx.shape[1]
+    dp = td * (td + 1) // 2
+    out = np.zeros((len(idx), k, k))
+    for i in range(len(idx)):
+        G = X[idx[i]] - X[idx[i]].mean(0)
+        U = np.linalg.svd(G, full_matrices=False)[0][:, :td]
+        cols = [np.ones(k)] + [U[:, t] for t in range(td)]
+        cols += [U[:, j] * U[:, l] for j in range(td) for l in range(j, td)]
+        Q = np.linalg.qr(np.stack(cols, 1))[0]
+        H = Q[:, 1 + td:1 + td + dp]
+        S = H.sum(0)
+        H = H / np.where(S > 1e-4, S, 1.0)
+        out[i] = H @ H.T
+    return out
 
 
 def main():
@@ -95,6 +122,21 @@ def main():
     out.update(ltsa_idx_oracle_order=idx2, ltsa_V=V, ltsa_embedding=E2,
                ltsa_embedding_sklearn=E2_sk, ltsa_nnz=np.int64(rp2[-1]))
     print(f"LTSA: embedding angle vs sklearn {ang2:.2e}, nnz {rp2[-1]}")
+
+    # ---- Hessian LLE on the same S-curve, k=12, td=2 ----
+    B = oracle.hessian_blocks(Xs, idx2, td)
+    B_np = hlle_blocks_numpy(Xs, idx2, td)
+    berr = np.abs(B - B_np).max()
+    assert berr < 1e-9, berr
+    rp3, col3, vals3 = oracle.assemble(2, idx2, B, 0.0)
+    E3, ev3 = oracle.dense_embedding(rp3, col3, vals3, td)
+    rp4, col4, vals4 = oracle.assemble(2, idx2, B_np, 0.0)
+    E3_np, _ = oracle.dense_embedding(rp4, col4, vals4, td)
+    ang3 = principal_angles(E3, E3_np).max()
+    assert ang3 < 1e-6, ang3
+    out.update(hlle_B=B[:64], hlle_embedding=E3, hlle_embedding_numpy=E3_np,
+               hlle_evals=ev3, hlle_nnz=np.int64(rp3[-1]), hlle_M_checksum=np.float64(np.abs(vals3).sum()))
+    print(f"HLLE: blocks vs numpy {berr:.2e}, embedding angle vs numpy {ang3:.2e}, evals {ev3}, nnz {rp3[-1]}")
 
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **out)
     print("wrote", os.path.join(HERE, "golden_small.npz"))

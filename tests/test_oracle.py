@@ -159,3 +159,62 @@ def test_oracle_small_inputs(n):
     idx, _, cnt = oracle.knn_brute(X, n - 1)
     for i in range(n):
         assert set(idx[i]) == set(range(n)) - {i}
+
+
+def _hlle_blocks_np(X, idx, td, flip=None):
+    """Donoho-Grimes Hessian blocks from an SVD tangent basis and a Householder
+    QR; flip multiplies the basis columns by +-1."""
+    k = idx.shape[1]
+    dp = td * (td + 1) // 2
+    out = np.zeros((len(idx), k, k))
+    for i in range(len(idx)):
+        G = X[idx[i]] - X[idx[i]].mean(0)
+        U = np.linalg.svd(G, full_matrices=False)[0][:, :td]
+        if flip is not None:
+            U = U * flip
+        cols = [np.ones(k)] + [U[:, t] for t in range(td)]
+        cols += [U[:, j] * U[:, l] for j in range(td) for l in range(j, td)]
+        H = np.linalg.qr(np.stack(cols, 1))[0][:, 1 + td:1 + td + dp]
+        S = H.sum(0)
+        H = H / np.where(S > 1e-4, S, 1.0)
+        out[i] = H @ H.T
+    return out
+
+
+def test_oracle_hessian_vs_fixture(golden):
+    """hessian_weight_matrix (routines/locally_linear.hpp:161-255) on the
+    lifted S-curve: the committed blocks, nnz, M checksum and embedding."""
+    Xs = datasets.lifted_s_curve(1500, d=8, seed=11, noise=0.02, dtype=np.float64)
+    idx = golden["ltsa_idx_oracle_order"]
+    B = oracle.hessian_blocks(Xs, idx, 2)
+    assert np.abs(B[:64] - golden["hlle_B"]).max() < 1e-12
+    rp, col, vals = oracle.assemble(2, idx, B, 0.0)
+    assert int(rp[-1]) == int(golden["hlle_nnz"])
+    assert abs(np.abs(vals).sum() - golden["hlle_M_checksum"]) < 1e-9 * golden["hlle_M_checksum"]
+    E, lam = oracle.dense_embedding(rp, col, vals, 2)
+    assert _angles(E, golden["hlle_embedding"]).max() < 1e-6
+    assert _angles(golden["hlle_embedding"], golden["hlle_embedding_numpy"]).max() < 1e-6
+    # not the LTSA embedding of the same neighbourhoods
+    assert _angles(E, golden["ltsa_embedding"]).max() > 1e-2
+
+
+def test_oracle_hessian_block_is_a_sign_free_projector():
+    """Every column of the Gram-Schmidt basis after the constant one sums to
+    zero, so the column-sum division (routines/locally_linear.hpp:226-231) does
+    not fire and B is the orthogonal projector onto the quadratic part, rank
+    td (td + 1) / 2: independent of the eigenvector signs and of how the
+    tangent basis was computed."""
+    Xs = datasets.lifted_s_curve(400, d=6, seed=4, noise=0.01, dtype=np.float64)
+    idx, _, _ = oracle.knn_brute(Xs, 10)
+    for td in (1, 2):
+        B = oracle.hessian_blocks(Xs, idx, td)
+        dp = td * (td + 1) // 2
+        assert np.abs(np.einsum("nab,nbc->nac", B, B) - B).max() < 1e-12
+        assert np.abs(np.trace(B, axis1=1, axis2=2) - dp).max() < 1e-12
+        assert np.abs(B.sum(2)).max() < 1e-12
+        V = oracle.ltsa_basis(Xs, idx, td)
+        assert np.abs(np.einsum("nab,nbt->nat", B, V)).max() < 1e-12
+        for flip in ([1.0] * td, [-1.0] + [1.0] * (td - 1), [-1.0] * td):
+            assert np.abs(B - _hlle_blocks_np(Xs, idx, td, np.array(flip))).max() < 1e-9
+    with pytest.raises(ValueError):
+        oracle.hessian_blocks(Xs, idx, 3)
