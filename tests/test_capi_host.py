@@ -84,3 +84,30 @@ def test_datasets_are_seeded_and_shaped():
     assert all(500 <= n <= 20000 and d in (3, 16, 64, 128) and k in (8, 12, 16, 24, 32) for n, d, k, _ in specs)
     X = datasets.swiss_roll(2000, seed=0)
     assert X.shape == (2000, 3)
+
+
+def test_noalloc_entry_point_host_checks(lib):
+    """tk_check_connected_noalloc refuses bad sizes and arguments on the host,
+    before any CUDA call, and writes the reason into the caller's buffer."""
+    c = ctypes.c_int(-1)
+    msg = ctypes.create_string_buffer(256)
+    dummy = ctypes.c_void_p(16)  # never dereferenced: every call below fails first
+
+    def call(n, k=2, idx=dummy, out=ctypes.byref(c), device=0):
+        msg.value = b"stale"
+        return lib.tk_check_connected_noalloc(device, None, n, k, idx, out, msg, len(msg))
+
+    assert call(0) == _capi.TK_ERR_NO_DATA and msg.value == b"No data"
+    assert call(10, k=0) == _capi.TK_ERR_INVALID_ARG
+    assert call(10, idx=None) == _capi.TK_ERR_INVALID_ARG
+    assert call(10, out=None) == _capi.TK_ERR_INVALID_ARG
+    st = call(_capi.TK_NOALLOC_MAX_POINTS + 1)
+    assert st == _capi.TK_ERR_INVALID_ARG
+    assert str(_capi.TK_NOALLOC_MAX_POINTS) in msg.value.decode() and b"limit" in msg.value
+    assert call(10, device=-1) == _capi.TK_ERR_NO_DEVICE
+    assert c.value == -1
+    # a NULL or empty message buffer is allowed
+    assert lib.tk_check_connected_noalloc(0, None, 0, 2, dummy, ctypes.byref(c), None, 0) == _capi.TK_ERR_NO_DATA
+    import torch
+    if not torch.cuda.is_available():
+        assert call(10) == _capi.TK_ERR_NO_DEVICE and msg.value.startswith(b"no CUDA device")
