@@ -359,6 +359,9 @@ int tk_batch_destroy(tk_batch* batch);
  *     TK_ERR_INVALID_ARG with a message naming the limit.
  *   - The first call on a device does the set-up (resolves the device address of
  *     the scratch array and loads the kernel): make it before any stream capture.
+ *     The resolved address is kept for the life of the process; cudaDeviceReset
+ *     destroys the array it points to, so a process that resets a device must not
+ *     call this entry point on that device afterwards.
  *   - Every call on a device shares the one scratch array: calls that overlap in
  *     time on that device (other threads, other streams) race and must be
  *     serialised by the caller.

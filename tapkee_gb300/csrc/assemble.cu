@@ -168,12 +168,17 @@ void scan_to_offsets(tk_ctx* ctx, const int* in, int64_t n, int64_t* out)
 
 namespace {
 
-__global__ void k_fill_rev(const int32_t* __restrict__ idx, int64_t nk, const int64_t* rptr, int* fillc,
+// Entries outside [0, N) were flagged by k_indeg (DEV_ERR_BOUNDS, turned into
+// TK_ERR_INVALID_ARG by the host after the row phase) and are skipped here too,
+// so a caller's bad index is never used as an address.
+__global__ void k_fill_rev(const int32_t* __restrict__ idx, int64_t nk, int64_t N, const int64_t* rptr, int* fillc,
                            int32_t* rev)
 {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x)
     {
         const int j = idx[e];
+        if (j < 0 || j >= N)
+            continue;
         const int pos = atomicAdd(&fillc[j], 1);
         rev[rptr[j] + pos] = (int32_t)e;
     }
@@ -856,7 +861,7 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     k_indeg<<<g, 256, 0, st>>>(idx, nk, N, k, cnt, repeats, ctx->dev_err);
     TK_CHECK_LAUNCH();
     scan_to_offsets(ctx, cnt, N, a.rptr);
-    k_fill_rev<<<g, 256, 0, st>>>(idx, nk, a.rptr, fillc, a.rev);
+    k_fill_rev<<<g, 256, 0, st>>>(idx, nk, N, a.rptr, fillc, a.rev);
     TK_CHECK_LAUNCH();
     k_sort_rev<<<g, 256, 0, st>>>(N, a.rptr, a.rev);
     TK_CHECK_LAUNCH();

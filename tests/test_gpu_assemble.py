@@ -96,3 +96,23 @@ def test_assembly_self_loops(ctx):
     rr, rc, rv = oracle.assemble(0, idx, w, 1e-9)
     assert np.array_equal(rp, rr) and np.array_equal(col, rc)
     assert np.abs(vals - rv).max() <= 1e-12 * np.abs(rv).max()
+
+
+@pytest.mark.parametrize("method", ["lle", "ltsa"])
+def test_assembly_out_of_range_neighbours_are_reported(ctx, method):
+    """A neighbour index outside [0, N) in a caller's list is reported as a bad
+    argument by assembly (never used as an address), and the context stays
+    usable."""
+    import tapkee_gb300 as tk
+    rng = np.random.default_rng(9)
+    N, k, td = 700, 8, 2
+    idx = np.stack([rng.choice(N, size=k, replace=False) for _ in range(N)]).astype(np.int32)
+    w = rng.random((N, k)) if method == "lle" else rng.standard_normal((N, k, td))
+    bad = idx.copy()
+    bad[11, 2] = N + 5
+    bad[600, 0] = -3
+    with pytest.raises(tk.WrongParameterError, match="index out of range"):
+        ctx.assemble(method, bad, w, 1e-9)
+    rp, col, vals = ctx.assemble(method, idx, w, 1e-9)
+    rr, rc, rv = oracle.assemble(0 if method == "lle" else 1, idx, w, 1e-9)
+    assert np.array_equal(rp, rr) and np.array_equal(col, rc)

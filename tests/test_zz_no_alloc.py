@@ -97,3 +97,27 @@ def test_noalloc_rejections(ctx):
     assert st == _capi.TK_ERR_INVALID_ARG and "out of range" in msg
     st, c, msg = _noalloc(lib, idx_dev)
     assert st == _capi.TK_OK and c == 1
+
+
+def test_noalloc_calls_allocate_no_device_memory(ctx):
+    """After the set-up call, calls (up to the size limit) leave the device's free
+    memory unchanged: nothing is allocated, by the library or by the runtime."""
+    import torch
+    lib = _capi.load()
+    graphs = [torch.from_numpy(g).to("cuda:0") for g in
+              (_heap_graph(MAX_N), _heap_graph(MAX_N, cut=True), _heap_graph(1000))]
+    torch.cuda.synchronize()
+    st, _, msg = _noalloc(lib, graphs[2])  # set-up (a no-op when an earlier test made it)
+    assert st == _capi.TK_OK, msg
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    results = []
+    for _ in range(3):
+        for g in graphs:
+            st, c, msg = _noalloc(lib, g)
+            assert st == _capi.TK_OK, msg
+            results.append(c)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, (free0, free1)
+    assert results == [1, 0, 1] * 3
