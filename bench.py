@@ -395,7 +395,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp16x3-split screen / f32+float-float re-rank and weights",
             "data": "synthetic (seeded lifted Swiss roll)", "config": workload, "stage_ms": stage,
-            "rows_uncertified": int(info.rows_uncertified), "nnz": nnz, "k_used": kk,
+            "rows_uncertified": int(info.rows_uncertified), "tie_rows": int(info.tie_rows),
+            "extra_neighbor_rows": int(info.extra_rows), "nnz": nnz, "k_used": kk,
             "fp32_path": fp32, "ltsa": ltsa, "eigen": eigen, "batch": batch, "roofline": roofline,
             "e2e": {"value": args.n / (e2e_ms / 1000.0), "unit": "points/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -107,6 +107,11 @@ typedef struct tk_knn_stats
                                  certified and were recomputed exactly          */
     int32_t candidates;       /* candidates kept per row by the screen          */
     int32_t screen;           /* engine used                                    */
+    int64_t tie_rows;         /* rows whose k-th and (k+1)-th nearest distances
+                                 lie within 1e-12 relative: their sets follow
+                                 the reference's nth_element partition           */
+    int64_t extra_rows;       /* rows for which the reference returns k + 1
+                                 neighbours (see tk_knn_extra_rows)             */
 } tk_knn_stats;
 
 /* Summary of the operator held by a context after tk_local_operator(). */
@@ -123,6 +128,8 @@ typedef struct tk_operator_info
     float stage_ms[6];        /* device time per stage: knn, connectivity, weights,
                                  assembly, total, and the distance-screen kernel
                                  alone (last kNN pass)                               */
+    int64_t tie_rows;         /* see tk_knn_stats (last kNN pass)                   */
+    int64_t extra_rows;       /* see tk_knn_stats (last kNN pass)                   */
 } tk_operator_info;
 
 /* ---- context -------------------------------------------------------------- */
@@ -158,11 +165,28 @@ long long tk_kernel_launch_count(void);
  * Replaces find_neighbors_bruteforce_impl (neighbors/neighbors.hpp:119-149) with
  * KernelDistance (neighbors/neighbors.hpp:40-55) over eigen_kernel_callback
  * (callbacks/eigen_callbacks.hpp:34-46).
- * idx_out (N x k) receives, per row, the k nearest other points ordered by
- * (distance, index); d2_out (N x k, optional) their FP64 squared distances.
+ * idx_out (N x k) receives, per row, the reference's neighbour set: the k
+ * nearest other points ordered by (distance, index). Where the k-th and
+ * (k+1)-th nearest distances tie (within 1e-12 relative; stats->tie_rows), the
+ * row instead holds the first k records of the first k + 1 that libstdc++'s
+ * std::nth_element(begin, begin + k + 1, end) leaves over the row's N records in
+ * index order, minus the point itself, in that partition order -- the
+ * reference's selection (neighbors/neighbors.hpp:135-146, distances_comparator
+ * :28-34). d2_out (N x k, optional) receives the FP64 squared distances.
  * Requires 1 <= k <= N-1. */
 int tk_knn_brute(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, int k, int screen,
                  int32_t* idx_out, double* d2_out, tk_knn_stats* stats);
+
+/* The rows of the last brute kNN pass on ctx (tk_knn_brute, or the final pass of
+ * tk_local_operator) for which the reference returns k + 1 neighbours: the point
+ * has k + 1 or more exact duplicates and the partition leaves it outside the
+ * first k + 1 records (neighbors/neighbors.hpp:140-146 then keeps all k + 1).
+ * The first k of them are in idx_out, which is what the reference's weight and
+ * connectivity routines read (they take k from the first row's list:
+ * routines/locally_linear.hpp:96, neighbors/connected.hpp:27). Writes up to
+ * `capacity` (row, (k+1)-th neighbour) pairs into rows[] / extra[] (host
+ * memory; either may be NULL) and *count = the number of such rows. */
+int tk_knn_extra_rows(tk_ctx* ctx, int32_t* rows, int32_t* extra, int64_t capacity, int64_t* count);
 
 /* Reachability of every vertex from vertex 0 along kNN out-edges.
  * Replaces is_connected (neighbors/connected.hpp:19-62). *connected = 1 or 0. */

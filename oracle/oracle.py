@@ -44,7 +44,7 @@ def lib():
         build()
         L = ctypes.CDLL(_LIB_PATH)
         i64, i32, dptr, iptr = ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p
-        L.oracle_knn_brute.argtypes = [dptr, i64, i64, i32, iptr, dptr, iptr, i32]
+        L.oracle_knn_brute.argtypes = [dptr, i64, i64, i32, iptr, dptr, iptr, iptr, i32]
         L.oracle_knn_brute.restype = i32
         L.oracle_knn_brute_rows.argtypes = [dptr, i64, i64, i32, iptr, i64, iptr, i32]
         L.oracle_knn_brute_rows.restype = i32
@@ -74,18 +74,21 @@ def _X64(X):
     return np.ascontiguousarray(np.asarray(X, dtype=np.float64))
 
 
-def knn_brute(X, k, nthreads=None):
-    """Returns (idx N x k int32 in partition order, dist N x k, row_count N)."""
+def knn_brute(X, k, nthreads=None, return_extra=False):
+    """Returns (idx N x k int32 in partition order, dist N x k, row_count N) and,
+    with return_extra, also extra N: the (k+1)-th reference neighbour of rows with
+    row_count k + 1, -1 elsewhere."""
     X = _X64(X)
     N, D = X.shape
     idx = np.zeros((N, k), np.int32)
     dist = np.zeros((N, k), np.float64)
     cnt = np.zeros(N, np.int32)
+    extra = np.full(N, -1, np.int32)
     rc = lib().oracle_knn_brute(X.ctypes.data, N, D, k, idx.ctypes.data, dist.ctypes.data, cnt.ctypes.data,
-                                _threads(nthreads))
+                                extra.ctypes.data, _threads(nthreads))
     if rc != 0:
         raise ValueError("oracle_knn_brute: invalid arguments")
-    return idx, dist, cnt
+    return (idx, dist, cnt, extra) if return_extra else (idx, dist, cnt)
 
 
 def knn_brute_rows(X, k, rows, nthreads=None):

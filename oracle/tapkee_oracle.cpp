@@ -56,13 +56,14 @@ static inline double kernel_dot(const double* X, int64_t D, int64_t a, int64_t b
 // partitions at k+1 with the strict comparator of neighbors.hpp:28-34, and the
 // first k+1 records minus the query itself (by identity) are kept in partition
 // order. Rows where the query is not among the first k+1 records (k+1 exact
-// duplicates) yield k+1 neighbors in the reference; here the first k are kept
-// and row_count[i] records k+1 so callers can detect it.
+// duplicates) yield k+1 neighbors in the reference; here the first k are kept,
+// row_count[i] records k+1 and extra_out[i] (optional; -1 elsewhere) the
+// (k+1)-th, so callers can detect and compare them.
 //
 // The reference's brute loop is serial; queries are independent, so the loop is
 // split across OpenMP threads (same per-query arithmetic, same results).
 int oracle_knn_brute(const double* X, int64_t N, int64_t D, int k, int32_t* idx_out, double* dist_out,
-                     int32_t* row_count, int nthreads)
+                     int32_t* row_count, int32_t* extra_out, int nthreads)
 {
     if (N <= 0 || k <= 0 || k > N - 1)
         return -1;
@@ -84,7 +85,9 @@ int oracle_knn_brute(const double* X, int64_t N, int64_t D, int k, int32_t* idx_
                                  return l.second < r.second;
                              });
             int c = 0, total = 0;
-            for (int m = 0; m < k + 1; ++m)
+            if (extra_out)
+                extra_out[i] = -1;
+            for (int m = 0; m < k + 1 && m < N; ++m)
             {
                 if (distances[m].first != i)
                 {
@@ -95,6 +98,8 @@ int oracle_knn_brute(const double* X, int64_t N, int64_t D, int k, int32_t* idx_
                             dist_out[i * k + c] = distances[m].second;
                         ++c;
                     }
+                    else if (extra_out)
+                        extra_out[i] = (int32_t)distances[m].first;
                     ++total;
                 }
             }

@@ -49,7 +49,8 @@ class tk_params(ctypes.Structure):
 
 
 class tk_knn_stats(ctypes.Structure):
-    _fields_ = [("rows_uncertified", ctypes.c_int64), ("candidates", ctypes.c_int32), ("screen", ctypes.c_int32)]
+    _fields_ = [("rows_uncertified", ctypes.c_int64), ("candidates", ctypes.c_int32), ("screen", ctypes.c_int32),
+                ("tie_rows", ctypes.c_int64), ("extra_rows", ctypes.c_int64)]
 
 
 class tk_batch_problem(ctypes.Structure):
@@ -71,6 +72,8 @@ class tk_operator_info(ctypes.Structure):
         ("nnz", ctypes.c_int64),
         ("rows_uncertified", ctypes.c_int64),
         ("stage_ms", ctypes.c_float * 6),
+        ("tie_rows", ctypes.c_int64),
+        ("extra_rows", ctypes.c_int64),
     ]
 
 
@@ -101,6 +104,7 @@ SIGNATURES = {
     "tk_version": (ctypes.c_char_p, []),
     "tk_kernel_launch_count": (ctypes.c_longlong, []),
     "tk_knn_brute": (_I, [_P, _P, _I, _I64, _I, _I64, _I, _I, _P, _P, ctypes.POINTER(tk_knn_stats)]),
+    "tk_knn_extra_rows": (_I, [_P, _P, _P, _I64, ctypes.POINTER(_I64)]),
     "tk_check_connected": (_I, [_P, _I64, _I, _P, ctypes.POINTER(_I)]),
     "tk_lle_weights": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P]),
     "tk_lle_weights_grad": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P, _P, _P]),

@@ -178,6 +178,8 @@ class LocalOperator:
     connectivity_retries: int
     rows_uncertified: int
     stage_ms: dict = field(default_factory=dict)
+    tie_rows: int = 0
+    extra_rows: int = 0
 
     def to_scipy(self):
         import scipy.sparse as sp
@@ -237,7 +239,11 @@ class Context:
     # -- stages ---------------------------------------------------------------
     def knn_brute(self, X, k, screen="tensor", return_distances=False, return_stats=False):
         """Brute-force k nearest neighbours (neighbors/neighbors.hpp:119-149).
-        Rows ordered by (FP64 squared distance, index)."""
+        Rows ordered by (FP64 squared distance, index), except tie rows (the k-th
+        and (k+1)-th distances within 1e-12 relative), which hold the reference's
+        nth_element selection in its partition order. return_stats adds a dict
+        with rows_uncertified, candidates, tie_rows, extra_rows and, when
+        extra_rows > 0, extra = [(row, (k+1)-th reference neighbour), ...]."""
         xb, dt = _as_points(X)
         N, D = xb.arr.shape
         idx = _empty((N, k), np.int32, xb)
@@ -249,8 +255,24 @@ class Context:
         if return_distances:
             out.append(d2.arr)
         if return_stats:
-            out.append({"rows_uncertified": st.rows_uncertified, "candidates": st.candidates})
+            stats = {"rows_uncertified": st.rows_uncertified, "candidates": st.candidates,
+                     "tie_rows": st.tie_rows, "extra_rows": st.extra_rows}
+            if st.extra_rows > 0:
+                stats["extra"] = self.knn_extra_rows()
+            out.append(stats)
         return out[0] if len(out) == 1 else tuple(out)
+
+    def knn_extra_rows(self):
+        """(row, (k+1)-th neighbour) pairs of the last brute kNN pass for which the
+        reference returns k + 1 neighbours (tk_knn_extra_rows), ascending by row."""
+        n = ctypes.c_int64(0)
+        self._check(self.lib.tk_knn_extra_rows(self.ptr, None, None, 0, ctypes.byref(n)))
+        rows = np.empty(n.value, np.int32)
+        extra = np.empty(n.value, np.int32)
+        if n.value:
+            self._check(self.lib.tk_knn_extra_rows(self.ptr, rows.ctypes.data, extra.ctypes.data, n.value,
+                                                   ctypes.byref(n)))
+        return list(zip(rows.tolist(), extra.tolist()))
 
     def find_neighbors(self, X, k, check_connectivity=True, screen="tensor", return_distances=False):
         """find_neighbors with neighbors_method=Brute (neighbors/neighbors.hpp:173-213)
@@ -414,7 +436,8 @@ class Context:
         val = _empty((info.nnz,), np.float64, xb)
         self._check(self.lib.tk_operator_copy(self.ptr, idx.ptr, w.ptr, rp.ptr, col.ptr, val.ptr))
         return LocalOperator(idx.arr, w.arr, rp.arr, col.arr, val.arr, k, info.method, td,
-                             info.connectivity_retries, info.rows_uncertified, stage)
+                             info.connectivity_retries, info.rows_uncertified, stage, info.tie_rows,
+                             info.extra_rows)
 
     def synchronize(self):
         self._check(self.lib.tk_ctx_synchronize(self.ptr))

@@ -635,7 +635,10 @@ void enqueue(tk_batch* B)
         RS.probs = B->probs;
         RS.prob_R = B->prob_R;
         RS.idx_all = B->idx_all;
-        rerank_batch(ctx, RS, S.rows, S.kc, S.cand_idx, S.cand_val, S.nrm, c1, c2, B->nfailed + g);
+        int64_t max_n = 1;
+        for (int q : S.probs)
+            max_n = std::max<int64_t>(max_n, B->hp[q].N);
+        rerank_batch(ctx, RS, S.rows, max_n, S.kc, S.cand_idx, S.cand_val, S.nrm, c1, c2, B->nfailed + 4 * g);
     }
     for (KGroup& K : B->kg)
     {
@@ -808,7 +811,7 @@ void plan(tk_batch* B, const tk_batch_problem* problems, int count)
     B->row_prob_out = dalloc<int32_t>(own, (size_t)B->total_rows);
     B->idx_all = dalloc<int32_t>(own, (size_t)B->total_idx);
     B->w_all = dalloc<double>(own, (size_t)B->total_idx);
-    B->nfailed = dalloc<unsigned>(own, B->sg.size());
+    B->nfailed = dalloc<unsigned>(own, 4 * B->sg.size());  // re-rank counters, 4 per screen group
     B->H = dalloc<float>(own, (size_t)P * 3 * B_DMAX);
     B->r_bits = dalloc<unsigned>(own, P);
     upload(B->probs, B->hp, st);
@@ -983,14 +986,16 @@ int tk_batch_get_info(tk_batch* B, int p, tk_operator_info* info)
         const int64_t r0 = h.out_row0 - K.out_row0;
         TK_CUDA(cudaMemcpy(&ends[0], K.row_ptr + r0, sizeof(int64_t), cudaMemcpyDeviceToHost));
         TK_CUDA(cudaMemcpy(&ends[1], K.row_ptr + r0 + h.N, sizeof(int64_t), cudaMemcpyDeviceToHost));
-        unsigned nf = 0;
-        TK_CUDA(cudaMemcpy(&nf, B->nfailed + h.group, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        unsigned cnt[4] = {};
+        TK_CUDA(cudaMemcpy(cnt, B->nfailed + 4 * h.group, sizeof(cnt), cudaMemcpyDeviceToHost));
         std::memset(info, 0, sizeof(*info));
         info->n = h.N;
         info->k = h.k;
         info->method = TK_METHOD_KLLE;
         info->nnz = ends[1] - ends[0];
-        info->rows_uncertified = nf;  // of the problem's screen group
+        info->rows_uncertified = cnt[0];  // of the problem's screen group
+        info->tie_rows = cnt[1];
+        info->extra_rows = cnt[2];
         info->stage_ms[4] = B->last_ms;
     });
 }

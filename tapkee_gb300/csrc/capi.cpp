@@ -8,6 +8,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "tk_internal.h"
 
@@ -417,6 +418,37 @@ int tk_knn_brute(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_
             stats->rows_uncertified = nf;
             stats->candidates = candidates_for(k);
             stats->screen = screen;
+            stats->tie_rows = ctx->knn_ties;
+            stats->extra_rows = ctx->knn_extra;
+        }
+    });
+}
+
+int tk_knn_extra_rows(tk_ctx* ctx, int32_t* rows, int32_t* extra, int64_t capacity, int64_t* count)
+{
+    return guarded(ctx, [&] {
+        if (!count || capacity < 0)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        *count = ctx->knn_extra;
+        const int64_t n = std::min<int64_t>(capacity, ctx->knn_extra);
+        if (n <= 0 || (!rows && !extra))
+            return;
+        std::vector<int32_t> pairs((size_t)(2 * n));
+        const void* src = ctx->scratch.bufs["rerank.extra"].ptr;
+        TK_CUDA(cudaMemcpyAsync(pairs.data(), src, sizeof(int32_t) * (size_t)(2 * n), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+        // rows in ascending order (the device appends them in completion order)
+        std::vector<std::pair<int32_t, int32_t>> pr((size_t)n);
+        for (int64_t e = 0; e < n; ++e)
+            pr[(size_t)e] = {pairs[(size_t)(2 * e)], pairs[(size_t)(2 * e + 1)]};
+        std::sort(pr.begin(), pr.end());
+        for (int64_t e = 0; e < n; ++e)
+        {
+            if (rows)
+                rows[e] = pr[(size_t)e].first;
+            if (extra)
+                extra[e] = pr[(size_t)e].second;
         }
     });
 }
@@ -757,6 +789,8 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
         o.connectivity_retries = retries;
         o.nnz = nnz;
         o.rows_uncertified = uncert;
+        o.tie_rows = ctx->knn_ties;
+        o.extra_rows = ctx->knn_extra;
         o.stage_ms[0] = ms_knn;
         o.stage_ms[1] = ms_conn;
         o.stage_ms[2] = elapsed(ctx->ev[4], ctx->ev[5]);

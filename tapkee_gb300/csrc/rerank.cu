@@ -22,11 +22,28 @@
 // goes to the fallback, which scans all N points with an FP32 direct-difference
 // filter (relative error <= (D + 4) 2^-23) against e_k, then ranks the few
 // survivors in FP64.
+//
+// Ties at the k-boundary. The reference keeps the first k + 1 records of
+// std::nth_element(begin, begin + k + 1, end) over all N (point, distance)
+// records in index order, minus the query itself (neighbors/neighbors.hpp:
+// 129-146), so exact ties across the boundary are broken by the positions the
+// partition leaves them in, not by index. A row whose k-th and (k + 1)-th
+// nearest exact distances lie within 1e-12 relative is a tie row: it is counted,
+// and k_nth_select recomputes it with a restatement of libstdc++'s introselect
+// over the row's N records, taking the first k + 1 records minus the query, in
+// partition order. When the query has k + 1 or more exact duplicates it can fall
+// outside those k + 1 records; the reference then returns k + 1 neighbours for
+// the row. Such rows are counted and listed with their (k + 1)-th neighbour; the
+// first k are returned, which is what the reference's weight and connectivity
+// routines read (they take k from neighbors[0].size(): routines/
+// locally_linear.hpp:96, neighbors/connected.hpp:27).
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
 
 #include "ff.cuh"
+#include "nth_select.h"
 #include "tk_internal.h"
 
 namespace tk {
@@ -153,7 +170,8 @@ constexpr int RR_WARPS = 8;
 template <int KC, bool BATCH>
 __global__ void __launch_bounds__(RR_WARPS * 32)
     k_rerank(const RowSpace RS, int64_t rows, const float* nrm, const int32_t* cand_idx, const float* cand_val,
-             float c1, float c2, int32_t* failed, double* failed_ub, unsigned* nfailed)
+             float c1, float c2, int32_t* failed, double* failed_ub, unsigned* nfailed, int32_t* tie_list,
+             unsigned* ntie)
 {
     constexpr int PER = (KC + 31) / 32;
     constexpr int NONE = 0x7fffffff - 255;  // slots >= NONE hold no candidate
@@ -373,6 +391,34 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                     if (V.d2_out)
                         V.d2_out[i * k + rank[s]] = (double)kh[s] + (double)kl[s];
                 }
+            // tie row: ranks k - 1 and k both exact and within 1e-12 relative.
+            // Where their FP32 intervals do not overlap (a relative gap of at
+            // least ~2^-21) they were not refined, and the row is no tie row.
+            unsigned h1 = 0u, h2 = 0u;
+            double v1 = 0.0, v2 = 0.0;
+#pragma unroll
+            for (int s = 0; s < PER; ++s)
+            {
+                if (rank[s] == k - 1 && exact[s])
+                {
+                    h1 = 1u;
+                    v1 = (double)kh[s] + (double)kl[s];
+                }
+                if (rank[s] == k && exact[s] && j[s] < NONE)
+                {
+                    h2 = 1u;
+                    v2 = (double)kh[s] + (double)kl[s];
+                }
+            }
+            const unsigned b1 = __ballot_sync(0xffffffffu, h1 != 0u);
+            const unsigned b2 = __ballot_sync(0xffffffffu, h2 != 0u);
+            if (b1 && b2)
+            {
+                const double a = __shfl_sync(0xffffffffu, v1, __ffs(b1) - 1);
+                const double b = __shfl_sync(0xffffffffu, v2, __ffs(b2) - 1);
+                if (lane == 0 && b - a <= 1e-12 * b)
+                    tie_list[atomicAdd(ntie, 1u)] = (int32_t)p;
+            }
         }
         else if (lane == 0)
         {
@@ -386,11 +432,14 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
 // Exact fallback: one CTA per failed row (persistent over the failed list).
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_fallback(const RowSpace RS, const int32_t* failed,
-                                                  const double* failed_ub, const unsigned* nfailed, unsigned* err)
+                                                  const double* failed_ub, const unsigned* nfailed, unsigned* err,
+                                                  int32_t* tie_list, unsigned* ntie)
 {
     __shared__ int32_t sj[FB_CAP];
     __shared__ double sd[FB_CAP];
     __shared__ unsigned cnt;
+    __shared__ double edge[2];  // exact distances of ranks k - 1 and k
+    __shared__ int edge_n;
     const unsigned nf = *nfailed;
     for (unsigned f = blockIdx.x; f < nf; f += gridDim.x)
     {
@@ -412,7 +461,10 @@ __global__ void __launch_bounds__(256) k_fallback(const RowSpace RS, const int32
         const double slack = (double)(D + 8) * 1.1920928955078125e-07;
         const float thr = (float)(ub * (1.0 + slack)) * 1.0000005f + 1e-30f;
         if (threadIdx.x == 0)
+        {
             cnt = 0;
+            edge_n = 0;
+        }
         __syncthreads();
         for (int64_t jj = threadIdx.x; jj < N; jj += blockDim.x)
         {
@@ -455,8 +507,85 @@ __global__ void __launch_bounds__(256) k_fallback(const RowSpace RS, const int32
                 if (d2_out)
                     d2_out[i * k + r] = sd[t];
             }
+            // the (k + 1)-th nearest is a survivor whenever it ties with the k-th:
+            // the filter keeps every point up to the k-th distance's upper bound
+            if (r + 1 == (unsigned)k || r == (unsigned)k)
+            {
+                edge[r - (k - 1)] = sd[t];
+                atomicAdd(&edge_n, 1);
+            }
         }
         __syncthreads();
+        if (threadIdx.x == 0 && edge_n == 2 && edge[1] - edge[0] <= 1e-12 * edge[1])
+            tie_list[atomicAdd(ntie, 1u)] = (int32_t)p;
+        __syncthreads();
+    }
+}
+
+// One CTA per tie row (persistent over the tie list). The CTA computes the row's
+// N exact distances into its slot of the record scratch (N doubles and N ints),
+// then thread 0 runs the selection and writes the first k records of the first
+// k + 1 minus the query, in partition order. A row where the query is not among
+// the first k + 1 records is listed in extra (row, (k + 1)-th neighbour).
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_nth_select(const RowSpace RS, const int32_t* tie_list, const unsigned* ntie,
+                                                    double* rec_d, int32_t* rec_j, int64_t rec_stride,
+                                                    int32_t* extra, unsigned* nextra, unsigned* err)
+{
+    const unsigned nt = *ntie;
+    double* d = rec_d + (int64_t)blockIdx.x * rec_stride;
+    int32_t* jv = rec_j + (int64_t)blockIdx.x * rec_stride;
+    for (unsigned t = blockIdx.x; t < nt; t += gridDim.x)
+    {
+        const int64_t p = tie_list[t];
+        RowView V;
+        if (!row_view<BATCH>(RS, p, V))
+            continue;
+        const int64_t N = V.N, i = V.i;
+        const int k = V.k;
+        __syncthreads();  // the previous row's records are no longer read
+        for (int64_t m = threadIdx.x; m < N; m += blockDim.x)
+        {
+            d[m] = exact_d2(V.X, V.dtype, V.ldx, V.D, i, m);
+            jv[m] = (int32_t)m;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            NthSelect S{d, jv, false};
+            S.nth_element(N, (int64_t)k + 1);
+            if (S.bad)
+                atomicOr(err, DEV_ERR_NONFINITE);
+            else
+            {
+                const int64_t top = ((int64_t)k + 1 < N) ? (int64_t)k + 1 : N;
+                int c = 0;
+                int32_t last_other = -1;
+                for (int64_t m = 0; m < top; ++m)
+                {
+                    if (jv[m] == (int32_t)i)
+                        continue;
+                    if (c < k)
+                    {
+                        V.idx_out[i * k + c] = jv[m];
+                        if (V.d2_out)
+                            V.d2_out[i * k + c] = d[m];
+                        ++c;
+                    }
+                    else
+                        last_other = jv[m];
+                }
+                if (last_other >= 0)
+                {
+                    const unsigned e = atomicAdd(nextra, 1u);
+                    if (extra)
+                    {
+                        extra[2 * e] = (int32_t)i;
+                        extra[2 * e + 1] = last_other;
+                    }
+                }
+            }
+        }
     }
 }
 
@@ -502,17 +631,29 @@ void screen_error_model(int screen, int Dp, float* c1, float* c2)
 
 namespace {
 
+// Counters of one re-rank pass (device, 16 bytes, cleared by launch_rerank):
+// [0] uncertified rows, [1] tie rows, [2] rows with k + 1 reference neighbours.
+constexpr int CNT_FAILED = 0, CNT_TIES = 1, CNT_EXTRA = 2;
+
+// CTAs of the tie-row selection: each holds a row's N records (12 B each) in
+// the scratch, which is kept to about 64 MB.
+int select_grid(tk_ctx* ctx, int64_t max_n)
+{
+    const int64_t per = std::max<int64_t>(max_n, 1) * 12;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(2 * ctx->num_sms, ((int64_t)64 << 20) / per));
+}
+
 template <bool BATCH>
 void launch_rerank(tk_ctx* ctx, const RowSpace& S, int64_t rows, int kc, const int32_t* cand_idx,
                    const float* cand_val, const float* nrm, float eps_c1, float eps_c2, int32_t* failed,
-                   double* failed_ub, unsigned* nfailed)
+                   double* failed_ub, int32_t* ties, unsigned* counts)
 {
     cudaStream_t st = ctx->stream;
-    TK_CUDA(cudaMemsetAsync(nfailed, 0, sizeof(unsigned), st));
+    TK_CUDA(cudaMemsetAsync(counts, 0, 4 * sizeof(unsigned), st));
     const int blocks = 8 * ctx->num_sms;
 #define TK_RERANK(KCV)                                                                                         \
     k_rerank<KCV, BATCH><<<blocks, RR_WARPS * 32, 0, st>>>(S, rows, nrm, cand_idx, cand_val, eps_c1, eps_c2, failed,    \
-                                                    failed_ub, nfailed)
+                                                    failed_ub, counts + CNT_FAILED, ties, counts + CNT_TIES)
     if (kc == 32)
         TK_RERANK(32);
     else if (kc == 64)
@@ -525,7 +666,8 @@ void launch_rerank(tk_ctx* ctx, const RowSpace& S, int64_t rows, int kc, const i
         throw Error(TK_ERR_INTERNAL, "rerank: unsupported candidate count");
 #undef TK_RERANK
     TK_CHECK_LAUNCH();
-    k_fallback<BATCH><<<ctx->num_sms, 256, 0, st>>>(S, failed, failed_ub, nfailed, ctx->dev_err);
+    k_fallback<BATCH><<<ctx->num_sms, 256, 0, st>>>(S, failed, failed_ub, counts + CNT_FAILED, ctx->dev_err, ties,
+                                                    counts + CNT_TIES);
     TK_CHECK_LAUNCH();
 }
 
@@ -539,7 +681,8 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
     const int64_t N = P.N;
     int32_t* failed = (int32_t*)ctx->scratch.get("rerank.failed", sizeof(int32_t) * (size_t)N);
     double* failed_ub = (double*)ctx->scratch.get("rerank.failed_ub", sizeof(double) * (size_t)N);
-    unsigned* nfailed = (unsigned*)ctx->scratch.get("rerank.nfailed", 16);
+    int32_t* ties = (int32_t*)ctx->scratch.get("rerank.ties", sizeof(int32_t) * (size_t)N);
+    unsigned* counts = (unsigned*)ctx->scratch.get("rerank.nfailed", 16);
     RowSpace S;
     S.X = X;
     S.dtype = dtype;
@@ -553,18 +696,48 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
     S.d2_out = d2_out;
     S.far_val = P.far_val;
     S.c2_far = P.c2_far;
-    launch_rerank<false>(ctx, S, N, kc, cand_idx, cand_val, P.nrm, eps_c1, eps_c2, failed, failed_ub, nfailed);
-    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, nfailed, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    launch_rerank<false>(ctx, S, N, kc, cand_idx, cand_val, P.nrm, eps_c1, eps_c2, failed, failed_ub, ties, counts);
+    unsigned* hc = reinterpret_cast<unsigned*>(ctx->host_i64);
+    TK_CUDA(cudaMemcpyAsync(hc, counts, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     TK_CUDA(cudaStreamSynchronize(st));
-    return (int64_t) * reinterpret_cast<unsigned*>(ctx->host_i64);
+    const int64_t nfailed = hc[CNT_FAILED];
+    const int64_t nties = hc[CNT_TIES];
+    ctx->knn_ties = nties;
+    ctx->knn_extra = 0;
+    if (nties > 0)
+    {
+        // the reference's selection for the tie rows (rare: exact ties occur in
+        // duplicated or lattice data, not in continuous noise)
+        const int grid = select_grid(ctx, N);
+        double* rec_d = (double*)ctx->scratch.get("rerank.sel_d", sizeof(double) * (size_t)grid * N);
+        int32_t* rec_j = (int32_t*)ctx->scratch.get("rerank.sel_j", sizeof(int32_t) * (size_t)grid * N);
+        int32_t* extra = (int32_t*)ctx->scratch.get("rerank.extra", sizeof(int32_t) * 2 * (size_t)nties);
+        k_nth_select<false><<<grid, 256, 0, st>>>(S, ties, counts + CNT_TIES, rec_d, rec_j, N, extra,
+                                                  counts + CNT_EXTRA, ctx->dev_err);
+        TK_CHECK_LAUNCH();
+        TK_CUDA(cudaMemcpyAsync(hc, counts, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        TK_CUDA(cudaStreamSynchronize(st));
+        ctx->knn_extra = hc[CNT_EXTRA];
+    }
+    return nfailed;
 }
 
-void rerank_batch(tk_ctx* ctx, const RowSpace& S, int64_t rows, int kc, const int32_t* cand_idx,
-                  const float* cand_val, const float* nrm, float eps_c1, float eps_c2, unsigned* nfailed_out)
+void rerank_batch(tk_ctx* ctx, const RowSpace& S, int64_t rows, int64_t max_n, int kc, const int32_t* cand_idx,
+                  const float* cand_val, const float* nrm, float eps_c1, float eps_c2, unsigned* counts_out)
 {
     int32_t* failed = (int32_t*)ctx->scratch.get("rerank.failed", sizeof(int32_t) * (size_t)rows);
     double* failed_ub = (double*)ctx->scratch.get("rerank.failed_ub", sizeof(double) * (size_t)rows);
-    launch_rerank<true>(ctx, S, rows, kc, cand_idx, cand_val, nrm, eps_c1, eps_c2, failed, failed_ub, nfailed_out);
+    int32_t* ties = (int32_t*)ctx->scratch.get("rerank.ties", sizeof(int32_t) * (size_t)rows);
+    launch_rerank<true>(ctx, S, rows, kc, cand_idx, cand_val, nrm, eps_c1, eps_c2, failed, failed_ub, ties,
+                        counts_out);
+    // the selection reads the tie count on the device (no host synchronisation
+    // inside a captured batch); extra rows are counted, not listed
+    const int grid = select_grid(ctx, max_n);
+    double* rec_d = (double*)ctx->scratch.get("rerank.sel_d", sizeof(double) * (size_t)grid * max_n);
+    int32_t* rec_j = (int32_t*)ctx->scratch.get("rerank.sel_j", sizeof(int32_t) * (size_t)grid * max_n);
+    k_nth_select<true><<<grid, 256, 0, ctx->stream>>>(S, ties, counts_out + CNT_TIES, rec_d, rec_j, max_n, nullptr,
+                                                      counts_out + CNT_EXTRA, ctx->dev_err);
+    TK_CHECK_LAUNCH();
 }
 
 } // namespace tk

@@ -103,6 +103,8 @@ struct tk_ctx
     int64_t* host_i64 = nullptr;      // pinned small readback area (16 entries)
     cudaEvent_t ev[12] = {};
     float screen_ms = 0.f;            // device time of the last distance screen
+    int64_t knn_ties = 0;             // tie rows of the last brute kNN pass
+    int64_t knn_extra = 0;            // rows of that pass with k + 1 reference neighbours
     int num_sms = 0;
     // operator held by the context
     tk_operator_info op{};
@@ -187,12 +189,17 @@ struct RowSpace
 // problem row_prob[g]); warps = warps per block of the solve kernel (4 or 8).
 void lle_weights_batch(tk_ctx* ctx, const BatchProb* probs, const int32_t* row_prob, int64_t out_row0, int64_t rows,
                        const int32_t* idx, int k, double klle_shift, double* W, int warps);
-void rerank_batch(tk_ctx* ctx, const RowSpace& S, int64_t rows, int kc, const int32_t* cand_idx,
-                  const float* cand_val, const float* nrm, float eps_c1, float eps_c2, unsigned* nfailed_out);
+// counts_out: 4 device counters (uncertified rows, tie rows, rows with k + 1
+// reference neighbours, unused); max_n bounds the group's problem sizes.
+void rerank_batch(tk_ctx* ctx, const RowSpace& S, int64_t rows, int64_t max_n, int kc, const int32_t* cand_idx,
+                  const float* cand_val, const float* nrm, float eps_c1, float eps_c2, unsigned* counts_out);
 bool tensor_screen_supported(int Dp);
 
-// rerank.cu: exact FP64 re-rank, certification and exact fallback.
-// Returns the number of uncertified rows (device -> host read).
+// rerank.cu: exact FP64 re-rank, certification, exact fallback, and the
+// reference's nth_element selection for tie rows. Returns the number of
+// uncertified rows (device -> host read); sets ctx->knn_ties and ctx->knn_extra
+// and leaves the extra rows as (row, (k + 1)-th neighbour) pairs in the scratch
+// buffer "rerank.extra".
 int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t ldx, int k, int kc,
                const int32_t* cand_idx, const float* cand_val, float eps_c1, float eps_c2, int32_t* idx_out,
                double* d2_out);

@@ -1,7 +1,8 @@
 """Brute kNN through the C ABI vs the CPU oracle (GPU).
 
-Bar: neighbour index sets bit-exact; rows ordered by (FP64 distance, index);
-squared distances equal to FP64 within 1e-12 relative."""
+Bar: neighbour index sets bit-exact; rows ordered by (FP64 distance, index),
+except tie rows, which hold the reference's partition order; squared distances
+equal to FP64 within 1e-12 relative."""
 import numpy as np
 import pytest
 
@@ -64,16 +65,68 @@ def test_small_and_ragged_sizes(ctx, screen):
         assert np.array_equal(idx, _ordered(X, ref)[0]), (n, k)
 
 
-@pytest.mark.parametrize("screen", SCREENS)
-def test_duplicate_points_tie_break_by_index(ctx, screen):
-    # 40 copies of 5 distinct points: many exact ties; ties resolve by index
+def _tie_rows(X, k):
+    """Rows whose k-th and (k+1)-th nearest other points are at distances within
+    1e-12 relative (exact squared distances, numpy FP64)."""
+    X = np.asarray(X, np.float64)
+    d = ((X[:, None, :] - X[None, :, :]) ** 2).sum(-1)
+    np.fill_diagonal(d, np.inf)
+    d.sort(axis=1)
+    if k >= len(X) - 1:
+        return np.zeros(len(X), bool)
+    return d[:, k] - d[:, k - 1] <= 1e-12 * d[:, k]
+
+
+def _lattice(shape, dtype):
+    g = np.stack(np.meshgrid(*[np.arange(s) for s in shape], indexing="ij"), -1).reshape(-1, len(shape))
+    return np.ascontiguousarray(g[np.random.default_rng(3).permutation(len(g))], dtype=dtype)
+
+
+def _duplicates(dtype):
     base = np.random.default_rng(1).normal(size=(5, 3))
-    X = np.repeat(base, 40, axis=0).astype(np.float64)
-    k = 6
-    idx = ctx.knn_brute(X, k, screen=screen)
+    return np.ascontiguousarray(np.repeat(base, 40, axis=0), dtype=dtype)
+
+
+TIE_CASES = [
+    ("40 copies of 5 points, k=3", lambda dt: _duplicates(dt), 3),
+    ("40 copies of 5 points, k=6", lambda dt: _duplicates(dt), 6),
+    ("40 copies of 5 points, k=45", lambda dt: _duplicates(dt), 45),
+    ("integer line, k=3", lambda dt: np.arange(300, dtype=dt).reshape(300, 1), 3),
+    ("integer line, k=11", lambda dt: np.arange(300, dtype=dt).reshape(300, 1), 11),
+    ("2-D integer grid 40x40, k=10", lambda dt: _lattice((40, 40), dt), 10),
+    ("2-D integer grid 40x40, k=6", lambda dt: _lattice((40, 40), dt), 6),
+    ("3-D integer grid 12^3, k=12", lambda dt: _lattice((12, 12, 12), dt), 12),
+]
+
+
+@pytest.mark.parametrize("screen", SCREENS)
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("case", range(len(TIE_CASES)))
+def test_ties_follow_the_reference_partition(ctx, screen, dtype, case):
+    """Exact ties at the k-boundary (duplicated points, integer lattices): every
+    row's set equals the oracle's (std::nth_element at k + 1 over the row's
+    records in index order, minus the query: neighbors/neighbors.hpp:129-146);
+    tie rows keep the partition order itself; the tie rows are counted; and the
+    rows for which the reference returns k + 1 neighbours are listed with their
+    (k + 1)-th neighbour."""
+    name, make, k = TIE_CASES[case]
+    X = make(dtype)
+    idx, st = ctx.knn_brute(X, k, screen=screen, return_stats=True)
+    ref, _, cnt, extra = oracle.knn_brute(X, k, return_extra=True)
     for i in range(len(X)):
-        same = [j for j in range(len(X)) if j != i and (X[j] == X[i]).all()]
-        assert idx[i].tolist() == same[:k]
+        assert set(idx[i].tolist()) == set(ref[i].tolist()), (name, i)
+    ties = _tie_rows(X, k)
+    assert st["tie_rows"] == int(ties.sum()) and ties.sum() > 0, name
+    assert np.array_equal(idx[ties], ref[ties]), name  # partition order on tie rows
+    want = [(int(i), int(extra[i])) for i in np.nonzero(cnt == k + 1)[0]]
+    assert st["extra_rows"] == len(want), name
+    assert st.get("extra", []) == want, name
+
+
+def test_continuous_data_has_no_tie_rows(ctx):
+    X = datasets.lifted_swiss_roll(20_000, 64, seed=4)
+    _, st = ctx.knn_brute(X, 16, return_stats=True)
+    assert st["tie_rows"] == 0 and st["extra_rows"] == 0
 
 
 def test_invalid_arguments(ctx):
