@@ -144,6 +144,7 @@ def main():
     ap.add_argument("--no-ltsa", action="store_true")
     ap.add_argument("--no-eigen", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-default-connectivity", action="store_true")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--check-connectivity", type=int, default=0)
     args = ap.parse_args()
@@ -263,6 +264,36 @@ def main():
         fp32 = {"value": args.n / (ms_f / 1000.0), "unit": "points/s", "ms_per_step": ms_f,
                 "screen_kernel_ms": float(np.mean([i.stage_ms[5] for i in inf_f])),
                 "tc_over_fp32": ms_f / ms_step}
+
+    # the reference's default path on the same workload: check_connectivity=true
+    # (defines/keywords.hpp:272) doubles k while the directed kNN graph is not
+    # reachable from vertex 0 (neighbors/neighbors.hpp:196-204); same timing rules
+    default_conn = None
+    if not args.no_default_connectivity and not CHECK:
+        for _ in range(2):
+            ctx.local_operator(Xd, "lle", num_neighbors=args.k, klle_shift=1e-3, check_connectivity=True,
+                               copy_out=False)
+        ct, cinf = [], []
+        for _ in range(3):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            cinf.append(ctx.local_operator(Xd, "lle", num_neighbors=args.k, klle_shift=1e-3,
+                                           check_connectivity=True, copy_out=False))
+            e1.record(stream)
+            e1.synchronize()
+            ct.append(e0.elapsed_time(e1))
+        cms = float(np.mean(ct))
+        ci = cinf[-1]
+        default_conn = {"check_connectivity": True, "k_final": int(ci.k),
+                        "connectivity_retries": int(ci.connectivity_retries), "ms_per_step": cms,
+                        "points_per_s": args.n / (cms / 1000.0),
+                        "stage_ms": {"knn_all_passes": float(np.mean([i.stage_ms[0] for i in cinf])),
+                                     "connectivity_bfs_all_passes": float(np.mean([i.stage_ms[1] for i in cinf])),
+                                     "weights": float(np.mean([i.stage_ms[2] for i in cinf])),
+                                     "assembly": float(np.mean([i.stage_ms[3] for i in cinf]))},
+                        "tie_rows": int(ci.tie_rows), "nnz": int(ci.nnz)}
 
     # LTSA workload (lifted S-curve N=50000 D=32 k=20 td=2, float32): same timing
     # rules, reported beside the headline
@@ -397,7 +428,7 @@ def main():
             "data": "synthetic (seeded lifted Swiss roll)", "config": workload, "stage_ms": stage,
             "rows_uncertified": int(info.rows_uncertified), "tie_rows": int(info.tie_rows),
             "extra_neighbor_rows": int(info.extra_rows), "nnz": nnz, "k_used": kk,
-            "fp32_path": fp32, "ltsa": ltsa, "eigen": eigen, "batch": batch, "roofline": roofline,
+            "fp32_path": fp32, "default_connectivity": default_conn, "ltsa": ltsa, "eigen": eigen, "batch": batch, "roofline": roofline,
             "e2e": {"value": args.n / (e2e_ms / 1000.0), "unit": "points/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clocks, "gpu_launches": int(launches)}

@@ -57,11 +57,12 @@ typedef enum tk_dtype
     TK_F64 = 1
 } tk_dtype;
 
-/* Method tags (defines/methods.hpp:74,82). */
+/* Method tags (defines/methods.hpp:74,82,90). */
 typedef enum tk_method
 {
-    TK_METHOD_KLLE = 0, /* KernelLocallyLinearEmbedding            */
-    TK_METHOD_KLTSA = 1 /* KernelLocalTangentSpaceAlignment         */
+    TK_METHOD_KLLE = 0,  /* KernelLocallyLinearEmbedding            */
+    TK_METHOD_KLTSA = 1, /* KernelLocalTangentSpaceAlignment         */
+    TK_METHOD_HLLE = 2   /* HessianLocallyLinearEmbedding           */
 } tk_method;
 
 /* Distance screening engine of the brute kNN. Both are followed by the same
@@ -219,11 +220,23 @@ int tk_lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D,
 int tk_ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
                   int k, int td, double* V_out);
 
+/* Hessian LLE basis: per point, the product columns Yr (k x dp, dp = td (td+1)/2)
+ * of the orthonormalised [1, V, v_j v_l] built from the LTSA tangent basis V;
+ * the point's Hessian block is B = Yr Yr^T. Y_out is N x k x dp. Replaces the
+ * per-point part of hessian_weight_matrix (routines/locally_linear.hpp:183-234).
+ * td must be 1 or 2 (the reference places the product columns correctly only
+ * for those, :208-214) and k > td + dp. */
+int tk_hessian_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                     int k, int td, double* Y_out);
+
 /* Sparse alignment matrix M in CSR (= CSC, M is symmetric), duplicates summed:
  *   TK_METHOD_KLLE : M = (I - W)^T (I - W) + shift I   from weights = W (N x k)
  *                    (triplets of routines/locally_linear.hpp:133-146)
  *   TK_METHOD_KLTSA: M = shift I + sum_i S_i^T (I - P_i) S_i from weights = V
  *                    (N x k x td) (triplets of routines/locally_linear.hpp:65-77)
+ *   TK_METHOD_HLLE : M = sum_i S_i^T B_i S_i, B_i = Y_i Y_i^T, from weights = Y
+ *                    (N x k x td(td+1)/2, tk_hessian_basis); shift unused
+ *                    (triplets of routines/locally_linear.hpp:236-243)
  * followed by sparse_matrix_from_triplets (utils/sparse.hpp:16-21).
  * Columns are ascending within each row. Two-phase: with col_idx == NULL the
  * call only writes row_ptr (if non-NULL) and *nnz_io = nnz; with buffers whose

@@ -28,7 +28,7 @@ TK_ERR_NOT_CONVERGED = 11
 
 TK_F32, TK_F64 = 0, 1
 TK_NOALLOC_MAX_POINTS = 2097152
-TK_METHOD_KLLE, TK_METHOD_KLTSA = 0, 1
+TK_METHOD_KLLE, TK_METHOD_KLTSA, TK_METHOD_HLLE = 0, 1, 2
 TK_SCREEN_TENSOR, TK_SCREEN_FP32 = 0, 1
 
 CANCEL_FN = ctypes.CFUNCTYPE(ctypes.c_int)
@@ -109,6 +109,7 @@ SIGNATURES = {
     "tk_lle_weights": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P]),
     "tk_lle_weights_grad": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _D, _P, _P, _P]),
     "tk_ltsa_basis": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _I, _P]),
+    "tk_hessian_basis": (_I, [_P, _P, _I, _I64, _I, _I64, _P, _I, _I, _P]),
     "tk_assemble": (_I, [_P, _I, _I64, _I, _I, _P, _P, _D, _P, _P, _P, ctypes.POINTER(_I64)]),
     "tk_eigenproblem_pair": (_I, [_P, _I, _P, _I, _I64, _I, _I64, _P, _P, _P, _P, _P]),
     "tk_smallest_eigenvectors": (_I, [_P, _I64, _P, _P, _P, _I, _I, _D, _I64, _P, _P,

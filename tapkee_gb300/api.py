@@ -86,6 +86,8 @@ METHODS = {
     "ltsa": C.TK_METHOD_KLTSA,
     "local_tangent_space_alignment": C.TK_METHOD_KLTSA,
     "kltsa": C.TK_METHOD_KLTSA,
+    "hlle": C.TK_METHOD_HLLE,
+    "hessian_locally_linear_embedding": C.TK_METHOD_HLLE,
 }
 SCREENS = {"tensor": C.TK_SCREEN_TENSOR, "fp32": C.TK_SCREEN_FP32}
 
@@ -334,13 +336,30 @@ class Context:
         self._check(self.lib.tk_ltsa_basis(self.ptr, xb.ptr, dt, N, D, D, ib.ptr, k, int(target_dimension), V.ptr))
         return V.arr
 
-    def assemble(self, method, idx, weights, shift):
-        """M in CSR (routines/locally_linear.hpp:133-146 / :65-77 + utils/sparse.hpp:16-21)."""
+    def hessian_basis(self, X, idx, target_dimension=2):
+        """Hessian LLE product columns Yr (N x k x td(td+1)/2); the point's block
+        is B = Yr Yr^T (routines/locally_linear.hpp:183-234)."""
+        xb, dt = _as_points(X)
+        ib = _as_index(idx, xb)
+        N, D = xb.arr.shape
+        k = ib.arr.shape[1]
+        td = int(target_dimension)
+        Y = _empty((N, k, td * (td + 1) // 2), np.float64, xb)
+        self._check(self.lib.tk_hessian_basis(self.ptr, xb.ptr, dt, N, D, D, ib.ptr, k, td, Y.ptr))
+        return Y.arr
+
+    def assemble(self, method, idx, weights, shift, target_dimension=None):
+        """M in CSR (routines/locally_linear.hpp:133-146 / :65-77 / :236-243 +
+        utils/sparse.hpp:16-21). weights: W (N x k) for LLE, V (N x k x td) for
+        LTSA, Yr (N x k x td(td+1)/2) for HLLE, whose target_dimension is derived
+        from the column count unless given."""
         m = METHODS[method] if isinstance(method, str) else int(method)
         ib = _as_index(idx, None)
         wb = _as_f64(weights)
         N, k = ib.arr.shape
         td = wb.arr.shape[2] if wb.arr.ndim == 3 else 0
+        if m == C.TK_METHOD_HLLE:
+            td = int(target_dimension) if target_dimension is not None else {1: 1, 3: 2}.get(td, 0)
         rp = _empty((N + 1,), np.int64, wb)
         nnz = ctypes.c_int64(0)
         self._check(self.lib.tk_assemble(self.ptr, m, N, k, td, ib.ptr, wb.ptr, float(shift), rp.ptr, None, None,
@@ -402,7 +421,8 @@ class Context:
     def local_operator(self, X, method="lle", num_neighbors=5, target_dimension=2, klle_shift=1e-3,
                        nullspace_shift=1e-9, check_connectivity=True, screen="tensor", cancel_function=None,
                        copy_out=True):
-        """The whole stage of KLLE/KLTSA embed() up to the eigensolver."""
+        """The whole stage of KLLE / KLTSA / HLLE embed() up to the eigensolver.
+        HLLE adds no diagonal shift (nullspace_shift and klle_shift are unused)."""
         if method not in METHODS:
             raise UnsupportedMethodError(f"method {method!r} is not provided by this library")
         xb, dt = _as_points(X)
@@ -428,7 +448,7 @@ class Context:
         if not copy_out:
             return info
         k, td = info.k, info.target_dimension
-        wshape = (N, k) if info.method == C.TK_METHOD_KLLE else (N, k, td)
+        wshape = {C.TK_METHOD_KLLE: (N, k), C.TK_METHOD_KLTSA: (N, k, td)}.get(info.method, (N, k, td * (td + 1) // 2))
         idx = _empty((N, k), np.int32, xb)
         w = _empty(wshape, np.float64, xb)
         rp = _empty((N + 1,), np.int64, xb)
@@ -456,6 +476,10 @@ def default_context() -> Context:
 # ---------------------------------------------------------------- eigensolver
 
 
+# Largest N of the dense eigensolver path (a 16384 x 16384 FP64 matrix is 2 GiB).
+DENSE_EIGEN_MAX_N = 16384
+
+
 def smallest_eigenvectors(op: LocalOperator, target_dimension: int, skip: int = 1, eigen_method: str = "arpack",
                           context=None):
     """Consumes the CSR of M unchanged and returns (vectors N x td, values td) as
@@ -466,7 +490,8 @@ def smallest_eigenvectors(op: LocalOperator, target_dimension: int, skip: int = 
       (routines/eigendecomposition.hpp:31-50,252-266). Problems smaller than four
       block widths go to the dense solver below.
     - "dense" (routines/eigendecomposition.hpp:56-87): symmetrise, self-adjoint
-      solve of the dense N x N matrix on the GPU in FP64, columns skip..skip+td."""
+      solve of the dense N x N matrix on the GPU in FP64, columns skip..skip+td;
+      refused with WrongParameterError above N = DENSE_EIGEN_MAX_N."""
     if eigen_method not in ("arpack", "dense"):
         raise UnsupportedMethodError(f"eigen_method {eigen_method!r} is not provided (use 'arpack' or 'dense')")
     n = len(op.row_ptr) - 1
@@ -477,6 +502,10 @@ def smallest_eigenvectors(op: LocalOperator, target_dimension: int, skip: int = 
             if _is_torch(E):
                 E, w = E.cpu().numpy(), w.cpu().numpy()
             return np.ascontiguousarray(E), np.asarray(w)
+    if n > DENSE_EIGEN_MAX_N:
+        raise WrongParameterError(
+            f"the dense eigensolver holds the N x N matrix in FP64 ({8 * n * n / 2**30:.1f} GiB at N = {n}); "
+            f"it accepts N <= {DENSE_EIGEN_MAX_N}: use eigen_method='arpack' (td + skip <= 14)")
     torch = _torch()
     dev = "cuda"
     rp = torch.as_tensor(np.asarray(op.row_ptr.cpu() if _is_torch(op.row_ptr) else op.row_ptr)).to(dev)
@@ -502,7 +531,7 @@ def embed(data, method="lle", neighbors_method=None, eigen_method=None, num_neig
           nullspace_shift=None, klle_shift=None, check_connectivity=None, screen="tensor", context=None,
           **unsupported):
     """Python signature of the reference module's ``embed`` for the methods this
-    library provides (KLLE, KLTSA with brute-force neighbours). ``data`` is
+    library provides (KLLE, KLTSA, HLLE with brute-force neighbours). ``data`` is
     features x samples; returns samples x target_dimension (numpy)."""
     for key, val in unsupported.items():
         if val is not None:

@@ -28,6 +28,10 @@
 //   LTSA row j: source j  -> (j, shift)
 //               source r  -> (j, +1) then (n_b, -P_r[a][b])      [j = n_a of r]
 //               P_r = (1/k) 1 1^T + V_r V_r^T
+//   HLLE row j: source r  -> (n_b, B_r[a][b])                    [j = n_a of r]
+//               B_r = Y_r Y_r^T, Y_r the dp product columns (routines/
+//               locally_linear.hpp:234-243); no diagonal term
+// For HLLE the td argument of the kernels is the column count dp of Y.
 #include <cstdint>
 
 #include "tk_internal.h"
@@ -355,17 +359,24 @@ __device__ bool process_row(RowTable<CAP>& T, int lane, int method, int64_t j, i
         }
         else
         {
+            const bool hlle = method == TK_METHOD_HLLE;
             if (slot < 0)
             {
-                if (lane == 0)
-                    ok &= table_add<CAP, VALUES>(T, (int)j, shift);
-                __syncwarp();
+                if (!hlle)
+                {
+                    if (lane == 0)
+                        ok &= table_add<CAP, VALUES>(T, (int)j, shift);
+                    __syncwarp();
+                }
             }
             else
             {
-                if (lane == 0)
-                    ok &= table_add<CAP, VALUES>(T, (int)j, 1.0);
-                __syncwarp();
+                if (!hlle)
+                {
+                    if (lane == 0)
+                        ok &= table_add<CAP, VALUES>(T, (int)j, 1.0);
+                    __syncwarp();
+                }
                 const double* Va = wts + (src * k + slot) * (int64_t)td;
                 for (int t0 = 0; t0 < k; t0 += 32)
                 {
@@ -375,10 +386,10 @@ __device__ bool process_row(RowTable<CAP>& T, int lane, int method, int64_t j, i
                     if (VALUES && valid)
                     {
                         const double* Vb = wts + (src * k + t) * (int64_t)td;
-                        double pab = 1.0 / k;
+                        double pab = hlle ? 0.0 : 1.0 / k;
                         for (int q = 0; q < td; ++q)
                             pab += Va[q] * Vb[q];
-                        v = -pab;
+                        v = hlle ? pab : -pab;
                     }
                     ok &= warp_add<CAP, VALUES>(T, lane, valid, valid ? idx[src * k + t] : 0, v);
                 }
@@ -552,6 +563,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
     const int S = STAGE / KS;      // sources per round (0 when k >= STAGE: every row takes the large table)
     const int64_t nw = (int64_t)gridDim.x * ROW_WARPS;
     const bool lle = method == TK_METHOD_KLLE;
+    const bool hlle = method == TK_METHOD_HLLE;
     const double inv_k = 1.0 / k;
     const FastDiv div_k(k), div_ks(KS);
     // no point lists itself or a neighbour twice (always so for kNN output):
@@ -619,25 +631,26 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
                     {
                         if (slot < 0)
                         {
-                            // source j: (j, shift)
-                            col = (t == 0) ? (int)j : -1;
+                            // source j: (j, shift); nothing for HLLE
+                            col = (t == 0 && !hlle) ? (int)j : -1;
                             v = shift;
                         }
                         else if (t == 0)
                         {
-                            col = (int)j;  // (j, +1), added before the row of P_r
+                            col = hlle ? -1 : (int)j;  // LTSA's (j, +1), added before the row of P_r
                             v = 1.0;
                         }
                         else
                         {
-                            // (n_b, -P_r[a][b]), P_r = (1/k) 1 1^T + V_r V_r^T
+                            // LTSA: (n_b, -P_r[a][b]), P_r = (1/k) 1 1^T + V_r V_r^T
+                            // HLLE: (n_b, B_r[a][b]),  B_r = Y_r Y_r^T
                             const double* Va = wts + (src * k + slot) * (int64_t)td;
                             const double* Vb = wts + (src * k + t - 1) * (int64_t)td;
-                            double pab = inv_k;
+                            double pab = hlle ? 0.0 : inv_k;
                             for (int q = 0; q < td; ++q)
                                 pab += Va[q] * Vb[q];
                             col = idx[src * k + t - 1];
-                            v = -pab;
+                            v = hlle ? pab : -pab;
                         }
                     }
                     F.scol[it] = col;
@@ -881,6 +894,26 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
                                                                            ctx->dev_err);
     TK_CHECK_LAUNCH();
     scan_to_offsets(ctx, a.row_nnz, N, row_ptr);
+}
+
+void reverse_lists(tk_ctx* ctx, int64_t N, int k, const int32_t* idx, int64_t* rptr, int32_t* rev)
+{
+    cudaStream_t st = ctx->stream;
+    const int64_t nk = N * (int64_t)k;
+    if (nk >= (int64_t)1 << 31)
+        throw Error(TK_ERR_UNSUPPORTED, "reverse lists support N*k < 2^31");
+    int* cnt = (int*)ctx->scratch.get("rev.cnt", sizeof(int) * (size_t)N * 2);
+    int* fillc = cnt + N;
+    unsigned* repeats = (unsigned*)ctx->scratch.get("rev.repeats", 16);
+    const int g = 4 * ctx->num_sms;
+    TK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)N * 2, st));
+    k_indeg<<<g, 256, 0, st>>>(idx, nk, N, k, cnt, repeats, ctx->dev_err);
+    TK_CHECK_LAUNCH();
+    scan_to_offsets(ctx, cnt, N, rptr);
+    k_fill_rev<<<g, 256, 0, st>>>(idx, nk, N, rptr, fillc, rev);
+    TK_CHECK_LAUNCH();
+    k_sort_rev<<<g, 256, 0, st>>>(N, rptr, rev);
+    TK_CHECK_LAUNCH();
 }
 
 int64_t assemble_rows(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx, const double* weights,

@@ -511,6 +511,27 @@ int tk_lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D,
     });
 }
 
+int tk_hessian_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                     int k, int td, double* Y_out)
+{
+    return guarded(ctx, [&] {
+        validate_points(X, dtype, N, D, ldx);
+        if (k < 1 || !idx || !Y_out)
+            throw Error(TK_ERR_INVALID_ARG, "bad arguments");
+        const size_t count = (size_t)N * k * weight_columns(TK_METHOD_HLLE, td);
+        int64_t ldd;
+        const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "io.X");
+        const int32_t* idx_d = device_array(ctx, idx, (size_t)N * k, "io.idx_in");
+        bool yh;
+        double* Y_d = device_out(ctx, Y_out, count, "io.Y", &yh);
+        hessian_basis(ctx, Xd, dtype, N, D, ldd, idx_d, k, td, Y_d);
+        check_device_errors(ctx);
+        if (yh)
+            copy_back(ctx, Y_out, Y_d, count);
+        TK_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 int tk_ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
                   int td, double* V_out)
 {
@@ -647,11 +668,12 @@ int tk_assemble(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t
     return guarded(ctx, [&] {
         if (N <= 0)
             throw Error(TK_ERR_NO_DATA, "No data");
-        if (method != TK_METHOD_KLLE && method != TK_METHOD_KLTSA)
+        if (method != TK_METHOD_KLLE && method != TK_METHOD_KLTSA && method != TK_METHOD_HLLE)
             throw Error(TK_ERR_UNSUPPORTED, "unsupported method");
-        if (k < 1 || !idx || !weights || !nnz_io || (method == TK_METHOD_KLTSA && td < 1))
+        if (k < 1 || !idx || !weights || !nnz_io || (method != TK_METHOD_KLLE && td < 1))
             throw Error(TK_ERR_INVALID_ARG, "bad arguments");
-        const size_t wcount = (size_t)N * k * (method == TK_METHOD_KLTSA ? td : 1);
+        const size_t wcount = (size_t)N * k * weight_columns(method, td);
+        td = method == TK_METHOD_KLLE ? td : weight_columns(method, td);
         const int32_t* idx_d = device_array(ctx, idx, (size_t)N * k, "io.idx_in");
         const double* w_d = device_array(ctx, weights, wcount, "io.w_in");
         bool rh = false;
@@ -692,7 +714,7 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
         if (!params)
             throw Error(TK_ERR_INVALID_ARG, "params is NULL");
         const tk_params& p = *params;
-        if (p.method != TK_METHOD_KLLE && p.method != TK_METHOD_KLTSA)
+        if (p.method != TK_METHOD_KLLE && p.method != TK_METHOD_KLTSA && p.method != TK_METHOD_HLLE)
             throw Error(TK_ERR_UNSUPPORTED, "unsupported method");
         check_dtype(dtype);
         // ImplementationBase (methods/base.hpp:38-44): no data, target dimension in [1, N)
@@ -763,20 +785,27 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
 
         // weights
         TK_CUDA(cudaEventRecord(ctx->ev[4], st));
-        const size_t wcount = (size_t)N * k * (p.method == TK_METHOD_KLTSA ? td : 1);
+        const int wcols = weight_columns(p.method, td);
+        const size_t wcount = (size_t)N * k * wcols;
         double* w_d = (double*)ctx->scratch.get("op.w", sizeof(double) * wcount);
         if (p.method == TK_METHOD_KLLE)
             lle_weights(ctx, Xd, dtype, N, D, ldd, idx_d, k, p.klle_shift, w_d);
-        else
+        else if (p.method == TK_METHOD_KLTSA)
             ltsa_basis(ctx, Xd, dtype, N, D, ldd, idx_d, k, td, w_d);
+        else
+            hessian_basis(ctx, Xd, dtype, N, D, ldd, idx_d, k, td, w_d);
+        // assembly takes the weight columns (HLLE: the dp product columns); the
+        // Hessian matrix has no diagonal shift (routines/locally_linear.hpp:236-243)
+        const int atd = p.method == TK_METHOD_KLLE ? td : wcols;
+        const double ashift = p.method == TK_METHOD_HLLE ? 0.0 : p.nullspace_shift;
         TK_CUDA(cudaEventRecord(ctx->ev[5], st));
 
         // M
         int64_t* rp_d = (int64_t*)ctx->scratch.get("op.rowptr", sizeof(int64_t) * ((size_t)N + 1));
-        const int64_t nnz = assemble_rows(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d);
+        const int64_t nnz = assemble_rows(ctx, p.method, N, k, atd, idx_d, w_d, ashift, rp_d);
         int32_t* col_d = (int32_t*)ctx->scratch.get("op.col", sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1));
         double* val_d = (double*)ctx->scratch.get("op.vals", sizeof(double) * (size_t)std::max<int64_t>(nnz, 1));
-        assemble_write(ctx, p.method, N, k, td, idx_d, w_d, p.nullspace_shift, rp_d, col_d, val_d);
+        assemble_write(ctx, p.method, N, k, atd, idx_d, w_d, ashift, rp_d, col_d, val_d);
         TK_CUDA(cudaEventRecord(ctx->ev[6], st));
         check_device_errors(ctx);
 
@@ -840,7 +869,7 @@ int tk_operator_copy(tk_ctx* ctx, int32_t* idx, double* weights, int64_t* row_pt
         const tk_operator_info& o = ctx->op;
         auto& bufs = ctx->scratch.bufs;
         const size_t nk = (size_t)o.n * o.k;
-        const size_t wc = nk * (o.method == TK_METHOD_KLTSA ? o.target_dimension : 1);
+        const size_t wc = nk * weight_columns(o.method, o.target_dimension);
         auto cp = [&](void* dst, const char* name, size_t bytes) {
             if (!dst || bytes == 0)
                 return;

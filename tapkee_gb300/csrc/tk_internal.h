@@ -222,12 +222,28 @@ void lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, i
 void ltsa_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
                 int k, int td, double* V);
 
+// hessian.cu: the dp = td (td + 1) / 2 product columns Y (N x k x dp) of every
+// point's orthonormalised Hessian basis; B = Y Y^T per point (td 1 or 2).
+void hessian_basis(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
+                   int k, int td, double* Y);
+
+// Columns per (point, neighbour) of a method's weights: LLE 1, LTSA td, HLLE
+// td (td + 1) / 2.
+inline int weight_columns(int method, int td)
+{
+    return method == TK_METHOD_KLTSA ? td : (method == TK_METHOD_HLLE ? td * (td + 1) / 2 : 1);
+}
+
 // assemble.cu: the row phase (reverse adjacency, every row's sorted columns and
 // values into a row scratch, row counts, row_ptr) returns nnz; the write phase
 // then copies the rows into col_idx/vals (device pointers) from the state kept
 // in the context's scratch.
 // Exclusive scan of n int counters into n + 1 int64 offsets (deterministic).
 void scan_to_offsets(tk_ctx* ctx, const int* in, int64_t n, int64_t* out);
+// Reverse adjacency of an N x k neighbour table: rev[rptr[j] .. rptr[j+1]) holds
+// the edge ids e = r k + a with idx[e] = j, ascending (so by source r). Entries
+// outside [0, N) are skipped and raise DEV_ERR_BOUNDS. rptr: N + 1, rev: N k.
+void reverse_lists(tk_ctx* ctx, int64_t N, int k, const int32_t* idx, int64_t* rptr, int32_t* rev);
 // The row phase without reading nnz back (row_ptr[N] holds it on the device).
 void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, const int32_t* idx,
                           const double* weights, double shift, int64_t* row_ptr);

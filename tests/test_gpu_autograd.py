@@ -87,3 +87,19 @@ def test_lle_weights_grad_entry_point_matches_adjoint_formula(ctx):
     g_ref = adjoint_numpy(X, idx, SHIFT, W, G)
     err = np.abs(Xd.grad.cpu().numpy() - g_ref).max() / np.abs(g_ref).max()
     assert err < 1e-4, err
+
+
+def test_lle_weights_grad_is_bit_reproducible(ctx):
+    """dL/dX is a pull over reverse neighbour lists in a fixed order (no atomics):
+    repeated calls give bit-identical gradients."""
+    X = datasets.lifted_swiss_roll(6000, 32, seed=2)
+    idx = ctx.knn_brute(X, 16)
+    Xd = torch.from_numpy(X).cuda()
+    idd = torch.from_numpy(idx).cuda()
+    G = torch.from_numpy(np.random.default_rng(4).normal(size=idx.shape)).cuda()
+    grads = []
+    for _ in range(3):
+        Xg = Xd.clone().requires_grad_(True)
+        (tka.lle_weights(Xg, idd, SHIFT, context=ctx) * G).sum().backward()
+        grads.append(Xg.grad.clone())
+    assert torch.equal(grads[0], grads[1]) and torch.equal(grads[0], grads[2])

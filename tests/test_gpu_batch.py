@@ -69,3 +69,59 @@ def test_batch_rejects_bad_problems(ctx):
         Batch([X], [100], context=ctx)           # k > N - 1
     with pytest.raises(UnsupportedMethodError):
         Batch([torch.randn(100, 200, device="cuda")], [5], context=ctx)  # D > 128
+
+
+def _m_rows(idx, W, rows, shift):
+    """Rows of M = (I - W)^T (I - W) + shift I from the triplet definition of
+    routines/locally_linear.hpp:133-146 (FP64, numpy): row j gathers, from every
+    source r with j = r or j among r's neighbours, u_r[j] * u_r where u_r = e_r - w_r.
+    Returns one (columns ascending, values) pair per row."""
+    N, k = idx.shape
+    flat = idx.ravel()
+    order = np.argsort(flat, kind="stable")
+    starts = np.searchsorted(flat[order], np.arange(N + 1))
+    out = []
+    for j in rows:
+        acc = {int(j): shift}
+        srcs = [(int(j), 1.0)] + [(int(e // k), -W.ravel()[e]) for e in order[starts[j]:starts[j + 1]]]
+        for r, uj in srcs:
+            acc[r] = acc.get(r, 0.0) + uj
+            for a in range(k):
+                c = int(idx[r, a])
+                acc[c] = acc.get(c, 0.0) - uj * W[r, a]
+        cols = np.array(sorted(acc), np.int64)
+        out.append((cols, np.array([acc[c] for c in cols])))
+    return out
+
+
+def test_batch_full_size_workload_vs_oracle(ctx):
+    """The whole batched workload (256 problems, N ~ U[500, 20000], D in
+    {3, 16, 64, 128}, k in {8, 12, 16, 24, 32}) in one graph: per problem, 200
+    sampled rows have the oracle's neighbour sets, weights within 1e-5 of FP64,
+    and CSR rows of M equal to the triplet definition on the returned
+    neighbours and weights (columns exact, values within 1e-12)."""
+    import torch
+    from tapkee_gb300.batch import Batch
+    specs = datasets.batch_problems(256, seed=7)
+    data = [datasets.batch_problem_data(n, d, s) for n, d, _, s in specs]
+    Xs = [torch.from_numpy(x).cuda() for x in data]
+    b = Batch(Xs, [k for _, _, k, _ in specs], context=ctx)
+    b.run()
+    rng = np.random.default_rng(5)
+    worst_w = 0.0
+    for p, (n, d, k, _) in enumerate(specs):
+        got = b.result(p)
+        assert got.idx.shape == (n, k)
+        rows = np.sort(rng.choice(n, size=min(200, n), replace=False))
+        ref = oracle.knn_brute_rows(data[p], k, rows)
+        assert all(set(a) == set(c) for a, c in zip(got.idx[rows].tolist(), ref.tolist())), p
+        W_ref = oracle.lle_weights_rows(data[p], rows, got.idx[rows], 1e-3)
+        werr = np.abs(got.weights[rows] - W_ref).max() / np.abs(W_ref).max()
+        worst_w = max(worst_w, werr)
+        assert werr < 1e-5, (p, werr)
+        for j, (cols, vals) in zip(rows, _m_rows(got.idx, got.weights, rows, 1e-9)):
+            lo, hi = got.row_ptr[j], got.row_ptr[j + 1]
+            assert np.array_equal(got.col_idx[lo:hi], cols), (p, j)
+            assert np.abs(got.vals[lo:hi] - vals).max() <= 1e-12 * max(1.0, np.abs(vals).max()), (p, j)
+    b.close()
+    print(f"256 problems: worst sampled W error {worst_w:.2e}")

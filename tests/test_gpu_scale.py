@@ -70,3 +70,37 @@ def test_lle_tensor_screen_equals_fp32_screen(ctx, n):
     b = ctx.local_operator(X, "lle", num_neighbors=16, klle_shift=1e-3, check_connectivity=False, screen="fp32")
     assert a.rows_uncertified == 0
     assert np.array_equal(a.idx, b.idx)
+
+
+def test_lle_lifted_roll_200k_reference_default_connectivity(ctx):
+    """The reference's default path at N=200000 (check_connectivity=true,
+    defines/keywords.hpp:272): while is_connected fails, find_neighbors redoes
+    the search with 2k (neighbors/neighbors.hpp:196-204). The final k equals the
+    one the oracle's is_connected reaches on the same neighbour tables, every
+    doubling is logged with the reference's message, and sampled rows at the
+    final k match the oracle (sets exact, W within 1e-5)."""
+    X = datasets.lifted_swiss_roll(200_000, 64, seed=1)
+    msgs = []
+    ctx.set_logger(lambda lvl, m: msgs.append(m))
+    try:
+        op = ctx.local_operator(X, "lle", num_neighbors=16, klle_shift=1e-3, check_connectivity=True)
+    finally:
+        ctx.set_logger(None)
+    k, decisions = 16, []
+    while True:
+        conn = oracle.is_connected(ctx.knn_brute(X, k))
+        decisions.append((k, conn))
+        if conn:
+            break
+        k *= 2
+    assert op.k == k and op.connectivity_retries == len(decisions) - 1, decisions
+    for kk, conn in decisions[:-1]:
+        assert any(f"The neighborhood graph with {kk} neighbors is not connected. Recomputing with a larger "
+                   f"number of neighbors {2 * kk}." in m for m in msgs)
+    assert any(f"The neighborhood graph with {k} neighbors is connected." in m for m in msgs)
+    rows = np.sort(np.random.default_rng(2).choice(200_000, 300, replace=False))
+    ref = oracle.knn_brute_rows(X, k, rows)
+    assert all(set(a) == set(b) for a, b in zip(op.idx[rows].tolist(), ref.tolist()))
+    W_ref = oracle.lle_weights_rows(X, rows, op.idx[rows], 1e-3)
+    assert np.abs(op.weights[rows] - W_ref).max() / np.abs(W_ref).max() < 1e-5
+    _csr_checks(op, 1e-9, 1e-6)
