@@ -12,7 +12,10 @@ assembly of M (tk_local_operator). Prints one JSON line.
 * e2e          the public API with pinned host buffers: X copied in, idx / W /
                CSR copied out inside the timed region
 * roofline     the tensor screen kernel: algorithmic 2 N^2 D flops per launch over
-               its CUDA-event time, against the measured bf16 peak
+               its CUDA-event time, against the measured bf16 burst peak
+* rooflines    every other kernel group of the stage: algorithmic DRAM bytes per
+               launch over its CUDA-event time, against the measured HBM peak, with
+               the DRAM traffic of the committed ncu capture
 * cpu_baseline the CPU oracle (a port of the reference's FP64 routines) on a
                bounded sample of query rows, all host threads
 --impl reference times that CPU port alone (the reference itself needs Eigen,
@@ -37,7 +40,6 @@ sys.path.insert(0, ROOT)
 METRIC = "LLE kNN+weights points/s (N=200k,D=64,k=16): mixed-TC vs plain FP32, same GPU"
 N_DEF, D_DEF, K_DEF = 200_000, 64, 16
 CHECK = False
-PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "knn_tc_screen_lle_n200k_d64_k16.md")
 
 
 def peaks():
@@ -49,15 +51,74 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per screen launch from the committed ncu summary, if any."""
+def source_sha(rel):
+    """sha256 (16 hex digits) of a source file of the library."""
+    import hashlib
     try:
-        for line in open(PROFILE_SUMMARY):
-            if line.strip().startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].strip().split()[0])
-    except Exception:
-        pass
-    return None
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            return hashlib.sha256(f.read()).hexdigest()[:16]
+    except OSError:
+        return None
+
+
+def profile_counters():
+    """The `counters:` lines of the committed ncu summaries (profiles/*.md): per
+    kernel group, DRAM bytes per launch of one capture, its workload, and the
+    sha256 of the kernel's source file when it was captured; `stale` is true when
+    that source has changed since."""
+    out = {}
+    pdir = os.path.join(ROOT, "profiles")
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith(".md"):
+            continue
+        for line in open(os.path.join(pdir, fn)):
+            if not line.startswith("counters:"):
+                continue
+            kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
+            if "group" not in kv:
+                continue
+            kv["file"] = "profiles/" + fn
+            kv["stale"] = source_sha(kv.get("source", "")) != kv.get("source_sha256")
+            out[kv["group"]] = kv
+    return out
+
+
+def stage_rooflines(infos, n, d, k, kc, nnz, pk):
+    """One entry per kernel group of the stage: its CUDA-event time (mean over the
+    timed steps, from tk_operator_info.kernel_ms), its algorithmic (compulsory)
+    DRAM bytes per launch, achieved GB/s against the measured HBM copy peak, and
+    the ncu DRAM traffic of the committed capture with traffic / algorithmic."""
+    npad = (n + 255) // 256 * 256
+    dp = (d + 63) // 64 * 64
+    km = [float(np.mean([i.kernel_ms[j] for i in infos])) for j in range(8)]
+    groups = [
+        ("prep", "centre, PCA sketch, Morton sort, fp16 hi/lo layout (prep.cu)", km[0],
+         n * d * 4 + npad * (dp * 8 + 32 + 8)),
+        ("rerank", "k_rerank<32> + k_fallback + tie selection (rerank.cu)", km[2],
+         npad * kc * 8 + n * d * 4 + 8 * n + n * k * 4),
+        ("weights", "k_lle (lle.cu)", km[3], n * k * 4 + n * d * 4 + n * k * 8),
+        ("reverse_lists", "k_indeg, offsets scan, k_fill_rev, k_sort_rev (assemble.cu)", km[4],
+         n * k * 4 + n * k * 4 + 8 * (n + 1)),
+        ("row_pass", "k_rows_fused + k_rows_big count (assemble.cu)", km[5],
+         8 * (n + 1) + n * k * (4 + 4 + 8) + 12 * nnz + 4 * n),
+        ("csr_write", "offsets scan, k_compact, k_rows_big fill (assemble.cu)", km[6],
+         2 * 12 * nnz + 4 * n + 8 * (n + 1)),
+    ]
+    prof = profile_counters()
+    hbm = pk["hbm_gbs"]
+    out = []
+    for name, what, ms, alg in groups:
+        achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else None
+        e = {"group": name, "kernels": what, "bound": "hbm", "ms": ms, "algorithmic_bytes": int(alg),
+             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if achieved else None}
+        c = prof.get(name)
+        if c:
+            t = float(c["dram_bytes"])
+            e.update({"traffic": t, "traffic_over_algorithmic": t / alg if c.get("workload") == "lle_n200k_d64_k16"
+                      else None, "traffic_source": c["file"], "traffic_workload": c.get("workload"),
+                      "traffic_stale": c["stale"]})
+        out.append(e)
+    return out
 
 
 class ClockSampler:
@@ -415,12 +476,18 @@ def main():
     flops = 2.0 * args.n * args.n * args.d
     screen_ms = stage["screen_kernel"]
     achieved = flops / (screen_ms / 1000.0) / 1e12
-    peak = pk.get("bf16_tflops_sustained", 1700.0)
+    # the screen runs ~7 ms inside a ~10 ms step: the burst peak applies
+    peak = pk.get("bf16_tflops", 1900.0)
+    sc = profile_counters().get("screen", {})
     roofline = {"kernel": "k_screen_tc_wide (tcgen05 fp16 split GEMM, near/far tiles, fused top-32)", "bound": "tensor",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "peak_source": f"bf16_tflops_sustained of {pk_src}",
+                "frac_of_sustained": achieved / pk.get("bf16_tflops_sustained", 1700.0),
+                "peak_source": f"bf16_tflops (burst) of {pk_src}",
                 "algorithmic": "2*N^2*D flops per launch (near tiles execute 3 fp16 products, far tiles 1)",
-                "traffic": profile_traffic()}
+                "traffic": float(sc["dram_bytes"]) if sc else None,
+                "traffic_source": sc.get("file"), "traffic_stale": sc.get("stale")}
+    kc = 32 if args.k + 8 <= 32 else 64
+    rooflines = stage_rooflines(inf_tc, args.n, args.d, kk, kc, nnz, pk)
 
     line = {"metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -428,7 +495,8 @@ def main():
             "data": "synthetic (seeded lifted Swiss roll)", "config": workload, "stage_ms": stage,
             "rows_uncertified": int(info.rows_uncertified), "tie_rows": int(info.tie_rows),
             "extra_neighbor_rows": int(info.extra_rows), "nnz": nnz, "k_used": kk,
-            "fp32_path": fp32, "default_connectivity": default_conn, "ltsa": ltsa, "eigen": eigen, "batch": batch, "roofline": roofline,
+            "fp32_path": fp32, "default_connectivity": default_conn, "ltsa": ltsa, "eigen": eigen, "batch": batch,
+            "roofline": roofline, "rooflines": rooflines,
             "e2e": {"value": args.n / (e2e_ms / 1000.0), "unit": "points/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clocks, "gpu_launches": int(launches)}

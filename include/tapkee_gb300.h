@@ -131,6 +131,11 @@ typedef struct tk_operator_info
                                  alone (last kNN pass)                               */
     int64_t tie_rows;         /* see tk_knn_stats (last kNN pass)                   */
     int64_t extra_rows;       /* see tk_knn_stats (last kNN pass)                   */
+    float kernel_ms[8];       /* device time per kernel group (CUDA events): point
+                                 preparation, distance screen, re-rank (with the
+                                 exact fallback and tie selection), all of the last
+                                 kNN pass; weights; reverse lists, row pass and CSR
+                                 write of assembly; connectivity checks (all passes) */
 } tk_operator_info;
 
 /* ---- context -------------------------------------------------------------- */

@@ -74,6 +74,7 @@ class tk_operator_info(ctypes.Structure):
         ("stage_ms", ctypes.c_float * 6),
         ("tie_rows", ctypes.c_int64),
         ("extra_rows", ctypes.c_int64),
+        ("kernel_ms", ctypes.c_float * 8),
     ]
 
 

@@ -863,6 +863,7 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     if (nk >= (int64_t)1 << 31)
         throw Error(TK_ERR_UNSUPPORTED, "assembly supports N*k < 2^31");
     AsmState a = asm_state(ctx, method, N, k);
+    mark(ctx, KM_ASM0);
     int* cnt = (int*)ctx->scratch.get("asm.cnt", sizeof(int) * (size_t)N * 2);
     int* fillc = cnt + N;
     const int g = 4 * ctx->num_sms;
@@ -878,6 +879,7 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     TK_CHECK_LAUNCH();
     k_sort_rev<<<g, 256, 0, st>>>(N, a.rptr, a.rev);
     TK_CHECK_LAUNCH();
+    mark(ctx, KM_ASM_REV);
     set_smem_limits();
     if (wide_rows(method, k))
         k_rows_fused<HC_L, RCAP_L><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem<HC_L>) * ROW_WARPS, st>>>(
@@ -893,6 +895,7 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
                                                                            nullptr, nullptr, a.big, a.nbig,
                                                                            ctx->dev_err);
     TK_CHECK_LAUNCH();
+    mark(ctx, KM_ASM_ROWS);
     scan_to_offsets(ctx, a.row_nnz, N, row_ptr);
 }
 
@@ -939,6 +942,7 @@ void assemble_write(tk_ctx* ctx, int method, int64_t N, int k, int td, const int
                                                                           a.rptr, a.rev, a.row_nnz, row_ptr, col_idx,
                                                                           vals, a.big, a.nbig, ctx->dev_err);
     TK_CHECK_LAUNCH();
+    mark(ctx, KM_ASM_END);
 }
 
 } // namespace tk

@@ -192,7 +192,9 @@ int64_t knn_device(tk_ctx* ctx, const void* Xd, int dtype, int64_t N, int D, int
         throw Error(TK_ERR_UNSUPPORTED, "the tensor-core screen supports D <= 128; pass TK_SCREEN_FP32 for D = " +
                                             std::to_string(D));
     Prepared P;
+    mark(ctx, KM_PREP);
     prepare_points(ctx, Xd, dtype, N, D, ldx, tensor, P);
+    mark(ctx, KM_SCREEN0);
     int32_t* cand_idx = (int32_t*)ctx->scratch.get("knn.cand_idx", sizeof(int32_t) * (size_t)P.Npad * kc);
     float* cand_val = (float*)ctx->scratch.get("knn.cand_val", sizeof(float) * (size_t)P.Npad * kc);
     TK_CUDA(cudaEventRecord(ctx->ev[8], ctx->stream));
@@ -201,9 +203,11 @@ int64_t knn_device(tk_ctx* ctx, const void* Xd, int dtype, int64_t N, int D, int
     else
         screen_fp32(ctx, P, kc, cand_idx, cand_val);
     TK_CUDA(cudaEventRecord(ctx->ev[9], ctx->stream));
+    mark(ctx, KM_SCREEN1);
     float c1, c2;
     screen_error_model(screen, P.Dp, &c1, &c2);
     const int64_t nf = rerank(ctx, P, Xd, dtype, ldx, k, kc, cand_idx, cand_val, c1, c2, idx_d, d2_d);
+    mark(ctx, KM_RERANK);
     check_device_errors(ctx);
     ctx->screen_ms = 0.f;
     cudaEventElapsedTime(&ctx->screen_ms, ctx->ev[8], ctx->ev[9]);
@@ -253,10 +257,16 @@ int guarded(tk_ctx* ctx, F&& f)
     }
 }
 
+// Device time between two recorded events (0 if either was never recorded; the
+// error that leaves is cleared so that the next launch check does not see it).
 float elapsed(cudaEvent_t a, cudaEvent_t b)
 {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+    {
+        cudaGetLastError();
+        ms = 0.f;
+    }
     return ms;
 }
 
@@ -342,6 +352,8 @@ int tk_ctx_create(int device, void* stream, tk_ctx** out)
         TK_CUDA(cudaMallocHost(&ctx->host_i64, 16 * sizeof(int64_t)));
         for (auto& e : ctx->ev)
             TK_CUDA(cudaEventCreate(&e));
+        for (auto& e : ctx->kev)
+            TK_CUDA(cudaEventCreate(&e));
     });
     if (rc != TK_OK)
     {
@@ -367,6 +379,9 @@ int tk_ctx_destroy(tk_ctx* ctx)
     if (ctx->host_i64)
         cudaFreeHost(ctx->host_i64);
     for (auto& e : ctx->ev)
+        if (e)
+            cudaEventDestroy(e);
+    for (auto& e : ctx->kev)
         if (e)
             cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream)
@@ -739,6 +754,12 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
 
         cudaStream_t st = ctx->stream;
         TK_CUDA(cudaEventRecord(ctx->ev[0], st));
+        struct MarksOn
+        {
+            tk_ctx* c;
+            ~MarksOn() { c->marks_on = false; }
+        } marks_guard{ctx};
+        ctx->marks_on = true;
         int64_t ldd;
         const void* Xd = device_points(ctx, X, dtype, N, D, ldx, &ldd, "op.X");
 
@@ -826,6 +847,14 @@ int tk_local_operator(tk_ctx* ctx, const tk_params* params, const void* X, int d
         o.stage_ms[3] = elapsed(ctx->ev[5], ctx->ev[6]);
         o.stage_ms[4] = elapsed(ctx->ev[0], ctx->ev[6]);
         o.stage_ms[5] = ctx->screen_ms;
+        o.kernel_ms[0] = elapsed(ctx->kev[KM_PREP], ctx->kev[KM_SCREEN0]);
+        o.kernel_ms[1] = elapsed(ctx->kev[KM_SCREEN0], ctx->kev[KM_SCREEN1]);
+        o.kernel_ms[2] = elapsed(ctx->kev[KM_SCREEN1], ctx->kev[KM_RERANK]);
+        o.kernel_ms[3] = o.stage_ms[2];
+        o.kernel_ms[4] = elapsed(ctx->kev[KM_ASM0], ctx->kev[KM_ASM_REV]);
+        o.kernel_ms[5] = elapsed(ctx->kev[KM_ASM_REV], ctx->kev[KM_ASM_ROWS]);
+        o.kernel_ms[6] = elapsed(ctx->kev[KM_ASM_ROWS], ctx->kev[KM_ASM_END]);
+        o.kernel_ms[7] = ms_conn;
         ctx->op_valid = true;
         if (info)
             *info = o;

@@ -1,11 +1,22 @@
 // connectivity.cu -- is every vertex reachable from vertex 0 along kNN out-edges?
 //
-// Same predicate as the reference's iterative DFS (neighbors/connected.hpp:19-62),
-// evaluated as a level-synchronous BFS inside one CTA: the visited set is a
-// bitmap, frontiers are arrays in global memory. The CTA never waits on another
-// CTA, and the level loop is bounded by N (a BFS has at most N levels), so the
-// kernel always terminates.
+// Same predicate as the reference's iterative DFS (neighbors/connected.hpp:19-62).
+// check_connected evaluates it in two steps:
+//   1. k_in_edges marks every vertex that some list names; a vertex other than 0
+//      with no in-edge cannot be reached, so any such vertex answers "not
+//      connected" without a traversal (the common case of large kNN graphs, whose
+//      anti-hubs are nobody's neighbour);
+//   2. otherwise a level-synchronous BFS over the whole GPU: a cooperative launch
+//      (every CTA resident), frontiers in global memory, a visited bitmap, and a
+//      grid barrier between levels. Every barrier wait is bounded (2 s, the
+//      global timer): on expiry the CTA records DEV_ERR_TIMEOUT, raises an abort
+//      flag that every waiting CTA polls, and all CTAs return. The level loop is
+//      bounded by N (a BFS has at most N levels).
+// The allocation-free entry point keeps the one-CTA BFS (bfs_levels): its state
+// must fit its fixed static scratch and it takes no cooperative launch.
+#include <algorithm>
 #include <cstdarg>
+#include <cstring>
 #include <mutex>
 
 #include "tk_internal.h"
@@ -71,13 +82,179 @@ __device__ __forceinline__ unsigned long long bfs_levels(int64_t N, int k, const
     return total;
 }
 
-__global__ void __launch_bounds__(1024) k_bfs(int64_t N, int k, const int32_t* __restrict__ idx, unsigned* visited,
-                                              int32_t* qa, int32_t* qb, unsigned long long* out_count,
-                                              unsigned* err)
+// ---- whole-GPU connectivity check --------------------------------------------
+
+// Device state of one check (cleared by the host before the launches).
+struct BfsState
 {
-    const unsigned long long total = bfs_levels(N, k, idx, visited, qa, qb, err);
+    unsigned long long reached;  // vertices reached (written by CTA 0)
+    unsigned orphans;            // vertices other than 0 without an in-edge
+    unsigned front[3];           // frontier sizes, triple-buffered by level
+    unsigned bar_count;          // grid barrier: arrivals
+    unsigned bar_gen;            // grid barrier: generation
+    unsigned abort;              // a CTA gave up waiting
+};
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Marks every vertex named by some neighbour list; bad indices are reported.
+__global__ void k_in_edges(const int32_t* __restrict__ idx, int64_t nk, int64_t N, unsigned* has_in, unsigned* err)
+{
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nk; e += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int j = idx[e];
+        if (j < 0 || j >= N)
+        {
+            atomicOr(err, DEV_ERR_BOUNDS);
+            continue;
+        }
+        const unsigned bit = 1u << (j & 31);
+        if ((__ldcg(&has_in[j >> 5]) & bit) == 0u)
+            atomicOr(&has_in[j >> 5], bit);
+    }
+}
+
+// Counts the vertices 1..N-1 that no list names.
+__global__ void k_orphans(const unsigned* __restrict__ has_in, int64_t N, BfsState* st)
+{
+    const int64_t words = (N + 31) / 32;
+    unsigned c = 0;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x)
+    {
+        unsigned valid = (w == words - 1 && (N & 31)) ? ((1u << (N & 31)) - 1u) : 0xffffffffu;
+        if (w == 0)
+            valid &= ~1u;  // vertex 0 is the start
+        c += __popc(~has_in[w] & valid);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c)
+        atomicAdd(&st->orphans, c);
+}
+
+// Grid barrier for a cooperative launch, with a bounded wait. Returns false when
+// this CTA, or another, gave up (the caller returns).
+__device__ bool grid_barrier(BfsState* st, unsigned nblocks, unsigned* err)
+{
+    __shared__ int ok;
+    __syncthreads();
     if (threadIdx.x == 0)
-        *out_count = total;
+    {
+        ok = 1;
+        volatile unsigned* gen = &st->bar_gen;
+        volatile unsigned* abort = &st->abort;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&st->bar_count, 1u) == nblocks - 1)
+        {
+            atomicExch(&st->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&st->bar_gen, 1u);
+        }
+        else
+        {
+            const uint64_t t0 = global_ns();
+            while (*gen == g)
+            {
+                if (*abort)
+                {
+                    ok = 0;
+                    break;
+                }
+                if (global_ns() - t0 > 2000000000ull)
+                {
+                    atomicOr(err, DEV_ERR_TIMEOUT);
+                    atomicExch(&st->abort, 1u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Level-synchronous BFS from vertex 0 over the whole grid (cooperative launch).
+// The visited bitmap and the counters are cleared by the host. Level L reads the
+// frontier size front[L % 3] and its vertices from one array, appends newly
+// reached vertices to the other array and to front[(L + 1) % 3], and CTA 0
+// clears front[(L + 2) % 3], last read before the previous barrier.
+__global__ void __launch_bounds__(512) k_bfs_grid(int64_t N, int k, const int32_t* __restrict__ idx,
+                                                  unsigned* visited, int32_t* qa, int32_t* qb, BfsState* st,
+                                                  unsigned* err)
+{
+    if (__ldcg(&st->orphans) != 0u)
+        return;  // answered by the in-edge test
+    const unsigned nblocks = gridDim.x;
+    const int lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        visited[0] |= 1u;
+        qa[0] = 0;
+        st->front[0] = 1u;
+    }
+    if (!grid_barrier(st, nblocks, err))
+        return;
+    unsigned long long total = 0;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t level = 0; level < N; ++level)
+    {
+        const unsigned cur = __ldcg(&st->front[level % 3]);
+        if (cur == 0u)
+            break;
+        total += cur;
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            st->front[(level + 2) % 3] = 0u;
+        const int32_t* in = (level & 1) ? qb : qa;
+        int32_t* out = (level & 1) ? qa : qb;
+        unsigned* next = &st->front[(level + 1) % 3];
+        const int64_t work = (int64_t)cur * k;
+        // the loop runs a whole number of warp passes so that the warp-aggregated
+        // append below sees every lane
+        for (int64_t t0 = tid - lane; t0 < work; t0 += nthreads)
+        {
+            const int64_t t = t0 + lane;
+            bool fresh = false;
+            int32_t nb = 0;
+            if (t < work)
+            {
+                const int32_t v = __ldcg(&in[t / k]);
+                nb = idx[(int64_t)v * k + (int)(t % k)];
+                if (nb < 0 || nb >= N)
+                    atomicOr(err, DEV_ERR_BOUNDS);
+                else
+                {
+                    const unsigned bit = 1u << (nb & 31);
+                    if ((__ldcg(&visited[nb >> 5]) & bit) == 0u)
+                        fresh = (atomicOr(&visited[nb >> 5], bit) & bit) == 0u;
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, fresh);
+            if (m)
+            {
+                unsigned base = 0;
+                if (lane == __ffs(m) - 1)
+                    base = atomicAdd(next, (unsigned)__popc(m));
+                base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+                if (fresh)
+                    out[base + __popc(m & ((1u << lane) - 1u))] = nb;
+            }
+        }
+        if (!grid_barrier(st, nblocks, err))
+            return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        st->reached = total;
 }
 
 } // namespace
@@ -86,16 +263,36 @@ bool check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx)
 {
     cudaStream_t st = ctx->stream;
     const size_t words = (size_t)((N + 31) / 32);
-    unsigned* visited = (unsigned*)ctx->scratch.get("bfs.visited", sizeof(unsigned) * words);
+    // visited and has_in share one allocation (cleared together)
+    unsigned* visited = (unsigned*)ctx->scratch.get("bfs.visited", 2 * sizeof(unsigned) * words);
+    unsigned* has_in = visited + words;
     int32_t* qa = (int32_t*)ctx->scratch.get("bfs.qa", sizeof(int32_t) * (size_t)N);
     int32_t* qb = (int32_t*)ctx->scratch.get("bfs.qb", sizeof(int32_t) * (size_t)N);
-    unsigned long long* cnt = (unsigned long long*)ctx->scratch.get("bfs.count", 16);
-    TK_CUDA(cudaMemsetAsync(visited, 0, sizeof(unsigned) * words, st));
-    k_bfs<<<1, 1024, 0, st>>>(N, k, idx, visited, qa, qb, cnt, ctx->dev_err);
+    BfsState* state = (BfsState*)ctx->scratch.get("bfs.state", sizeof(BfsState));
+    TK_CUDA(cudaMemsetAsync(visited, 0, 2 * sizeof(unsigned) * words, st));
+    TK_CUDA(cudaMemsetAsync(state, 0, sizeof(BfsState), st));
+    const int64_t nk = N * (int64_t)k;
+    k_in_edges<<<(int)std::min<int64_t>((nk + 255) / 256, 8 * ctx->num_sms), 256, 0, st>>>(idx, nk, N, has_in,
+                                                                                          ctx->dev_err);
     TK_CHECK_LAUNCH();
-    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    k_orphans<<<(int)std::min<int64_t>(((int64_t)words + 255) / 256, 2 * ctx->num_sms), 256, 0, st>>>(has_in, N,
+                                                                                                  state);
+    TK_CHECK_LAUNCH();
+    // every CTA of the BFS must be resident at once (cooperative launch)
+    int per_sm = 0;
+    TK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_grid, 512, 0));
+    const int grid = std::max(1, std::min(per_sm, 2)) * ctx->num_sms;
+    void* args[] = {(void*)&N, (void*)&k, (void*)&idx, (void*)&visited, (void*)&qa, (void*)&qb, (void*)&state,
+                    (void*)&ctx->dev_err};
+    TK_CUDA(cudaLaunchCooperativeKernel((const void*)k_bfs_grid, dim3(grid), dim3(512), args, 0, st));
+    TK_CHECK_LAUNCH();
+    BfsState h{};
+    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, state, sizeof(BfsState), cudaMemcpyDeviceToHost, st));
     TK_CUDA(cudaStreamSynchronize(st));
-    return (int64_t)ctx->host_i64[0] == N;
+    std::memcpy(&h, ctx->host_i64, sizeof(BfsState));
+    if (h.orphans > 0)
+        return false;
+    return (int64_t)h.reached == N;
 }
 
 } // namespace tk

@@ -103,6 +103,10 @@ struct tk_ctx
     int64_t* host_i64 = nullptr;      // pinned small readback area (16 entries)
     cudaEvent_t ev[12] = {};
     float screen_ms = 0.f;            // device time of the last distance screen
+    // per-kernel timing marks of tk_local_operator (recorded only while marks_on,
+    // so they never enter a captured graph); see tk::mark
+    cudaEvent_t kev[10] = {};
+    bool marks_on = false;
     int64_t knn_ties = 0;             // tie rows of the last brute kNN pass
     int64_t knn_extra = 0;            // rows of that pass with k + 1 reference neighbours
     int num_sms = 0;
@@ -114,6 +118,25 @@ struct tk_ctx
 namespace tk {
 
 void log(tk_ctx* ctx, int level, const std::string& msg);
+
+// Timing marks (tk_ctx::kev) of one tk_local_operator call, in stream order.
+enum : int
+{
+    KM_PREP = 0,   // before the point preparation of the last kNN pass
+    KM_SCREEN0,    // before its distance screen
+    KM_SCREEN1,    // after the screen
+    KM_RERANK,     // after the re-rank, fallback and tie selection
+    KM_ASM0,       // assembly: start
+    KM_ASM_REV,    // after the reverse lists
+    KM_ASM_ROWS,   // after the row pass
+    KM_ASM_END,    // after the CSR write
+    KM_COUNT
+};
+inline void mark(tk_ctx* ctx, int m)
+{
+    if (ctx->marks_on)
+        cudaEventRecord(ctx->kev[m], ctx->stream);
+}
 
 // ---- kernel launchers (one translation unit each) -------------------------
 
