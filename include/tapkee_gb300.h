@@ -330,6 +330,13 @@ int tk_operator_get_info(const tk_ctx* ctx, tk_operator_info* info);
  * The context stays usable. No counterpart in the reference. */
 int tk_selftest_bounded_wait(tk_ctx* ctx, int* outcome);
 
+/* Failure-path self-test of the connectivity check's grid barrier: a cooperative
+ * launch whose CTA 0 returns without reaching the barrier. The other CTAs' waits
+ * (2 s limit) expire, they record the device-side timeout and return, and the call
+ * returns TK_ERR_TIMEOUT with *outcome = 1 (2 would mean the barrier completed).
+ * The context stays usable. No counterpart in the reference. */
+int tk_selftest_grid_barrier(tk_ctx* ctx, int* outcome);
+
 /* Waits for all work queued on the context's stream. */
 int tk_ctx_synchronize(tk_ctx* ctx);
 

@@ -123,6 +123,7 @@ SIGNATURES = {
     "tk_operator_get_info": (_I, [_P, ctypes.POINTER(tk_operator_info)]),
     "tk_ctx_synchronize": (_I, [_P]),
     "tk_selftest_bounded_wait": (_I, [_P, ctypes.POINTER(_I)]),
+    "tk_selftest_grid_barrier": (_I, [_P, ctypes.POINTER(_I)]),
     "tk_batch_tuning_default": (None, [ctypes.POINTER(tk_batch_tuning)]),
     "tk_batch_create": (_I, [_P, ctypes.POINTER(tk_batch_problem), _I, _D, _D, ctypes.POINTER(tk_batch_tuning),
                              ctypes.POINTER(_P)]),

@@ -621,6 +621,16 @@ int tk_selftest_bounded_wait(tk_ctx* ctx, int* outcome)
     });
 }
 
+int tk_selftest_grid_barrier(tk_ctx* ctx, int* outcome)
+{
+    return guarded(ctx, [&] {
+        const int o = barrier_selftest(ctx);
+        if (outcome)
+            *outcome = o;
+        check_device_errors(ctx);
+    });
+}
+
 int tk_smallest_eigenvectors(tk_ctx* ctx, int64_t N, const int64_t* row_ptr, const int32_t* col_idx,
                              const double* vals, int target_dimension, int skip, double tol, int64_t max_matvecs,
                              double* vectors, double* values, tk_eig_info* info)

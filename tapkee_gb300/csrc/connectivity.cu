@@ -257,7 +257,35 @@ __global__ void __launch_bounds__(512) k_bfs_grid(int64_t N, int k, const int32_
         st->reached = total;
 }
 
+// Failure-path self-test of grid_barrier: CTA 0 returns without arriving, so the
+// other CTAs' waits expire; each records DEV_ERR_TIMEOUT and returns.
+__global__ void __launch_bounds__(512) k_barrier_selftest(BfsState* st, unsigned* err)
+{
+    if (blockIdx.x == 0)
+        return;
+    if (grid_barrier(st, gridDim.x, err) && threadIdx.x == 0)
+        atomicExch(&st->orphans, 2u);  // the barrier completed: not expected
+}
+
 } // namespace
+
+int barrier_selftest(tk_ctx* ctx)
+{
+    cudaStream_t st = ctx->stream;
+    BfsState* state = (BfsState*)ctx->scratch.get("bfs.state", sizeof(BfsState));
+    TK_CUDA(cudaMemsetAsync(state, 0, sizeof(BfsState), st));
+    int per_sm = 0;
+    TK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_barrier_selftest, 512, 0));
+    const int grid = std::max(2, std::max(1, std::min(per_sm, 2)) * ctx->num_sms);
+    void* args[] = {(void*)&state, (void*)&ctx->dev_err};
+    TK_CUDA(cudaLaunchCooperativeKernel((const void*)k_barrier_selftest, dim3(grid), dim3(512), args, 0, st));
+    TK_CHECK_LAUNCH();
+    BfsState h{};
+    TK_CUDA(cudaMemcpyAsync(ctx->host_i64, state, sizeof(BfsState), cudaMemcpyDeviceToHost, st));
+    TK_CUDA(cudaStreamSynchronize(st));
+    std::memcpy(&h, ctx->host_i64, sizeof(BfsState));
+    return h.orphans == 2u ? 2 : (h.abort ? 1 : 0);
+}
 
 bool check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx)
 {

@@ -91,7 +91,13 @@ struct LleRows
     const int32_t* row_prob;
     const BatchProb* probs;
     int64_t out_row0;
+    unsigned long long* work;  // batch: counter of claimed rows (zero at launch)
 };
+
+// Rows a warp of a batch claims at a time. Rows of different problems cost very
+// different amounts (a row's cost grows with its problem's D, 3 to 128), so
+// warps take chunks from a shared counter instead of fixed runs.
+constexpr int LLE_CHUNK = 8;
 
 // Register-resident Cholesky for KP <= 32: lane a holds row a of the matrix
 // (L[c] = C_ac for c <= a) and ends with row a of the lower factor and invd =
@@ -201,12 +207,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         bG[m] = (itm < ITEMS) ? itm / NBLK : 0;
     }
 
-    // batch: each warp takes a contiguous run of rows, so the problem
-    // description is reloaded only where the run crosses into the next problem
-    const int64_t run = BATCH ? (RW.rows + nwarps - 1) / nwarps : 0;
-    const int64_t g_begin = BATCH ? warp * run : warp;
-    const int64_t g_end = BATCH ? min(RW.rows, g_begin + run) : RW.rows;
-    const int64_t g_step = BATCH ? 1 : nwarps;
+    // batch: each warp claims chunks of consecutive rows, so the problem
+    // description is reloaded only where a chunk crosses into the next problem
     const void* X = RW.X;
     int dtype = RW.dtype;
     int64_t N = RW.N;
@@ -214,6 +216,29 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
     int64_t ldx = RW.ldx;
     int64_t prob_row0 = 0;  // batch: output row of the current problem's point 0
     int cur = -1;
+    for (int pass = 0;; ++pass)
+    {
+    int64_t g_begin, g_end, g_step;
+    if constexpr (BATCH)
+    {
+        unsigned long long c0 = 0;
+        if (lane == 0)
+            c0 = atomicAdd(RW.work, (unsigned long long)LLE_CHUNK);
+        c0 = __shfl_sync(0xffffffffu, c0, 0);
+        if ((int64_t)c0 >= RW.rows)
+            break;
+        g_begin = (int64_t)c0;
+        g_end = min(RW.rows, (int64_t)c0 + LLE_CHUNK);
+        g_step = 1;
+    }
+    else
+    {
+        if (pass > 0)
+            break;
+        g_begin = warp;
+        g_end = RW.rows;
+        g_step = nwarps;
+    }
     for (int64_t g = g_begin; g < g_end; g += g_step)
     {
         int64_t i = g;
@@ -634,6 +659,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         }
         __syncwarp();
     }
+    }
 }
 
 template <int KP, int WARPS, bool BATCH>
@@ -675,14 +701,21 @@ void dispatch(tk_ctx* ctx, const LleRows& RW, const int32_t* idx, int k, double 
 void lle_solve(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
                double klle_shift, const double* rhs, bool normalize, double* W)
 {
-    const LleRows RW{X, dtype, N, D, ldx, N, nullptr, nullptr, 0};
+    if (lle_pair_supported(X, dtype, ldx, k))
+    {
+        lle_pair_solve(ctx, X, N, D, ldx, idx, k, klle_shift, rhs, normalize, W);
+        return;
+    }
+    const LleRows RW{X, dtype, N, D, ldx, N, nullptr, nullptr, 0, nullptr};
     dispatch<false>(ctx, RW, idx, k, klle_shift, rhs, normalize, W, 8);
 }
 
 void lle_weights_batch(tk_ctx* ctx, const BatchProb* probs, const int32_t* row_prob, int64_t out_row0, int64_t rows,
                        const int32_t* idx, int k, double klle_shift, double* W, int warps)
 {
-    const LleRows RW{nullptr, 0, 0, 0, 0, rows, row_prob, probs, out_row0};
+    unsigned long long* work = (unsigned long long*)ctx->scratch.get("lle.work", 256);
+    TK_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned long long), ctx->stream));
+    const LleRows RW{nullptr, 0, 0, 0, 0, rows, row_prob, probs, out_row0, work};
     dispatch<true>(ctx, RW, idx, k, klle_shift, nullptr, true, W, warps);
 }
 

@@ -13,6 +13,7 @@
 // ill-conditioned tangent space; they are redone with an FP64 Jacobi.
 #include <cfloat>
 #include <cmath>
+#include <type_traits>
 
 #include "ff.cuh"
 #include "tk_internal.h"
@@ -20,7 +21,10 @@
 namespace tk {
 namespace {
 
-template <int M, typename T>
+// TD bounds the basis width td (the refinement's arrays): 2, 4 or 8. The float
+// kernel takes the smallest that fits td, which keeps its shared memory, and so
+// its warps per SM, in step with the basis actually asked for.
+template <int M, typename T, int TD = 8>
 struct JacobiSmem
 {
     T A[M][M + 1];
@@ -29,13 +33,13 @@ struct JacobiSmem
     int rp[M / 2], rq[M / 2];
     float Z[M][33];
     float Zl[M][33];     // low parts of the centred coordinates
-    float th[32][8], tl[32][8];  // t = Zc^T V for one chunk, float-float
-    float Vf[M][8];      // FP32 top eigenvectors
-    float GVh[M][8], GVl[M][8];  // G V, float-float
-    float Rf[M][8];      // residual G V - V Lam
-    float UR[M][8];      // (u_j . R_t) / (Lam_t - lambda_j)
-    float Oh[M][8], Ol[M][8];    // refined basis, float-float
-    float Lh[8][8], Ll[8][8];    // Rayleigh quotient V^T G V, float-float
+    float th[32][TD], tl[32][TD];  // t = Zc^T V for one chunk, float-float
+    float Vf[M][TD];      // FP32 top eigenvectors
+    float GVh[M][TD], GVl[M][TD];  // G V, float-float
+    float Rf[M][TD];      // residual G V - V Lam
+    float UR[M][TD];      // (u_j . R_t) / (Lam_t - lambda_j)
+    float Oh[M][TD], Ol[M][TD];    // refined basis, float-float
+    float Lh[TD][TD], Ll[TD][TD];    // Rayleigh quotient V^T G V, float-float
 };
 
 // x as a float pair (exact for float32 input, hi + lo split for float64)
@@ -53,8 +57,8 @@ __device__ __forceinline__ ff x_ff(const void* X, int dtype, int64_t off)
 // Coordinates of the neighbours of one point in dimensions [d0, d0 + 32),
 // centred on their mean, in float-float: Z[a][lane] + Zl[a][lane] = x_{n_a} -
 // mean for d = d0 + lane (zero for a >= k or d >= D).
-template <int M, typename T>
-__device__ __forceinline__ void stage_centred(JacobiSmem<M, T>& S, int lane, const void* X, int dtype, int64_t ldx,
+template <int M, typename T, int TD>
+__device__ __forceinline__ void stage_centred(JacobiSmem<M, T, TD>& S, int lane, const void* X, int dtype, int64_t ldx,
                                               int D, const int32_t* nbrs, int k, int d0)
 {
     const int d = d0 + lane;
@@ -75,8 +79,8 @@ __device__ __forceinline__ void stage_centred(JacobiSmem<M, T>& S, int lane, con
 
 // Parallel cyclic Jacobi on the symmetric M x M matrix S.A (one warp). On exit
 // diag(A) holds the eigenvalues and the columns of V the eigenvectors.
-template <int M, typename T>
-__device__ void warp_jacobi(JacobiSmem<M, T>& S, int lane, int max_sweeps)
+template <int M, typename T, int TD>
+__device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
 {
     for (int t = lane; t < M * M; t += 32)
         S.V[t / M][t % M] = (t / M == t % M) ? T(1) : T(0);
@@ -167,8 +171,8 @@ __device__ void warp_jacobi(JacobiSmem<M, T>& S, int lane, int max_sweeps)
 // Builds the centred neighbour Gram of point i into S.A (type T, M x M, zero
 // padded): FP32 products of the high parts for T = float (the refinement
 // corrects what this drops), exact pair products in FP64 for T = double.
-template <int M, typename T>
-__device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
+template <int M, typename T, int TD>
+__device__ void centred_gram(JacobiSmem<M, T, TD>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
                              const int32_t* nbrs, int k)
 {
     for (int t = lane; t < M * M; t += 32)
@@ -207,8 +211,8 @@ __device__ void centred_gram(JacobiSmem<M, T>& S, int lane, const void* X, int d
 // then the basis is re-orthonormalised (modified Gram-Schmidt) in float-float.
 // This removes the FP32 Gram and Jacobi errors to first order (error ~ eps^2 /
 // gap). Everything runs on the FP32 pipes; the result is S.Oh + S.Ol.
-template <int M>
-__device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
+template <int M, int TD>
+__device__ void refine_subspace(JacobiSmem<M, float, TD>& S, int lane, const void* X, int dtype, int64_t ldx, int D,
                                 const int32_t* nbrs, int k, int td, const int* top)
 {
     constexpr int RPL = (M + 31) / 32;  // basis rows per lane: a = lane + 32 r
@@ -218,10 +222,10 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
         S.Vf[a][t] = (a < k) ? S.V[a][top[t]] : 0.f;
     }
     __syncwarp();
-    ff acc[RPL][8];
+    ff acc[RPL][TD];
 #pragma unroll
     for (int r = 0; r < RPL; ++r)
-        for (int t = 0; t < 8; ++t)
+        for (int t = 0; t < TD; ++t)
             acc[r][t] = ff_zero();
     for (int d0 = 0; d0 < D; d0 += 32)
     {
@@ -362,14 +366,14 @@ __device__ void refine_subspace(JacobiSmem<M, float>& S, int lane, const void* X
     }
 }
 
-template <int M, int WARPS>
+template <int M, int WARPS, int TD>
 __global__ void __launch_bounds__(WARPS * 32) k_ltsa(const void* X, int dtype, int64_t N, int D, int64_t ldx,
                                               const int32_t* __restrict__ idx, int k, int td, double* V,
                                               int32_t* refine, unsigned* nrefine, unsigned* err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    JacobiSmem<M, float>& S = reinterpret_cast<JacobiSmem<M, float>*>(smem_raw)[wib];
+    JacobiSmem<M, float, TD>& S = reinterpret_cast<JacobiSmem<M, float, TD>*>(smem_raw)[wib];
     __shared__ int nb_s[WARPS][M];
     const int64_t nw = (int64_t)gridDim.x * WARPS;
     for (int64_t i = (int64_t)blockIdx.x * WARPS + wib; i < N; i += nw)
@@ -522,13 +526,22 @@ void launch(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx
     int32_t* refine = (int32_t*)ctx->scratch.get("ltsa.refine", sizeof(int32_t) * (size_t)N);
     unsigned* nrefine = (unsigned*)ctx->scratch.get("ltsa.nrefine", 16);
     TK_CUDA(cudaMemsetAsync(nrefine, 0, 16, st));
-    const size_t smem = sizeof(JacobiSmem<M, float>) * WARPS;
-    static_assert(sizeof(JacobiSmem<M, float>) * WARPS <= 200 * 1024, "shared memory budget");
-    TK_CUDA(cudaFuncSetAttribute(k_ltsa<M, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<int64_t>((N + WARPS - 1) / WARPS, (int64_t)ctx->num_sms * 16);
-    k_ltsa<M, WARPS><<<grid, WARPS * 32, smem, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine,
-                                                     ctx->dev_err);
-    TK_CHECK_LAUNCH();
+    auto run = [&](auto tdc) {
+        constexpr int TD = decltype(tdc)::value;
+        const size_t smem = sizeof(JacobiSmem<M, float, TD>) * WARPS;
+        static_assert(sizeof(JacobiSmem<M, float, TD>) * WARPS <= 200 * 1024, "shared memory budget");
+        TK_CUDA(cudaFuncSetAttribute(k_ltsa<M, WARPS, TD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_ltsa<M, WARPS, TD><<<grid, WARPS * 32, smem, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine,
+                                                             ctx->dev_err);
+        TK_CHECK_LAUNCH();
+    };
+    if (td <= 2)
+        run(std::integral_constant<int, 2>{});
+    else if (td <= 4)
+        run(std::integral_constant<int, 4>{});
+    else
+        run(std::integral_constant<int, 8>{});
     const size_t smem64 = sizeof(JacobiSmem<M, double>);
     TK_CUDA(cudaFuncSetAttribute(k_ltsa_fp64<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem64));
     k_ltsa_fp64<M><<<ctx->num_sms * 4, 32, smem64, st>>>(X, dtype, N, D, ldx, idx, k, td, V, refine, nrefine,

@@ -229,6 +229,10 @@ int64_t rerank(tk_ctx* ctx, const Prepared& P, const void* X, int dtype, int64_t
 
 // connectivity.cu
 bool check_connected(tk_ctx* ctx, int64_t N, int k, const int32_t* idx);
+// One cooperative launch whose CTA 0 never reaches the BFS grid barrier: returns 1
+// when the other CTAs' bounded waits expired as designed, 2 if the barrier
+// completed, 0 otherwise.
+int barrier_selftest(tk_ctx* ctx);
 
 // lle.cu
 void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx,
@@ -237,6 +241,11 @@ void lle_weights(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_
 // ones) and, when normalize is false, the raw solution instead of weights.
 void lle_solve(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
                double klle_shift, const double* rhs, bool normalize, double* W);
+// lle_pair.cu: the same solve, two points per warp, for float32 points with
+// 16-byte aligned rows and k <= 16 (lle_solve dispatches to it).
+bool lle_pair_supported(const void* X, int dtype, int64_t ldx, int k);
+void lle_pair_solve(tk_ctx* ctx, const void* X, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
+                    double klle_shift, const double* rhs, bool normalize, double* W);
 // dL/dX (N x D, FP64, row stride D) of the weights W for upstream dL/dW = G.
 void lle_weights_grad(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t ldx, const int32_t* idx, int k,
                       double klle_shift, const double* W, const double* G, double* gX);

@@ -34,9 +34,12 @@ def test_batch_matches_single_problem_path(ctx, tuning):
             got = b.result(p)
             ref = ctx.local_operator(data[p], "lle", num_neighbors=k, klle_shift=1e-3, check_connectivity=False)
             assert got.idx.shape == (n, k)
-            # same neighbours (rows ordered by (distance, index)); the weights come
-            # from the same solve on the same neighbours; M identical
-            _same_operator(got, ref, tol=1e-9)
+            # same neighbours (rows ordered by (distance, index)) and the same M
+            # structure; the values agree to 1e-6: the single-problem path solves
+            # float32 rows with k <= 16 two points per warp (lle_pair.cu), the
+            # batch with k_lle, and both are refined to FP64-level accuracy (each is
+            # checked against the oracle at 1e-5 in the other tests)
+            _same_operator(got, ref, tol=1e-6)
     b.close()
 
 

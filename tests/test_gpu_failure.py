@@ -32,3 +32,21 @@ def test_bounded_wait_expires_and_context_survives(ctx, golden):
     # and through the Python error mapping
     with pytest.raises(tk.DeviceError, match="bounded wait expired"):
         ctx._check(ctx.lib.tk_selftest_bounded_wait(ctx.ptr, None))
+
+
+def test_grid_barrier_wait_expires_and_context_survives(ctx, golden):
+    """The connectivity check's grid barrier (cooperative launch): CTA 0 never
+    arrives, the other CTAs give up after the 2 s limit, and the next check on the
+    same context is right (its state is cleared per call)."""
+    outcome = ctypes.c_int(0)
+    t0 = time.perf_counter()
+    st = ctx.lib.tk_selftest_grid_barrier(ctx.ptr, ctypes.byref(outcome))
+    elapsed = time.perf_counter() - t0
+    assert st == C.TK_ERR_TIMEOUT
+    assert outcome.value == 1
+    assert "bounded wait expired" in ctx.lib.tk_last_error(ctx.ptr).decode()
+    assert 1.5 < elapsed < 30.0
+    assert ctx.check_connected(golden["lle_idx"]) is True
+    rng = np.random.default_rng(0)
+    two = np.concatenate([rng.normal(size=(60, 2)), rng.normal(size=(60, 2)) + 100.0])
+    assert ctx.check_connected(ctx.knn_brute(two, 5)) is False

@@ -64,3 +64,28 @@ def test_out_of_range_neighbours_are_reported(ctx):
         ctx.lle_weights(X, bad)
     V = ctx.ltsa_basis(X, idx, 2)  # the context stays usable
     assert V.shape == (800, 12, 2)
+
+
+@pytest.mark.parametrize("n,d,k", [(3001, 64, 16), (2001, 4, 12), (1999, 36, 8), (1500, 100, 15), (1200, 128, 16),
+                                   (999, 8, 3), (1000, 20, 16)])
+def test_lle_weights_pair_kernel(ctx, n, d, k):
+    """The two-points-per-warp solve (float32, k <= 16, 16-byte aligned rows):
+    odd N (the last pair has one point), D with a ragged last float4 and chunk,
+    D over two chunks, k > D (two refinement steps), small k."""
+    X = datasets.lifted_swiss_roll(n, d, seed=n + d, dtype=np.float32)
+    idx, _, _ = oracle.knn_brute(X, k)
+    W = ctx.lle_weights(X, idx, 1e-3)
+    ref = oracle.lle_weights(X, idx, 1e-3)
+    assert _rel(W, ref) < TOL, _rel(W, ref)
+    assert np.allclose(W.sum(1), 1.0, atol=1e-12)
+
+
+def test_lle_weights_pair_kernel_bad_index(ctx):
+    import tapkee_gb300 as tk
+    X = datasets.lifted_swiss_roll(800, 16, seed=5)
+    idx, _, _ = oracle.knn_brute(X, 12)
+    bad = idx.copy()
+    bad[401, 5] = 800
+    with pytest.raises(tk.WrongParameterError, match="index out of range"):
+        ctx.lle_weights(X, bad)
+    assert _rel(ctx.lle_weights(X, idx), oracle.lle_weights(X, idx, 1e-3)) < TOL
