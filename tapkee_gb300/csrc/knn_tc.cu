@@ -653,23 +653,31 @@ struct TwCfg
     static constexpr int A_BYTES = 2 * A_ATOM;               // hi + lo
     static constexpr int AX_BYTES = 128 * 32;                // constant norm slice of A
     static constexpr int BX_BYTES = TW_N * 32;               // norm column slice of B
-    static constexpr int B_STAGE = 2 * B_ATOM + BX_BYTES;    // 72 KB
-    static constexpr int STAGES = 2;
+    // two rings: every tile's high parts and norm column (3 deep), and the low
+    // parts that only near tiles load (2 deep)
+    static constexpr int B_STAGE = B_ATOM + BX_BYTES;        // 40 KB: high parts + norm column
+    static constexpr int STAGES = 3;
+    static constexpr int L_STAGE = B_ATOM;                   // 32 KB: low parts
+    static constexpr int L_STAGES = 2;
     static constexpr int MERGE_BYTES = 4 * TW_KC * 32 * 8;   // warps 4-7 lists: value + id
-    static constexpr int NB_WORDS = 2048;                    // near bits staged in shared memory
+    static constexpr int NB_WORDS = 512;                     // near bits staged in shared memory
     static constexpr size_t OFF_B = A_BYTES;
-    static constexpr size_t OFF_AX = OFF_B + (size_t)STAGES * B_STAGE;
+    static constexpr size_t OFF_L = OFF_B + (size_t)STAGES * B_STAGE;
+    static constexpr size_t OFF_AX = OFF_L + (size_t)L_STAGES * L_STAGE;
     static constexpr size_t OFF_BAR = OFF_AX + AX_BYTES;
-    static constexpr size_t OFF_MERGE = OFF_BAR + 256;
-    static constexpr size_t OFF_FAR = OFF_MERGE + MERGE_BYTES;
+    // the half-list merge runs after the last tile's MMAs: it reuses the high ring
+    static constexpr size_t OFF_MERGE = OFF_B;
+    static constexpr size_t OFF_FAR = OFF_BAR + 256;
     static constexpr size_t OFF_NB = OFF_FAR + 128 * 4;
+    static_assert(MERGE_BYTES <= STAGES * B_STAGE, "merge buffer inside the high ring");
     static constexpr size_t SMEM = OFF_NB + (size_t)NB_WORDS * 4 + 1024;
     static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
 struct TwBarriers
 {
-    uint64_t full[2], empty[2], tfull[2], tempty[2], afull, fin;
+    uint64_t full[TwCfg::STAGES], empty[TwCfg::STAGES], lfull[TwCfg::L_STAGES], lempty[TwCfg::L_STAGES];
+    uint64_t tfull[2], tempty[2], afull, fin;
     uint32_t tmem_base;
     int abort;
 };
@@ -699,6 +707,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     unsigned char* gbase = smem_raw + (base - raw);
     const uint32_t A_s = base;
     const uint32_t B_s = base + (uint32_t)C::OFF_B;
+    const uint32_t L_s = base + (uint32_t)C::OFF_L;
     const uint32_t AX_s = base + (uint32_t)C::OFF_AX;
     TwBarriers& Bar = *reinterpret_cast<TwBarriers*>(gbase + C::OFF_BAR);
     float* merge_v = reinterpret_cast<float*>(gbase + C::OFF_MERGE);
@@ -741,6 +750,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(smem_u32(&Bar.full[st]), 1);
             mbar_init(smem_u32(&Bar.empty[st]), 1);
         }
+        for (int st = 0; st < C::L_STAGES; ++st)
+        {
+            mbar_init(smem_u32(&Bar.lfull[st]), 1);
+            mbar_init(smem_u32(&Bar.lempty[st]), 1);
+        }
         for (int b = 0; b < 2; ++b)
         {
             mbar_init(smem_u32(&Bar.tfull[b]), 1);
@@ -777,7 +791,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             ZigZag zz((int)(q0 / TW_N), ntiles);
             for (int s = 0; s < it0; ++s)
                 zz.next();
-            int issued = 0;
+            int issued = 0, lissued = 0;  // loads issued into the high and the low ring
             for (int it = 0; it < nit; ++it)
             {
                 const int tile = zz.next();
@@ -785,14 +799,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
                 if (!mbar_wait(smem_u32(&Bar.empty[slot]), ph ^ 1u, abort, err))
                     break;
+                if (is_near(tile))
+                {
+                    const int ls = lissued % C::L_STAGES;
+                    const uint32_t lph = (uint32_t)(lissued / C::L_STAGES) & 1u;
+                    if (!mbar_wait(smem_u32(&Bar.lempty[ls]), lph ^ 1u, abort, err))
+                        break;
+                    const uint32_t lb = smem_u32(&Bar.lfull[ls]);
+                    mbar_expect_tx(lb, (uint32_t)C::L_STAGE);
+                    tma_load_2d(L_s + ls * C::L_STAGE, &tmB_lo, 0, tile * TW_N, lb);
+                    ++lissued;
+                }
                 const uint32_t fb = smem_u32(&Bar.full[slot]);
                 const uint32_t bst = B_s + slot * C::B_STAGE;
-                const bool nr = is_near(tile);
-                mbar_expect_tx(fb, nr ? (uint32_t)C::B_STAGE : (uint32_t)(C::B_ATOM + C::BX_BYTES));
+                mbar_expect_tx(fb, (uint32_t)C::B_STAGE);
                 tma_load_2d(bst, &tmB_hi, 0, tile * TW_N, fb);
-                if (nr)
-                    tma_load_2d(bst + C::B_ATOM, &tmB_lo, 0, tile * TW_N, fb);
-                tma_load_2d(bst + 2 * C::B_ATOM, &tm_nrm, 0, tile * TW_N, fb);
+                tma_load_2d(bst + C::B_ATOM, &tm_nrm, 0, tile * TW_N, fb);
                 issued = it + 1;
             }
             if (*abort)
@@ -801,6 +823,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 mbar_wait(afull, 0u, &no_abort, err);
                 for (int g = (issued > C::STAGES ? issued - C::STAGES : 0); g < issued; ++g)
                     mbar_wait(smem_u32(&Bar.full[g % C::STAGES]), (uint32_t)(g / C::STAGES) & 1u, &no_abort, err);
+                for (int g = (lissued > C::L_STAGES ? lissued - C::L_STAGES : 0); g < lissued; ++g)
+                    mbar_wait(smem_u32(&Bar.lfull[g % C::L_STAGES]), (uint32_t)(g / C::L_STAGES) & 1u, &no_abort,
+                              err);
             }
         }
     }
@@ -813,19 +838,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc_fence_after();
             int issued_any = 0;
             const uint64_t axd = umma_desc_sw32(AX_s);
-            uint64_t adesc[2][4], bdesc0[2][4];
+            uint64_t adesc[2][4], bdh[4], bdl[4];
 #pragma unroll
             for (int part = 0; part < 2; ++part)
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk)
-                {
                     adesc[part][kk] = umma_desc(A_s + part * C::A_ATOM + (uint32_t)kk * 32u);
-                    bdesc0[part][kk] = umma_desc(B_s + part * C::B_ATOM + (uint32_t)kk * 32u);
-                }
-            const uint64_t bx0 = umma_desc_sw32(B_s + 2 * C::B_ATOM);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+            {
+                bdh[kk] = umma_desc(B_s + (uint32_t)kk * 32u);  // high ring, slot 0
+                bdl[kk] = umma_desc(L_s + (uint32_t)kk * 32u);  // low ring, slot 0
+            }
+            const uint64_t bx0 = umma_desc_sw32(B_s + C::B_ATOM);
             ZigZag zz((int)(q0 / TW_N), ntiles);
             for (int s = 0; s < it0; ++s)
                 zz.next();
+            int lc = 0;  // near tiles consumed (low-ring position)
             for (int it = 0; ok && it < nit; ++it)
             {
                 const bool nr = is_near(zz.next());
@@ -833,28 +862,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
                 const int buf = it & 1;
                 const uint32_t bph = (uint32_t)(it >> 1) & 1u;
+                const int ls = lc % C::L_STAGES;
                 if (!mbar_wait(smem_u32(&Bar.full[slot]), ph, abort, err))
+                    break;
+                if (nr && !mbar_wait(smem_u32(&Bar.lfull[ls]), (uint32_t)(lc / C::L_STAGES) & 1u, abort, err))
                     break;
                 if (!mbar_wait(smem_u32(&Bar.tempty[buf]), bph ^ 1u, abort, err))
                     break;
                 tc_fence_after();
                 const uint64_t soff = (uint64_t)((slot * C::B_STAGE) >> 4);
+                const uint64_t loff = (uint64_t)((ls * C::L_STAGE) >> 4);
                 const uint32_t d = tmem + (uint32_t)(buf * TW_N);
                 umma_f16_w(d, axd, bx0 + soff, 0u);  // -|2^s y|^2 / 2 in every row
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk)
-                    umma_f16_w(d, adesc[0][kk], bdesc0[0][kk] + soff, 1u);  // h_x . h_y
+                    umma_f16_w(d, adesc[0][kk], bdh[kk] + soff, 1u);  // h_x . h_y
                 if (nr)
                 {
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk)
-                        umma_f16_w(d, adesc[0][kk], bdesc0[1][kk] + soff, 1u);  // h_x . l_y
+                        umma_f16_w(d, adesc[0][kk], bdl[kk] + loff, 1u);  // h_x . l_y
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk)
-                        umma_f16_w(d, adesc[1][kk], bdesc0[0][kk] + soff, 1u);  // l_x . h_y
+                        umma_f16_w(d, adesc[1][kk], bdh[kk] + soff, 1u);  // l_x . h_y
                 }
                 umma_commit(smem_u32(&Bar.tfull[buf]));
                 umma_commit(smem_u32(&Bar.empty[slot]));
+                if (nr)
+                {
+                    umma_commit(smem_u32(&Bar.lempty[ls]));
+                    ++lc;
+                }
                 issued_any = 1;
             }
             if (issued_any)

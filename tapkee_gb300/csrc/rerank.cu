@@ -326,42 +326,15 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
             }
             if (__any_sync(0xffffffffu, any))
             {
-                // exact (float-float) distances of the candidates that need them,
-                // one candidate at a time by the whole warp: lanes own dimensions,
-                // and a fixed xor tree sums the lane partials
-                const float* Xf = reinterpret_cast<const float*>(X);
 #pragma unroll
                 for (int s = 0; s < PER; ++s)
-                {
-                    unsigned m = __ballot_sync(0xffffffffu, need[s]);
-                    while (m)
+                    if (need[s])
                     {
-                        const int src = __ffs(m) - 1;
-                        m &= m - 1u;
-                        const int64_t jj = __shfl_sync(0xffffffffu, j[s], src);
-                        ff acc = ff_zero();
-                        float cross = 0.f;  // sum of 2 hi lo (relative size 2^-24 of the total)
-                        for (int d = lane; d < D; d += 32)
-                        {
-                            const ff z = two_sum(__ldg(Xf + jj * ldx + d), -__ldg(Xf + i * ldx + d));
-                            acc = ff_add(acc, two_prod(z.hi, z.hi));
-                            cross = fmaf(2.f * z.hi, z.lo, cross);
-                        }
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1)
-                        {
-                            acc = ff_add(acc, ff_shfl_xor(acc, o));
-                            cross += __shfl_xor_sync(0xffffffffu, cross, o);
-                        }
-                        const ff e = ff_add(acc, ff{cross, 0.f});
-                        if (lane == src)
-                        {
-                            kh[s] = e.hi;
-                            kl[s] = e.lo;
-                            exact[s] = true;
-                        }
+                        const ff e = exact_key(X, dtype, ldx, D, i, j[s]);
+                        kh[s] = e.hi;
+                        kl[s] = e.lo;
+                        exact[s] = true;
                     }
-                }
                 rank_all();
             }
         }
