@@ -697,7 +697,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                      int64_t Npad, const uint32_t* __restrict__ near_bits, int nwords,
                      int32_t* __restrict__ cand_idx, float* __restrict__ cand_val, float* __restrict__ far_val,
                      const float* __restrict__ nrm, int full_blocks, int parts, int32_t* __restrict__ part_idx,
-                     float* __restrict__ part_val, float* __restrict__ part_far, unsigned* err)
+                     float* __restrict__ part_val, float* __restrict__ part_far, const float* __restrict__ Tb,
+                     const float* __restrict__ rmax, float c1, float c2, unsigned* err)
 {
     using C = TwCfg;
     constexpr int KC = TW_KC;
@@ -912,16 +913,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int64_t q = q0 + row;
         const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);  // a power of two: thr below is exact
         const float inv_m2 = 1.0f / m2;
+        // The list starts full of a bound instead of empty: B = 1.1 T_b + 2 eps
+        // (T_b bounds every row's k-th neighbour distance, eps is the row's screen
+        // error), so only candidates screened below it are inserted. A point never
+        // inserted has a screened value >= B, and the list's last value is
+        // min(B, the 32nd screened value), so the re-rank's certification against
+        // the last value covers it as before; B only spares the early inserts of
+        // an empty list (at most 32 per row, most of them displaced again).
+        float cmp = FLT_MAX;
+        {
+            const float nq0 = nrm[q];
+            const float tb = Tb[blk];
+            if (nq0 < FLT_MAX && tb < FLT_MAX)
+            {
+                const float R = rmax[0];
+                const float eps = c1 * (nq0 + R * R) + c2 * sqrtf(nq0) * R;
+                cmp = fmaf(1.1f, tb, 2.f * eps) - nq0;
+            }
+        }
         float L[KC];
         int32_t Ix[KC];
 #pragma unroll
         for (int s = 0; s < KC; ++s)
         {
-            L[s] = FLT_MAX;
+            L[s] = cmp;
             Ix[s] = -1;
         }
-        float cmp = FLT_MAX;
-        float thr = -__int_as_float(0x7f800000);
+        float thr = (cmp < FLT_MAX) ? cmp * inv_m2 : -__int_as_float(0x7f800000);
         float far_max = -__int_as_float(0x7f800000);  // largest accumulator over far tiles
         ZigZag zz((int)(q0 / TW_N), ntiles);
         for (int s = 0; s < it0; ++s)
@@ -1410,7 +1428,8 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     TK_CUDA(cudaFuncSetAttribute(k_screen_tc_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TwCfg::SMEM));
     k_screen_tc_wide<<<grid, TC_THREADS, TwCfg::SMEM, st>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad, bits, nwords,
                                                            cand_idx, cand_val, P.far_val, P.nrm, full_blocks, parts,
-                                                           part_idx, part_val, part_far, ctx->dev_err);
+                                                           part_idx, part_val, part_far, Tb, P.rmax, c1, c2,
+                                                           ctx->dev_err);
     TK_CHECK_LAUNCH();
     if (parts > 1)
     {
