@@ -96,7 +96,8 @@ def stage_rooflines(infos, n, d, k, kc, nnz, pk):
          n * d * 4 + npad * (dp * 8 + 32 + 8)),
         ("rerank", "k_rerank<32> + k_fallback + tie selection (rerank.cu)", km[2],
          npad * kc * 8 + n * d * 4 + 8 * n + n * k * 4),
-        ("weights", "k_lle (lle.cu)", km[3], n * k * 4 + n * d * 4 + n * k * 8),
+        ("weights", "k_lle_pair for float32 k<=16 (lle_pair.cu), else k_lle (lle.cu)", km[3],
+         n * k * 4 + n * d * 4 + n * k * 8),
         ("reverse_lists", "k_indeg, offsets scan, k_fill_rev, k_sort_rev (assemble.cu)", km[4],
          n * k * 4 + n * k * 4 + 8 * (n + 1)),
         ("row_pass", "k_rows_fused + k_rows_big count (assemble.cu)", km[5],

@@ -644,6 +644,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // against with the larger error bound of high-part products.
 constexpr int TW_N = 256;
 constexpr int TW_KC = 32;
+// warps 0-7 epilogue, 8 producer of the high ring, 9 MMA issuer, 10 producer of
+// the low ring
+constexpr int TW_THREADS = 352;
 constexpr uint32_t IDESC_W = (1u << 4) | ((uint32_t)(TW_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 
 struct TwCfg
@@ -690,7 +693,7 @@ __device__ __forceinline__ void umma_f16_w(uint32_t dtmem, uint64_t adesc, uint6
         "l"(adesc), "l"(bdesc), "r"(IDESC_W), "r"(accumulate));
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TW_THREADS, 1)
     k_screen_tc_wide(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
                      const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo,
                      const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
@@ -792,7 +795,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             ZigZag zz((int)(q0 / TW_N), ntiles);
             for (int s = 0; s < it0; ++s)
                 zz.next();
-            int issued = 0, lissued = 0;  // loads issued into the high and the low ring
+            int issued = 0;  // loads issued into the high ring
             for (int it = 0; it < nit; ++it)
             {
                 const int tile = zz.next();
@@ -800,17 +803,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t ph = (uint32_t)(it / C::STAGES) & 1u;
                 if (!mbar_wait(smem_u32(&Bar.empty[slot]), ph ^ 1u, abort, err))
                     break;
-                if (is_near(tile))
-                {
-                    const int ls = lissued % C::L_STAGES;
-                    const uint32_t lph = (uint32_t)(lissued / C::L_STAGES) & 1u;
-                    if (!mbar_wait(smem_u32(&Bar.lempty[ls]), lph ^ 1u, abort, err))
-                        break;
-                    const uint32_t lb = smem_u32(&Bar.lfull[ls]);
-                    mbar_expect_tx(lb, (uint32_t)C::L_STAGE);
-                    tma_load_2d(L_s + ls * C::L_STAGE, &tmB_lo, 0, tile * TW_N, lb);
-                    ++lissued;
-                }
                 const uint32_t fb = smem_u32(&Bar.full[slot]);
                 const uint32_t bst = B_s + slot * C::B_STAGE;
                 mbar_expect_tx(fb, (uint32_t)C::B_STAGE);
@@ -824,6 +816,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 mbar_wait(afull, 0u, &no_abort, err);
                 for (int g = (issued > C::STAGES ? issued - C::STAGES : 0); g < issued; ++g)
                     mbar_wait(smem_u32(&Bar.full[g % C::STAGES]), (uint32_t)(g / C::STAGES) & 1u, &no_abort, err);
+            }
+        }
+    }
+    else if (warp == 10)
+    {
+        // ------------------------------------------------------------ producer of the low ring
+        // (near tiles only), so that runs of near tiles do not hold back the
+        // high-part loads of the far tiles behind them
+        if (lane == 0)
+        {
+            ZigZag zz((int)(q0 / TW_N), ntiles);
+            for (int s = 0; s < it0; ++s)
+                zz.next();
+            int lissued = 0;
+            for (int it = 0; it < nit; ++it)
+            {
+                const int tile = zz.next();
+                if (!is_near(tile))
+                    continue;
+                const int ls = lissued % C::L_STAGES;
+                const uint32_t lph = (uint32_t)(lissued / C::L_STAGES) & 1u;
+                if (!mbar_wait(smem_u32(&Bar.lempty[ls]), lph ^ 1u, abort, err))
+                    break;
+                const uint32_t lb = smem_u32(&Bar.lfull[ls]);
+                mbar_expect_tx(lb, (uint32_t)C::L_STAGE);
+                tma_load_2d(L_s + ls * C::L_STAGE, &tmB_lo, 0, tile * TW_N, lb);
+                ++lissued;
+            }
+            if (*abort)
+            {
+                volatile int no_abort = 0;
                 for (int g = (lissued > C::L_STAGES ? lissued - C::L_STAGES : 0); g < lissued; ++g)
                     mbar_wait(smem_u32(&Bar.lfull[g % C::L_STAGES]), (uint32_t)(g / C::L_STAGES) & 1u, &no_abort,
                               err);
@@ -1426,7 +1449,7 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
         part_far = (float*)ctx->scratch.get("tw.pfar", sizeof(float) * (size_t)split_rows * parts);
     }
     TK_CUDA(cudaFuncSetAttribute(k_screen_tc_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TwCfg::SMEM));
-    k_screen_tc_wide<<<grid, TC_THREADS, TwCfg::SMEM, st>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad, bits, nwords,
+    k_screen_tc_wide<<<grid, TW_THREADS, TwCfg::SMEM, st>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad, bits, nwords,
                                                            cand_idx, cand_val, P.far_val, P.nrm, full_blocks, parts,
                                                            part_idx, part_val, part_far, Tb, P.rmax, c1, c2,
                                                            ctx->dev_err);
