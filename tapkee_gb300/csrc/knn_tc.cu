@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(TW_THREADS, 1)
                      int64_t Npad, const uint32_t* __restrict__ near_bits, int nwords,
                      int32_t* __restrict__ cand_idx, float* __restrict__ cand_val, float* __restrict__ far_val,
                      const float* __restrict__ nrm, int full_blocks, int parts, int32_t* __restrict__ part_idx,
-                     float* __restrict__ part_val, float* __restrict__ part_far, const float* __restrict__ Tb,
+                     float* __restrict__ part_val, float* __restrict__ part_far, const float* __restrict__ Trow,
                      const float* __restrict__ rmax, float c1, float c2, unsigned* err)
 {
     using C = TwCfg;
@@ -936,17 +936,19 @@ __global__ void __launch_bounds__(TW_THREADS, 1)
         const int64_t q = q0 + row;
         const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);  // a power of two: thr below is exact
         const float inv_m2 = 1.0f / m2;
-        // The list starts full of a bound instead of empty: B = 1.1 T_b + 2 eps
-        // (T_b bounds every row's k-th neighbour distance, eps is the row's screen
-        // error), so only candidates screened below it are inserted. A point never
-        // inserted has a screened value >= B, and the list's last value is
-        // min(B, the 32nd screened value), so the re-rank's certification against
-        // the last value covers it as before; B only spares the early inserts of
-        // an empty list (at most 32 per row, most of them displaced again).
+        // The list starts full of a bound instead of empty: B = 1.1 T_r + 2 eps
+        // (T_r bounds this row's k-th neighbour distance, eps is the row's screen
+        // error), so only candidates screened below it are inserted. The k nearest
+        // other points and the row itself screen below B, so at least k + 1 real
+        // entries survive. A point never inserted has a screened value >= B, and
+        // the list's last value is min(B, the 32nd screened value), so the
+        // re-rank's certification against the last value covers it as before.
+        // B spares every insert of a candidate that cannot be among the k nearest;
+        // a list that keeps fewer than 32 real entries ends in entries (B, -1).
         float cmp = FLT_MAX;
         {
             const float nq0 = nrm[q];
-            const float tb = Tb[blk];
+            const float tb = Trow[q];
             if (nq0 < FLT_MAX && tb < FLT_MAX)
             {
                 const float R = rmax[0];
@@ -1218,11 +1220,14 @@ __global__ void k_merge_parts(int64_t row0, int64_t rows, int parts, const int32
 // differences; the window is the whole block when it has fewer valid rows), or
 // +inf when the window has at most k rows. The window's rows are a subset of
 // all points, so each row's true k-th neighbour distance e_k is at most this.
+// Tr gets each row's own k-th window distance (+inf for padding rows), the
+// bound that seeds the row's candidate list in the screen.
 // Rows adjacent in the spatial order are the near ones, so the window loses
 // little against all 127 block-mates (6.9 % against 6.8 % near pairs on the
 // lifted Swiss roll) at half the work. One CTA per block, one thread per row.
 template <int DP>
-__global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ xc, int64_t N, int k, float* Tb)
+__global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ xc, int64_t N, int k, float* Tb,
+                                                      float* Tr)
 {
     __shared__ __align__(16) float xs[128][DP];
     __shared__ float wmax[4];
@@ -1290,6 +1295,7 @@ __global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ 
 #pragma unroll
     for (int s = 0; s < 32; ++s)
         mine = fmaxf(mine, (s < k && t < nvalid) ? L[s] : 0.f);
+    Tr[r0 + t] = (t < nvalid) ? mine : __int_as_float(0x7f800000);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
         mine = fmaxf(mine, __shfl_xor_sync(0xffffffffu, mine, o));
@@ -1410,6 +1416,7 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     float* tr = (float*)ctx->scratch.get("tw.tr", sizeof(float) * (size_t)nt);
     uint32_t* bits = (uint32_t*)ctx->scratch.get("tw.bits", sizeof(uint32_t) * (size_t)nq * nwords);
     float* Tb = (float*)ctx->scratch.get("tw.tb", sizeof(float) * (size_t)nq);
+    float* Trow = (float*)ctx->scratch.get("tw.trow", sizeof(float) * (size_t)P.Npad);
     P.far_val = (float*)ctx->scratch.get("tw.far", sizeof(float) * (size_t)P.Npad);
     float c1, c2, c2f;
     screen_error_model(TK_SCREEN_TENSOR, P.Dp, &c1, &c2);
@@ -1419,7 +1426,7 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     TK_CHECK_LAUNCH();
     k_spheres<TW_N><<<nt, 256, 0, st>>>(P.xc, P.N, P.Dp, tc, tr, tcT);
     TK_CHECK_LAUNCH();
-    k_blockmate<64><<<nq, 128, 0, st>>>(P.xc, P.N, k, Tb);
+    k_blockmate<64><<<nq, 128, 0, st>>>(P.xc, P.N, k, Tb, Trow);
     TK_CHECK_LAUNCH();
     k_classify<<<nq, 256, 0, st>>>(qc, qr, tcT, tr, Tb, nt, nwords, P.Dp, P.rmax, c1, c2f, bits);
     TK_CHECK_LAUNCH();
@@ -1451,7 +1458,7 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     TK_CUDA(cudaFuncSetAttribute(k_screen_tc_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TwCfg::SMEM));
     k_screen_tc_wide<<<grid, TW_THREADS, TwCfg::SMEM, st>>>(ah, al, bh, bl, bn, P.rmax + 1, P.N, P.Npad, bits, nwords,
                                                            cand_idx, cand_val, P.far_val, P.nrm, full_blocks, parts,
-                                                           part_idx, part_val, part_far, Tb, P.rmax, c1, c2,
+                                                           part_idx, part_val, part_far, Trow, P.rmax, c1, c2,
                                                            ctx->dev_err);
     TK_CHECK_LAUNCH();
     if (parts > 1)
