@@ -220,19 +220,24 @@ __device__ __forceinline__ float fmax3(float a, float b, float c)
     return r;
 }
 
-// Branchless sorted insertion into a register list (ascending).
+// Branchless sorted insertion into a register list (ascending); an entry equal
+// to v stays ahead of it. Slot s takes L[s-1] when v < L[s-1], v when
+// L[s-1] <= v < L[s], and keeps L[s] otherwise: for the values that is
+// min(L[s], max(v, L[s-1])), and each step's lower comparison is the next
+// step's upper one.
 template <int KC>
 __device__ __forceinline__ void reg_insert(float (&L)[KC], int32_t (&I)[KC], float v, int32_t id)
 {
+    bool up = v < L[KC - 1];
 #pragma unroll
     for (int s = KC - 1; s > 0; --s)
     {
-        const bool sh = v < L[s - 1];
-        const bool pl = !sh && (v < L[s]);
-        L[s] = sh ? L[s - 1] : (pl ? v : L[s]);
-        I[s] = sh ? I[s - 1] : (pl ? id : I[s]);
+        const bool lo = v < L[s - 1];
+        I[s] = lo ? I[s - 1] : (up ? id : I[s]);
+        L[s] = fminf(L[s], fmaxf(v, L[s - 1]));
+        up = lo;
     }
-    if (v < L[0])
+    if (up)
     {
         L[0] = v;
         I[0] = id;
@@ -1214,18 +1219,17 @@ __global__ void k_merge_parts(int64_t row0, int64_t rows, int parts, const int32
     far_val[q] = fv;
 }
 
-// Upper bound of the k-th neighbour distance of every query of a 128-row block:
-// the largest, over the block's rows, of the k-th smallest squared distance to
-// the other rows of a 64-row window of the block around its warp (direct FP32
-// differences; the window is the whole block when it has fewer valid rows), or
-// +inf when the window has at most k rows. The window's rows are a subset of
-// all points, so each row's true k-th neighbour distance e_k is at most this.
-// Tr gets each row's own k-th window distance (+inf for padding rows), the
-// bound that seeds the row's candidate list in the screen.
-// Rows adjacent in the spatial order are the near ones, so the window loses
-// little against all 127 block-mates (6.9 % against 6.8 % near pairs on the
-// lifted Swiss roll) at half the work. One CTA per block, one thread per row.
-template <int DP>
+// Upper bounds of the k-th neighbour distance, from the rows of each 128-row
+// block: Tr gets each row's k-th smallest squared distance to the other valid
+// rows of its block (direct FP32 differences; +inf for padding rows and when the
+// block has at most k valid rows), Tb the largest of them over the block. The
+// block's rows are a subset of all points, so each row's true k-th neighbour
+// distance e_k is at most its Tr. Tr seeds the row's candidate list in the
+// screen, Tb decides near and far tiles. One CTA per block, one thread per row;
+// all threads read the same row c at a time (shared-memory broadcast), and
+// the KB smallest distances stay sorted in registers (KB >= k), kept by a
+// min/max network.
+template <int DP, int KB>
 __global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ xc, int64_t N, int k, float* Tb,
                                                       float* Tr)
 {
@@ -1250,16 +1254,11 @@ __global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ 
         xr[4 * q + 2] = v.z;
         xr[4 * q + 3] = v.w;
     }
-    float L[32];  // the k smallest distances so far, ascending (k <= 32)
+    float L[KB];  // the KB smallest distances so far, ascending
 #pragma unroll
-    for (int s = 0; s < 32; ++s)
+    for (int s = 0; s < KB; ++s)
         L[s] = __int_as_float(0x7f800000);
-    // one window per warp (rows 32 w - 16 .. 32 w + 47, shifted into the block),
-    // so all lanes read the same row c: broadcast loads
-    const int w32 = t & ~31;
-    const int c_lo = (nvalid > 64) ? min(max(w32 - 16, 0), nvalid - 64) : 0;
-    const int c_hi = (nvalid > 64) ? c_lo + 64 : nvalid;
-    for (int c = c_lo; c < c_hi; ++c)
+    for (int c = 0; c < nvalid; ++c)
     {
         const float4* y4 = reinterpret_cast<const float4*>(&xs[c][0]);
         float d2a = 0.f, d2b = 0.f;
@@ -1278,14 +1277,13 @@ __global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ 
             z = xr[4 * q + 7] - yb.w;  d2b = fmaf(z, z, d2b);
         }
         const float d2 = d2a + d2b;
-        if (c != t && t < nvalid && d2 < L[31])
+        if (c != t && d2 < L[KB - 1])
         {
+            // slot s keeps L[s] when d2 >= L[s], takes d2 when L[s-1] <= d2 < L[s],
+            // and L[s-1] when d2 < L[s-1]
 #pragma unroll
-            for (int s = 31; s > 0; --s)
-            {
-                const bool sh = d2 < L[s - 1];
-                L[s] = sh ? L[s - 1] : (d2 < L[s] ? d2 : L[s]);
-            }
+            for (int s = KB - 1; s > 0; --s)
+                L[s] = fminf(L[s], fmaxf(d2, L[s - 1]));
             L[0] = fminf(L[0], d2);
         }
     }
@@ -1293,7 +1291,7 @@ __global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ 
     // rather than an indexed read keeps L in registers)
     float mine = 0.f;
 #pragma unroll
-    for (int s = 0; s < 32; ++s)
+    for (int s = 0; s < KB; ++s)
         mine = fmaxf(mine, (s < k && t < nvalid) ? L[s] : 0.f);
     Tr[r0 + t] = (t < nvalid) ? mine : __int_as_float(0x7f800000);
 #pragma unroll
@@ -1426,7 +1424,10 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     TK_CHECK_LAUNCH();
     k_spheres<TW_N><<<nt, 256, 0, st>>>(P.xc, P.N, P.Dp, tc, tr, tcT);
     TK_CHECK_LAUNCH();
-    k_blockmate<64><<<nq, 128, 0, st>>>(P.xc, P.N, k, Tb, Trow);
+    if (k <= 16)
+        k_blockmate<64, 16><<<nq, 128, 0, st>>>(P.xc, P.N, k, Tb, Trow);
+    else
+        k_blockmate<64, 32><<<nq, 128, 0, st>>>(P.xc, P.N, k, Tb, Trow);
     TK_CHECK_LAUNCH();
     k_classify<<<nq, 256, 0, st>>>(qc, qr, tcT, tr, Tb, nt, nwords, P.Dp, P.rmax, c1, c2f, bits);
     TK_CHECK_LAUNCH();

@@ -156,6 +156,7 @@ __device__ __forceinline__ bool row_view(const RowSpace& S, int64_t p, RowView& 
 }
 
 constexpr int RR_WARPS = 8;
+constexpr int RR_QMAX = 256;  // largest D whose query row is staged in shared memory
 
 // One warp per query row; lane l owns candidates l, l + 32, ... (KC <= 256).
 // float32 input: every candidate gets an FP32 direct-difference distance f (any
@@ -176,8 +177,10 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
     constexpr int PER = (KC + 31) / 32;
     constexpr int NONE = 0x7fffffff - 255;  // slots >= NONE hold no candidate
     __shared__ float f_s[RR_WARPS][KC];
+    __shared__ __align__(16) float q_s[RR_WARPS][RR_QMAX];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     float* fr = f_s[wib];
+    float* qs = q_s[wib];
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t p = warp; p < rows; p += nwarps)
@@ -226,6 +229,50 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                     const ff e = exact_key(X, dtype, ldx, D, i, j[s]);
                     kh[s] = e.hi;
                     kl[s] = e.lo;
+                }
+        }
+        else if (D <= RR_QMAX && (ldx & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
+        {
+            // FP32 screen of the candidates, lanes owning candidates: each lane
+            // reads its candidate's row with 16-byte loads (the rest of each
+            // sector stays in L1 for the next load) against the query row
+            // staged in shared memory, read as a broadcast
+            const float* Xf = reinterpret_cast<const float*>(X);
+            __syncwarp();
+            for (int d = lane; d < D; d += 32)
+                qs[d] = __ldg(Xf + i * ldx + d);
+            __syncwarp();
+            const int D4 = D >> 2;
+            const float4* q4 = reinterpret_cast<const float4*>(qs);
+#pragma unroll
+            for (int s = 0; s < PER; ++s)
+                if (j[s] < NONE)
+                {
+                    const float* yr = Xf + (int64_t)j[s] * ldx;
+                    const float4* y4 = reinterpret_cast<const float4*>(yr);
+                    float a = 0.f, b = 0.f;
+#pragma unroll 4
+                    for (int t = 0; t < D4; ++t)
+                    {
+                        const float4 y = __ldg(y4 + t);
+                        const float4 x = q4[t];
+                        float z;
+                        z = y.x - x.x;
+                        a = fmaf(z, z, a);
+                        z = y.y - x.y;
+                        b = fmaf(z, z, b);
+                        z = y.z - x.z;
+                        a = fmaf(z, z, a);
+                        z = y.w - x.w;
+                        b = fmaf(z, z, b);
+                    }
+                    for (int d = 4 * D4; d < D; ++d)
+                    {
+                        const float z = __ldg(yr + d) - qs[d];
+                        a = fmaf(z, z, a);
+                    }
+                    kh[s] = a + b;
+                    exact[s] = false;
                 }
         }
         else
