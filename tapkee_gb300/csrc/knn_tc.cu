@@ -941,9 +941,14 @@ __global__ void __launch_bounds__(TW_THREADS, 1)
         const int64_t q = q0 + row;
         const float m2 = -exp2f(1.0f - 2.0f * scale_log2[0]);  // a power of two: thr below is exact
         const float inv_m2 = 1.0f / m2;
-        // The list starts full of a bound instead of empty: B = 1.1 T_r + 2 eps
+        // The list starts full of a bound instead of empty: B = 1.01 T_r + 2 eps
         // (T_r bounds this row's k-th neighbour distance, eps is the row's screen
-        // error), so only candidates screened below it are inserted. The k nearest
+        // error), so only candidates screened below it are inserted. T_r is an
+        // FP32 direct-difference sum over centred coordinates: its relative
+        // rounding (D + 2) 2^-24 is far inside the 1 %, and the centring error
+        // of a squared distance, at most 2^-22 d R, inside one eps (>= c1 R^2 with
+        // c1 >= 16 2^-24, and d <= 2 R). A neighbour y of the k nearest so screens
+        // at most e_k + eps < B. The k nearest
         // other points and the row itself screen below B, so at least k + 1 real
         // entries survive. A point never inserted has a screened value >= B, and
         // the list's last value is min(B, the 32nd screened value), so the
@@ -958,7 +963,7 @@ __global__ void __launch_bounds__(TW_THREADS, 1)
             {
                 const float R = rmax[0];
                 const float eps = c1 * (nq0 + R * R) + c2 * sqrtf(nq0) * R;
-                cmp = fmaf(1.1f, tb, 2.f * eps) - nq0;
+                cmp = fmaf(1.01f, tb, 2.f * eps) - nq0;
             }
         }
         float L[KC];
