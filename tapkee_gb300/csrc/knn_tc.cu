@@ -1249,39 +1249,35 @@ __global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ 
         xs[r][d] = (r < nvalid) ? xc[(r0 + r) * DP + d] : 0.f;
     }
     __syncthreads();
-    float xr[DP];  // this thread's row
+    float2 xr[DP / 2];  // this thread's row, in pairs for the packed FP32 instructions
 #pragma unroll
     for (int q = 0; q < DP / 4; ++q)
     {
         const float4 v = reinterpret_cast<const float4*>(&xs[t][0])[q];
-        xr[4 * q] = v.x;
-        xr[4 * q + 1] = v.y;
-        xr[4 * q + 2] = v.z;
-        xr[4 * q + 3] = v.w;
+        xr[2 * q] = make_float2(v.x, v.y);
+        xr[2 * q + 1] = make_float2(v.z, v.w);
     }
     float L[KB];  // the KB smallest distances so far, ascending
 #pragma unroll
     for (int s = 0; s < KB; ++s)
         L[s] = __int_as_float(0x7f800000);
+    const float2 m1 = make_float2(-1.f, -1.f);
     for (int c = 0; c < nvalid; ++c)
     {
+        // two dimensions per instruction: z = x - y (one rounding, as a
+        // subtraction), acc += z z; four partial sums
         const float4* y4 = reinterpret_cast<const float4*>(&xs[c][0]);
-        float d2a = 0.f, d2b = 0.f;
+        float2 aa = make_float2(0.f, 0.f), ab = aa;
 #pragma unroll
-        for (int q = 0; q < DP / 4; q += 2)
+        for (int q = 0; q < DP / 4; ++q)
         {
-            const float4 ya = y4[q], yb = y4[q + 1];
-            float z;
-            z = xr[4 * q] - ya.x;      d2a = fmaf(z, z, d2a);
-            z = xr[4 * q + 1] - ya.y;  d2a = fmaf(z, z, d2a);
-            z = xr[4 * q + 2] - ya.z;  d2a = fmaf(z, z, d2a);
-            z = xr[4 * q + 3] - ya.w;  d2a = fmaf(z, z, d2a);
-            z = xr[4 * q + 4] - yb.x;  d2b = fmaf(z, z, d2b);
-            z = xr[4 * q + 5] - yb.y;  d2b = fmaf(z, z, d2b);
-            z = xr[4 * q + 6] - yb.z;  d2b = fmaf(z, z, d2b);
-            z = xr[4 * q + 7] - yb.w;  d2b = fmaf(z, z, d2b);
+            const float4 y = y4[q];
+            const float2 z0 = __ffma2_rn(make_float2(y.x, y.y), m1, xr[2 * q]);
+            const float2 z1 = __ffma2_rn(make_float2(y.z, y.w), m1, xr[2 * q + 1]);
+            aa = __ffma2_rn(z0, z0, aa);
+            ab = __ffma2_rn(z1, z1, ab);
         }
-        const float d2 = d2a + d2b;
+        const float d2 = (aa.x + aa.y) + (ab.x + ab.y);
         if (c != t && d2 < L[KB - 1])
         {
             // slot s keeps L[s] when d2 >= L[s], takes d2 when L[s-1] <= d2 < L[s],

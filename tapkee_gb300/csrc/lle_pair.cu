@@ -18,7 +18,10 @@
 //     (z = big + small + O(2^-22 |z|)), three products per term (big.big,
 //     big.small, small.big) accumulated in FP32. This is an FP32-accurate Gram;
 //     like the FP32 Gram of k_lle it only seeds the factor, and the float-float
-//     refinement against the exact differences sets the accuracy of w.
+//     refinement against the exact differences sets the accuracy of w;
+//   * the refinement's float-float products and sums run on Blackwell's packed
+//     FP32 instructions (__fadd2_rn, __fmul2_rn, __ffma2_rn), two neighbours per
+//     instruction, each component rounded as its scalar form.
 // Requires float32 input with 16-byte aligned rows (X 16-byte aligned, ldx a
 // multiple of 4); other inputs take k_lle.
 #include <cfloat>
@@ -60,15 +63,26 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1
                  : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// acc += p (hi + lo) without renormalising: acc.hi is the running sum, acc.lo
-// collects the exact rounding error of each addition and the low parts
-__device__ __forceinline__ void ff_acc(ff& acc, float ph, float pl)
+// Packed FP32 (two lanes of arithmetic per instruction) forms of the
+// error-free transformations: each component is rounded exactly as the scalar
+// __fadd_rn / __fmul_rn / fmaf would round it.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)  // a - b, one rounding
 {
-    const float s = __fadd_rn(acc.hi, ph);
-    const float bb = __fsub_rn(s, acc.hi);
-    const float e = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
-    acc.hi = s;
-    acc.lo = __fadd_rn(acc.lo, __fadd_rn(e, pl));
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// acc += p (ph + pl) without renormalising, for two independent accumulators:
+// acc.hi is the running sum, acc.lo collects the exact rounding error of each
+// addition (Knuth's two-sum) and the low parts
+__device__ __forceinline__ void ff_acc2(float2& ah, float2& al, float2 ph, float2 pl)
+{
+    const float2 s = add2(ah, ph);
+    const float2 bb = sub2(s, ah);
+    const float2 e = add2(sub2(ah, sub2(s, bb)), sub2(ph, bb));
+    ah = s;
+    al = add2(al, add2(e, pl));
 }
 
 // Lane l of a 16-lane segment holds row l of a 16 x 16 SPD matrix (L[c], c <= l)
@@ -276,11 +290,15 @@ __global__ void __launch_bounds__(PW * 32, 2)
             __syncwarp();
             S.w[h][l] = w;
             __syncwarp();
-            const float* wb = S.w[h];
-            ff part[16];
+            const float2* wb2 = reinterpret_cast<const float2*>(S.w[h]);
+            // neighbours in pairs (2i, 2i + 1): one packed instruction for both
+            float2 pth[8], ptl[8];
 #pragma unroll
-            for (int a = 0; a < 16; ++a)
-                part[a] = ff_zero();
+            for (int i = 0; i < 8; ++i)
+            {
+                pth[i] = make_float2(0.f, 0.f);
+                ptl[i] = make_float2(0.f, 0.f);
+            }
             for (int ch = 0; ch < nchunks; ++ch)
             {
                 if (nchunks > 1)
@@ -296,25 +314,41 @@ __global__ void __launch_bounds__(PW * 32, 2)
                     if (ch * CH + d >= D)
                         break;
                     const float xd = S.xr[h][d];
-                    float zh[16], zl[16];
-                    ff v = ff_zero();
+                    const float2 x2 = make_float2(xd, xd);
+                    float2 zh[8], zl[8];
+                    float2 vh = make_float2(0.f, 0.f), vl = vh;  // v over even / odd neighbours
 #pragma unroll
-                    for (int a = 0; a < 16; ++a)
+                    for (int i = 0; i < 8; ++i)
                     {
-                        const ff z = two_sum(S.nr[h][a][d], -xd);  // exact difference
-                        zh[a] = z.hi;
-                        zl[a] = z.lo;
-                        const ff pz = two_prod(wb[a], z.hi);
-                        ff_acc(v, pz.hi, fmaf(wb[a], z.lo, pz.lo));
+                        // exact difference n - x = zh + zl (Knuth's two-sum)
+                        const float2 n2 = make_float2(S.nr[h][2 * i][d], S.nr[h][2 * i + 1][d]);
+                        const float2 zs = sub2(n2, x2);
+                        const float2 bb = sub2(zs, n2);
+                        zh[i] = zs;
+                        zl[i] = sub2(sub2(n2, sub2(zs, bb)), add2(x2, bb));
+                        // w z = p + pe exactly for the high part, plus w zl
+                        const float2 w2 = wb2[i];
+                        const float2 pp = __fmul2_rn(w2, zs);
+                        const float2 pe = __ffma2_rn(w2, zs, neg2(pp));
+                        ff_acc2(vh, vl, pp, __ffma2_rn(w2, zl[i], pe));
                     }
-                    v = fast_two_sum(v.hi, v.lo);
+                    ff v = ff_add(ff{vh.x, vl.x}, ff{vh.y, vl.y});
+                    const float2 vh2 = make_float2(v.hi, v.hi), vl2 = make_float2(v.lo, v.lo);
 #pragma unroll
-                    for (int a = 0; a < 16; ++a)
+                    for (int i = 0; i < 8; ++i)
                     {
-                        const ff pz = two_prod(zh[a], v.hi);
-                        ff_acc(part[a], pz.hi, fmaf(zh[a], v.lo, fmaf(zl[a], v.hi, pz.lo)));
+                        const float2 pp = __fmul2_rn(zh[i], vh2);
+                        const float2 pe = __ffma2_rn(zh[i], vh2, neg2(pp));
+                        ff_acc2(pth[i], ptl[i], pp, __ffma2_rn(zh[i], vl2, __ffma2_rn(zl[i], vh2, pe)));
                     }
                 }
+            }
+            ff part[16];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+            {
+                part[2 * i] = ff{pth[i].x, ptl[i].x};
+                part[2 * i + 1] = ff{pth[i].y, ptl[i].y};
             }
             // reduce-scatter over the 16 lanes: lane l ends with (C w)_l
 #pragma unroll

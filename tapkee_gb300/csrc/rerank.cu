@@ -250,28 +250,27 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                 {
                     const float* yr = Xf + (int64_t)j[s] * ldx;
                     const float4* y4 = reinterpret_cast<const float4*>(yr);
-                    float a = 0.f, b = 0.f;
-#pragma unroll 4
+                    // two dimensions per packed FP32 instruction: z = y - x (one
+                    // rounding, as a subtraction), acc += z z
+                    const float2 m1 = make_float2(-1.f, -1.f);
+                    float2 aa = make_float2(0.f, 0.f), ab = aa;
+#pragma unroll 8
                     for (int t = 0; t < D4; ++t)
                     {
                         const float4 y = __ldg(y4 + t);
                         const float4 x = q4[t];
-                        float z;
-                        z = y.x - x.x;
-                        a = fmaf(z, z, a);
-                        z = y.y - x.y;
-                        b = fmaf(z, z, b);
-                        z = y.z - x.z;
-                        a = fmaf(z, z, a);
-                        z = y.w - x.w;
-                        b = fmaf(z, z, b);
+                        const float2 z0 = __ffma2_rn(make_float2(x.x, x.y), m1, make_float2(y.x, y.y));
+                        const float2 z1 = __ffma2_rn(make_float2(x.z, x.w), m1, make_float2(y.z, y.w));
+                        aa = __ffma2_rn(z0, z0, aa);
+                        ab = __ffma2_rn(z1, z1, ab);
                     }
+                    float a = (aa.x + aa.y) + (ab.x + ab.y);
                     for (int d = 4 * D4; d < D; ++d)
                     {
                         const float z = __ldg(yr + d) - qs[d];
                         a = fmaf(z, z, a);
                     }
-                    kh[s] = a + b;
+                    kh[s] = a;
                     exact[s] = false;
                 }
         }
