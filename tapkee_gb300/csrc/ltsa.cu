@@ -24,13 +24,20 @@ namespace {
 // TD bounds the basis width td (the refinement's arrays): 2, 4 or 8. The float
 // kernel takes the smallest that fits td, which keeps its shared memory, and so
 // its warps per SM, in step with the basis actually asked for.
+// One rotation of a Jacobi round: rows/columns (p, q), cosine and sine.
+template <typename T>
+struct alignas(2 * sizeof(T)) JacobiRot
+{
+    int p, q;
+    T c, s;
+};
+
 template <int M, typename T, int TD = 8>
 struct JacobiSmem
 {
     T A[M][M + 1];
     T V[M][M + 1];
-    T rc[M / 2], rs[M / 2];
-    int rp[M / 2], rq[M / 2];
+    JacobiRot<T> rot[M / 2];
     float Z[M][33];
     float Zl[M][33];     // low parts of the centred coordinates
     float th[32][TD], tl[32][TD];  // t = Zc^T V for one chunk, float-float
@@ -79,9 +86,40 @@ __device__ __forceinline__ void stage_centred(JacobiSmem<M, T, TD>& S, int lane,
 
 // Parallel cyclic Jacobi on the symmetric M x M matrix S.A (one warp). On exit
 // diag(A) holds the eigenvalues and the columns of V the eigenvectors.
+// A round applies M/2 disjoint rotations G = [[c, -s], [s, c]] at once:
+// A <- G A G^T, V <- V G^T. With the indices grouped by rotation, every 2 x 2
+// block B of A (rows of rotation i, columns of rotation j) becomes
+// G_i B G_j^T, independently of every other block; a lane updates whole blocks
+// of the upper triangle (i <= j) and writes both triangles, so one pass over
+// the blocks replaces a row pass and a column pass. A diagonal block's
+// off-diagonal entry, which its rotation annihilates, is set to zero.
 template <int M, typename T, int TD>
 __device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
 {
+    constexpr int H = M / 2;             // rotations per round
+    constexpr int NB = H * (H + 1) / 2;  // blocks (i <= j)
+    constexpr int NBR = (NB + 31) / 32;  // blocks per lane
+    constexpr int NV = M * H;            // (row of V, rotation) pairs
+    constexpr int NVR = (NV + 31) / 32;
+    // this lane's blocks: e = lane + 32 r in row-major order of the upper triangle
+    int bi[NBR], bj[NBR];
+#pragma unroll
+    for (int r = 0; r < NBR; ++r)
+    {
+        int e = lane + 32 * r, i = 0;
+        bi[r] = -1;
+        bj[r] = 0;
+        if (e < NB)
+        {
+            while (e >= H - i)
+            {
+                e -= H - i;
+                ++i;
+            }
+            bi[r] = i;
+            bj[r] = i + e;
+        }
+    }
     for (int t = lane; t < M * M; t += 32)
         S.V[t / M][t % M] = (t / M == t % M) ? T(1) : T(0);
     __syncwarp();
@@ -114,7 +152,7 @@ __device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
             break;
         for (int round = 0; round < M - 1; ++round)
         {
-            if (lane < M / 2)
+            if (lane < H)
             {
                 auto pos = [&](int t) { return t == 0 ? 0 : 1 + ((t - 1 + round) % (M - 1)); };
                 int p = pos(lane), q = pos(M - 1 - lane);
@@ -133,35 +171,55 @@ __device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
                     c = T(1) / sqrt(tt * tt + T(1));
                     s = tt * c;
                 }
-                S.rp[lane] = p;
-                S.rq[lane] = q;
-                S.rc[lane] = c;
-                S.rs[lane] = s;
+                S.rot[lane] = JacobiRot<T>{p, q, c, s};
             }
             __syncwarp();
-            // rows: A[p,:], A[q,:]
-            for (int e = lane; e < (M / 2) * M; e += 32)
+            // A: the blocks of the upper triangle, both triangles written
+#pragma unroll
+            for (int r = 0; r < NBR; ++r)
             {
-                const int i = e / M, j = e % M;
-                const int p = S.rp[i], q = S.rq[i];
-                const T c = S.rc[i], s = S.rs[i];
-                const T apj = S.A[p][j], aqj = S.A[q][j];
-                S.A[p][j] = c * apj - s * aqj;
-                S.A[q][j] = s * apj + c * aqj;
+                if (bi[r] < 0)
+                    continue;
+                const JacobiRot<T> ri = S.rot[bi[r]], rj = S.rot[bj[r]];
+                const T b00 = S.A[ri.p][rj.p], b01 = S.A[ri.p][rj.q];
+                const T b10 = S.A[ri.q][rj.p], b11 = S.A[ri.q][rj.q];
+                // X = B G_j^T, then Y = G_i X
+                const T x00 = b00 * rj.c - b01 * rj.s, x01 = b00 * rj.s + b01 * rj.c;
+                const T x10 = b10 * rj.c - b11 * rj.s, x11 = b10 * rj.s + b11 * rj.c;
+                const T y00 = ri.c * x00 - ri.s * x10, y10 = ri.s * x00 + ri.c * x10;
+                T y01 = ri.c * x01 - ri.s * x11;
+                T y10w = y10;
+                const T y11 = ri.s * x01 + ri.c * x11;
+                if (bi[r] == bj[r])
+                {
+                    y01 = T(0);
+                    y10w = T(0);
+                }
+                S.A[ri.p][rj.p] = y00;
+                S.A[ri.p][rj.q] = y01;
+                S.A[ri.q][rj.p] = y10w;
+                S.A[ri.q][rj.q] = y11;
+                if (bi[r] != bj[r])
+                {
+                    S.A[rj.p][ri.p] = y00;
+                    S.A[rj.q][ri.p] = y01;
+                    S.A[rj.p][ri.q] = y10w;
+                    S.A[rj.q][ri.q] = y11;
+                }
             }
-            __syncwarp();
-            // columns: A[:,p], A[:,q] and V[:,p], V[:,q]
-            for (int e = lane; e < (M / 2) * M; e += 32)
+            // V <- V G^T: row a, rotation i
+#pragma unroll
+            for (int r = 0; r < NVR; ++r)
             {
-                const int i = e / M, j = e % M;
-                const int p = S.rp[i], q = S.rq[i];
-                const T c = S.rc[i], s = S.rs[i];
-                const T ajp = S.A[j][p], ajq = S.A[j][q];
-                S.A[j][p] = c * ajp - s * ajq;
-                S.A[j][q] = s * ajp + c * ajq;
-                const T vjp = S.V[j][p], vjq = S.V[j][q];
-                S.V[j][p] = c * vjp - s * vjq;
-                S.V[j][q] = s * vjp + c * vjq;
+                const int e = lane + 32 * r;
+                if (e < NV)
+                {
+                    const int a = e / H, i = e % H;
+                    const JacobiRot<T> ri = S.rot[i];
+                    const T vp = S.V[a][ri.p], vq = S.V[a][ri.q];
+                    S.V[a][ri.p] = ri.c * vp - ri.s * vq;
+                    S.V[a][ri.q] = ri.s * vp + ri.c * vq;
+                }
             }
             __syncwarp();
         }
