@@ -168,7 +168,12 @@ __device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
                 {
                     const T theta = (aqq - app) / (T(2) * apq);
                     const T tt = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
-                    c = T(1) / sqrt(tt * tt + T(1));
+                    // c^2 + s^2 = 1 to the rounding of c either way; FP32 takes
+                    // the hardware reciprocal square root (2 ulp) for 1 / sqrt
+                    if constexpr (sizeof(T) == 4)
+                        c = rsqrtf(fmaf(tt, tt, 1.f));
+                    else
+                        c = T(1) / sqrt(tt * tt + T(1));
                     s = tt * c;
                 }
                 S.rot[lane] = JacobiRot<T>{p, q, c, s};

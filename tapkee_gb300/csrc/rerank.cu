@@ -164,7 +164,8 @@ constexpr int RR_QMAX = 256;  // largest D whose query row is staged in shared m
 // |f - d2| <= gam f (gam = (D + 8) 2^-23). Since gam f is increasing in f, the
 // intervals [(1 - gam) f, (1 + gam) f] of candidates taken in f order are
 // ordered too wherever neighbours in that order do not overlap; so only the
-// candidates whose interval overlaps a rank neighbour among the first k + 1
+// candidates whose interval overlaps a rank neighbour among the first k + 1,
+// and the later ones whose interval reaches below the upper end of rank k's,
 // need their exact (float-float) distance, and the ranking by (key, index) with
 // key = exact value where computed, else f, is the exact ranking. float64 input:
 // every candidate's distance in FP64.
@@ -352,6 +353,11 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
             __syncwarp();
             bool need[PER];
             bool any = false;
+            // upper end of the interval of rank k (the (k + 1)-th smallest f): a
+            // candidate of a later rank whose interval reaches below it may still
+            // be among the first k + 1 once exact values replace f, so it is
+            // refined too (equal f at the boundary: duplicated points)
+            const float U = fr[k] * (1.f + gam);
 #pragma unroll
             for (int s = 0; s < PER; ++s)
             {
@@ -368,6 +374,8 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                     if (V.d2_out && r < k)
                         need[s] = true;
                 }
+                else if (!exact[s] && kh[s] * (1.f - gam) <= U)
+                    need[s] = true;
                 any |= need[s];
             }
             if (__any_sync(0xffffffffu, any))
@@ -502,40 +510,66 @@ __global__ void __launch_bounds__(256) k_fallback(const RowSpace RS, const int32
         const int64_t i = V.i;
         int32_t* idx_out = V.idx_out;
         double* d2_out = V.d2_out;
-        const double ub = failed_ub[f];
+        double ub = failed_ub[f];
         // FP32 direct-difference filter with a relative slack covering its error
         const double slack = (double)(D + 8) * 1.1920928955078125e-07;
-        const float thr = (float)(ub * (1.0 + slack)) * 1.0000005f + 1e-30f;
-        if (threadIdx.x == 0)
+        // More survivors than slots: the k-th smallest exact distance among the
+        // FB_CAP kept (real points) bounds e_k too, so the scan is repeated with
+        // that tighter bound (a few times at most).
+        for (int attempt = 0;; ++attempt)
         {
-            cnt = 0;
-            edge_n = 0;
-        }
-        __syncthreads();
-        for (int64_t jj = threadIdx.x; jj < N; jj += blockDim.x)
-        {
-            if (jj == i)
-                continue;
-            float acc = 0.f;
-            for (int d0 = 0; d0 < D; d0 += 1024)
+            const float thr = (float)(ub * (1.0 + slack)) * 1.0000005f + 1e-30f;
+            if (threadIdx.x == 0)
             {
-                // D > 1024 is handled in chunks without caching the query
-                for (int d = d0; d < min(D, d0 + 1024); ++d)
+                cnt = 0;
+                edge_n = 0;
+            }
+            __syncthreads();
+            for (int64_t jj = threadIdx.x; jj < N; jj += blockDim.x)
+            {
+                if (jj == i)
+                    continue;
+                float acc = 0.f;
+                for (int d0 = 0; d0 < D; d0 += 1024)
                 {
-                    const float v = (float)(ldx_elem(X, dtype, jj * ldx + d) - ldx_elem(X, dtype, i * ldx + d));
-                    acc = fmaf(v, v, acc);
+                    // D > 1024 is handled in chunks without caching the query
+                    for (int d = d0; d < min(D, d0 + 1024); ++d)
+                    {
+                        const float v = (float)(ldx_elem(X, dtype, jj * ldx + d) - ldx_elem(X, dtype, i * ldx + d));
+                        acc = fmaf(v, v, acc);
+                    }
+                }
+                if (acc <= thr)
+                {
+                    const unsigned s = atomicAdd(&cnt, 1u);
+                    if (s < FB_CAP)
+                        sj[s] = (int32_t)jj;
                 }
             }
-            if (acc <= thr)
+            __syncthreads();
+            if (cnt <= (unsigned)FB_CAP)
+                break;
+            if (attempt == 4)
             {
-                const unsigned s = atomicAdd(&cnt, 1u);
-                if (s < FB_CAP)
-                    sj[s] = (int32_t)jj;
-                else
+                if (threadIdx.x == 0)
                     atomicOr(err, DEV_ERR_OVERFLOW);
+                break;
             }
+            for (unsigned t = threadIdx.x; t < (unsigned)FB_CAP; t += blockDim.x)
+                sd[t] = exact_d2(X, dtype, ldx, D, i, sj[t]);
+            __syncthreads();
+            for (unsigned t = threadIdx.x; t < (unsigned)FB_CAP; t += blockDim.x)
+            {
+                unsigned r = 0;
+                for (unsigned m = 0; m < (unsigned)FB_CAP; ++m)
+                    r += (sd[m] < sd[t] || (sd[m] == sd[t] && m < t)) ? 1u : 0u;
+                if (r == (unsigned)k - 1)
+                    edge[0] = sd[t];  // the kept set's k-th smallest
+            }
+            __syncthreads();
+            ub = edge[0];
+            __syncthreads();
         }
-        __syncthreads();
         const unsigned n = min(cnt, (unsigned)FB_CAP);
         for (unsigned t = threadIdx.x; t < n; t += blockDim.x)
             sd[t] = exact_d2(X, dtype, ldx, D, i, sj[t]);

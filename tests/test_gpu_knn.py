@@ -87,7 +87,15 @@ def _duplicates(dtype):
     return np.ascontiguousarray(np.repeat(base, 40, axis=0), dtype=dtype)
 
 
+def _copies4(dtype):
+    base = np.random.default_rng(4).normal(size=(50, 8))
+    return np.ascontiguousarray(np.repeat(base, 4, axis=0), dtype=dtype)
+
+
 TIE_CASES = [
+    # the nearest other point's 4 copies straddle ranks k - 1, k and k + 1: equal
+    # FP32 distances past rank k must be refined with the others
+    ("4 copies of 50 points, k=5", lambda dt: _copies4(dt), 5),
     ("40 copies of 5 points, k=3", lambda dt: _duplicates(dt), 3),
     ("40 copies of 5 points, k=6", lambda dt: _duplicates(dt), 6),
     ("40 copies of 5 points, k=45", lambda dt: _duplicates(dt), 45),
