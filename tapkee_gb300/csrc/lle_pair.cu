@@ -73,6 +73,18 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b)  // a - b, one roundi
 }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
+// (h + l) += (bh + bl) for two independent float-float values, as ff_add
+__device__ __forceinline__ void ff_add2(float2& h, float2& l, float2 bh, float2 bl)
+{
+    const float2 s = add2(h, bh);
+    const float2 bb = sub2(s, h);
+    const float2 e = add2(sub2(h, sub2(s, bb)), sub2(bh, bb));
+    const float2 lo = add2(e, add2(l, bl));
+    const float2 s2 = add2(s, lo);  // fast two-sum: |s| >= |lo|
+    h = s2;
+    l = sub2(lo, sub2(s2, s));
+}
+
 // acc += p (ph + pl) without renormalising, for two independent accumulators:
 // acc.hi is the running sum, acc.lo collects the exact rounding error of each
 // addition (Knuth's two-sum) and the low parts
@@ -224,13 +236,14 @@ __global__ void __launch_bounds__(PW * 32, 2)
                 {
                     const int d0 = kk * 8 + t, d1 = d0 + 4;
                     const float xa = S.xr[P][d0], xb = S.xr[P][d1];
-                    const float z00 = S.nr[P][g][d0] - xa, z10 = S.nr[P][g + 8][d0] - xa;
-                    const float z01 = S.nr[P][g][d1] - xb, z11 = S.nr[P][g + 8][d1] - xb;
-                    const uint32_t b00 = to_tf32(z00), b10 = to_tf32(z10), b01 = to_tf32(z01), b11 = to_tf32(z11);
-                    const uint32_t s00 = to_tf32(z00 - __uint_as_float(b00));
-                    const uint32_t s10 = to_tf32(z10 - __uint_as_float(b10));
-                    const uint32_t s01 = to_tf32(z01 - __uint_as_float(b01));
-                    const uint32_t s11 = to_tf32(z11 - __uint_as_float(b11));
+                    // (rows g, g + 8) per packed instruction
+                    const float2 za = sub2(make_float2(S.nr[P][g][d0], S.nr[P][g + 8][d0]), make_float2(xa, xa));
+                    const float2 zb = sub2(make_float2(S.nr[P][g][d1], S.nr[P][g + 8][d1]), make_float2(xb, xb));
+                    const uint32_t b00 = to_tf32(za.x), b10 = to_tf32(za.y), b01 = to_tf32(zb.x), b11 = to_tf32(zb.y);
+                    const float2 sa = sub2(za, make_float2(__uint_as_float(b00), __uint_as_float(b10)));
+                    const float2 sb = sub2(zb, make_float2(__uint_as_float(b01), __uint_as_float(b11)));
+                    const uint32_t s00 = to_tf32(sa.x), s10 = to_tf32(sa.y);
+                    const uint32_t s01 = to_tf32(sb.x), s11 = to_tf32(sb.y);
                     // A = rows g, g + 8 of Z; B (= Z^T) for neighbours 0-7 is row g,
                     // for neighbours 8-15 row g + 8
                     mma_tf32(acc[P][0], b00, b10, b01, b11, b00, b01);
@@ -343,25 +356,33 @@ __global__ void __launch_bounds__(PW * 32, 2)
                     }
                 }
             }
-            ff part[16];
+            // reduce-scatter over the 16 lanes: lane l ends with (C w)_l; the
+            // neighbour pairs (2i, 2i + 1) add with packed instructions down to
+            // two values, then the last level is scalar
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
+            for (int o = 4; o > 0; o >>= 1)  // pair offsets: value offsets 8, 4, 2
             {
-                part[2 * i] = ff{pth[i].x, ptl[i].x};
-                part[2 * i + 1] = ff{pth[i].y, ptl[i].y};
-            }
-            // reduce-scatter over the 16 lanes: lane l ends with (C w)_l
-#pragma unroll
-            for (int o = 8; o > 0; o >>= 1)
-            {
-                const bool upper = (l & o) != 0;
+                const bool upper = (l & (2 * o)) != 0;
 #pragma unroll
                 for (int q = 0; q < o; ++q)
                 {
-                    const ff send = upper ? part[q] : part[q + o];
-                    const ff keep = upper ? part[q + o] : part[q];
-                    part[q] = ff_add(keep, ff_shfl_xor(send, o));
+                    const float2 sh = upper ? pth[q] : pth[q + o], sl = upper ? ptl[q] : ptl[q + o];
+                    float2 kh = upper ? pth[q + o] : pth[q], kl = upper ? ptl[q + o] : ptl[q];
+                    const float2 rh = make_float2(__shfl_xor_sync(0xffffffffu, sh.x, 2 * o),
+                                                  __shfl_xor_sync(0xffffffffu, sh.y, 2 * o));
+                    const float2 rl = make_float2(__shfl_xor_sync(0xffffffffu, sl.x, 2 * o),
+                                                  __shfl_xor_sync(0xffffffffu, sl.y, 2 * o));
+                    ff_add2(kh, kl, rh, rl);
+                    pth[q] = kh;
+                    ptl[q] = kl;
                 }
+            }
+            ff part[1];
+            {
+                const bool upper = (l & 1) != 0;
+                const ff send = upper ? ff{pth[0].x, ptl[0].x} : ff{pth[0].y, ptl[0].y};
+                const ff keep = upper ? ff{pth[0].y, ptl[0].y} : ff{pth[0].x, ptl[0].x};
+                part[0] = ff_add(keep, ff_shfl_xor(send, 1));
             }
             float r = 0.f;
             if (l < k)

@@ -36,7 +36,7 @@ template <int M, typename T, int TD = 8>
 struct JacobiSmem
 {
     T A[M][M + 1];
-    T V[M][M + 1];
+    T VT[M][M + 2];  // eigenvectors as rows (VT[j][a] = V[a][j]); even stride: 8-byte pairs
     JacobiRot<T> rot[M / 2];
     float Z[M][33];
     float Zl[M][33];     // low parts of the centred coordinates
@@ -101,6 +101,8 @@ __device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
     constexpr int NBR = (NB + 31) / 32;  // blocks per lane
     constexpr int NV = M * H;            // (row of V, rotation) pairs
     constexpr int NVR = (NV + 31) / 32;
+    constexpr int NV2 = H * (M / 2);     // (rotation, pair of rows of V) for FP32
+    constexpr int NVR2 = (NV2 + 31) / 32;
     // this lane's blocks: e = lane + 32 r in row-major order of the upper triangle
     int bi[NBR], bj[NBR];
 #pragma unroll
@@ -121,7 +123,7 @@ __device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
         }
     }
     for (int t = lane; t < M * M; t += 32)
-        S.V[t / M][t % M] = (t / M == t % M) ? T(1) : T(0);
+        S.VT[t / M][t % M] = (t / M == t % M) ? T(1) : T(0);
     __syncwarp();
     for (int sweep = 0; sweep < max_sweeps; ++sweep)
     {
@@ -212,18 +214,40 @@ __device__ void warp_jacobi(JacobiSmem<M, T, TD>& S, int lane, int max_sweeps)
                     S.A[rj.q][ri.q] = y11;
                 }
             }
-            // V <- V G^T: row a, rotation i
-#pragma unroll
-            for (int r = 0; r < NVR; ++r)
+            // V <- V G^T, i.e. rows p and q of VT: rotation i, entries (2 a2, 2 a2 + 1)
+            if constexpr (sizeof(T) == 4)
             {
-                const int e = lane + 32 * r;
-                if (e < NV)
+#pragma unroll
+                for (int r = 0; r < NVR2; ++r)
                 {
-                    const int a = e / H, i = e % H;
-                    const JacobiRot<T> ri = S.rot[i];
-                    const T vp = S.V[a][ri.p], vq = S.V[a][ri.q];
-                    S.V[a][ri.p] = ri.c * vp - ri.s * vq;
-                    S.V[a][ri.q] = ri.s * vp + ri.c * vq;
+                    const int e = lane + 32 * r;
+                    if (e < NV2)
+                    {
+                        const int i = e / (M / 2), a = 2 * (e % (M / 2));
+                        const JacobiRot<T> ri = S.rot[i];
+                        const float2 c2 = make_float2(ri.c, ri.c), s2 = make_float2(ri.s, ri.s);
+                        float2* pp = reinterpret_cast<float2*>(&S.VT[ri.p][a]);
+                        float2* qq = reinterpret_cast<float2*>(&S.VT[ri.q][a]);
+                        const float2 vp = *pp, vq = *qq;
+                        *pp = __ffma2_rn(c2, vp, __fmul2_rn(make_float2(-ri.s, -ri.s), vq));
+                        *qq = __ffma2_rn(s2, vp, __fmul2_rn(c2, vq));
+                    }
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int r = 0; r < NVR; ++r)
+                {
+                    const int e = lane + 32 * r;
+                    if (e < NV)
+                    {
+                        const int a = e / H, i = e % H;
+                        const JacobiRot<T> ri = S.rot[i];
+                        const T vp = S.VT[ri.p][a], vq = S.VT[ri.q][a];
+                        S.VT[ri.p][a] = ri.c * vp - ri.s * vq;
+                        S.VT[ri.q][a] = ri.s * vp + ri.c * vq;
+                    }
                 }
             }
             __syncwarp();
@@ -282,7 +306,7 @@ __device__ void refine_subspace(JacobiSmem<M, float, TD>& S, int lane, const voi
     for (int e = lane; e < M * td; e += 32)
     {
         const int a = e / td, t = e % td;
-        S.Vf[a][t] = (a < k) ? S.V[a][top[t]] : 0.f;
+        S.Vf[a][t] = (a < k) ? S.VT[top[t]][a] : 0.f;
     }
     __syncwarp();
     ff acc[RPL][TD];
@@ -369,7 +393,7 @@ __device__ void refine_subspace(JacobiSmem<M, float, TD>& S, int lane, const voi
             float ur = 0.f;
             if (!is_top)
                 for (int a = 0; a < k; ++a)
-                    ur = fmaf(S.V[a][j], S.Rf[a][t], ur);
+                    ur = fmaf(S.VT[j][a], S.Rf[a][t], ur);
             const float gap = S.Lh[t][t] - lj;
             S.UR[j][t] = (!is_top && gap != 0.f) ? ur / gap : 0.f;
         }
@@ -386,7 +410,7 @@ __device__ void refine_subspace(JacobiSmem<M, float, TD>& S, int lane, const voi
                 float c = 0.f;
                 if (a < k)
                     for (int j = 0; j < M; ++j)
-                        c = fmaf(S.V[a][j], S.UR[j][t], c);
+                        c = fmaf(S.VT[j][a], S.UR[j][t], c);
                 const ff o = two_sum(S.Vf[a][t], c);
                 S.Oh[a][t] = o.hi;
                 S.Ol[a][t] = o.lo;
@@ -574,7 +598,7 @@ __global__ void __launch_bounds__(32) k_ltsa_fp64(const void* X, int dtype, int6
         for (int e = lane; e < k * td; e += 32)
         {
             const int a = e / td, t = e % td;
-            V[(i * k + a) * td + t] = S.V[a][top_s[td - 1 - t]];
+            V[(i * k + a) * td + t] = S.VT[top_s[td - 1 - t]][a];
         }
         __syncwarp();
     }
