@@ -179,15 +179,11 @@ int64_t knn_device(tk_ctx* ctx, const void* Xd, int dtype, int64_t N, int D, int
         throw Error(TK_ERR_UNSUPPORTED, "brute kNN supports up to 248 neighbours per point (k = " +
                                             std::to_string(k) + ")");
     // The tensor-core screen keeps its candidate lists in registers (KC <= 64);
-    // longer lists (k > 56) use the FP32 screen's shared-memory lists.
-    bool tensor = (screen == TK_SCREEN_TENSOR);
+    // longer lists (k > 56) are built in kc / 64 passes of 64 entries each.
+    const bool tensor = (screen == TK_SCREEN_TENSOR);
     if (tensor && kc > 64)
-    {
-        log(ctx, TK_LOG_INFO, "k = " + std::to_string(k) + " > 56: FP32 screen with " + std::to_string(kc) +
-                                  "-entry candidate lists");
-        tensor = false;
-        screen = TK_SCREEN_FP32;
-    }
+        log(ctx, TK_LOG_INFO, "k = " + std::to_string(k) + " > 56: tensor screen in " + std::to_string(kc / 64) +
+                                  " passes of 64 candidates");
     if (tensor && !tensor_screen_supported(((D + 63) / 64) * 64))
         throw Error(TK_ERR_UNSUPPORTED, "the tensor-core screen supports D <= 128; pass TK_SCREEN_FP32 for D = " +
                                             std::to_string(D));

@@ -297,12 +297,40 @@ __device__ __forceinline__ Item fetch_item(const ScreenWork& W, int j, int64_t N
     return it;
 }
 
-template <int DP, int KC, int QT, bool BATCH>
+// Where a launch writes its KC entries per row, for candidate lists longer than the
+// register lists (KC = 64): pass p of a multi-pass screen writes entries
+// [off, off + KC) of rows of ld entries, and keeps only candidates that come after
+// the previous passes' lists in the order (screened value, id). `lo` holds each
+// row's last screened value of pass p - 1 (before the row norm is added); pass p
+// takes t > lo, and t == lo only for ids that entries [0, off) do not hold. Every
+// candidate with t < lo is in those entries already (a list that ends at lo
+// rejected only values >= its last value at the time, which never rose), so the
+// passes together hold the ld smallest screened values of the row and the last
+// pass's last value bounds every candidate outside them. `last` (when set)
+// receives each row's last screened value of this pass for the next one.
+struct ListSlice
+{
+    int ld = 0, off = 0;          // row stride of the output lists and this pass's offset
+    const float* lo = nullptr;    // previous pass's last values (off > 0)
+    float* last = nullptr;        // this pass's last values (a later pass follows)
+};
+
+// true when the row's entries [0, off) hold id: only for candidates whose
+// screened value equals the previous pass's last value (exact float ties)
+__device__ __noinline__ bool listed_before(const int32_t* row_ids, int off, int32_t id)
+{
+    for (int s = 0; s < off; ++s)
+        if (row_ids[s] == id)
+            return true;
+    return false;
+}
+
+template <int DP, int KC, int QT, bool BATCH, bool LATER>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_screen_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
                 const __grid_constant__ CUtensorMap tm_nrm, const float* __restrict__ scale_log2, int64_t N,
                 int64_t Npad, ScreenWork work, int32_t* __restrict__ cand_idx, float* __restrict__ cand_val,
-                const float* __restrict__ nrm, unsigned* err)
+                const float* __restrict__ nrm, ListSlice slice, unsigned* err)
 {
     using C = TcCfg<DP, QT>;
     constexpr int QROWS = C::QT * TC_M;
@@ -521,6 +549,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const Item I = fetch_item<QROWS, BATCH>(work, j, N, ntiles1, scale_log2);
             const int64_t q = I.q0 + qt * TC_M + row;
             const float nq = nrm[q];
+            // pass p > 0 of a long list: only candidates after the previous passes'
+            const float lo = LATER ? slice.lo[q] : 0.f;
             // |y|^2 - 2 x.y = m2 * acc, m2 = -2^(1-2s) (exact power of two)
             const float m2 = -exp2f(1.0f - 2.0f * I.s);
             const float inv_m2 = 1.0f / m2;
@@ -598,7 +628,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                     for (int e2 = 1; e2 < 8; ++e2)
                                         x = (e == e2) ? w[e2] : x;
                                     const float t = m2 * x;
-                                    if (t < cmp && cb + e < I.n)
+                                    if (t < cmp && cb + e < I.n &&
+                                        (!LATER || t > lo ||
+                                         (t == lo &&
+                                          !listed_before(cand_idx + q * slice.ld, slice.off, (int32_t)(cb + e)))))
                                     {
                                         reg_insert<KC>(L, Ix, t, (int32_t)(cb + e));
                                         cmp = L[KC - 1];
@@ -612,12 +645,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (!alive)
                 break;
+            const int64_t o = BATCH ? q * KC : q * slice.ld + slice.off;
 #pragma unroll
             for (int s = 0; s < KC; ++s)
             {
-                cand_idx[q * KC + s] = Ix[s];
-                cand_val[q * KC + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+                cand_idx[o + s] = Ix[s];
+                cand_val[o + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
             }
+            if (!BATCH && slice.last)
+                slice.last[q] = L[KC - 1];
         }
     }
 
@@ -1385,21 +1421,25 @@ void make_map(CUtensorMap* m, const uint16_t* base, int64_t rows, int cols, int 
         throw Error(TK_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
 }
 
-template <int DP, int KC, int QT = TcCfg<DP>::QT, bool BATCH = false>
+template <int DP, int KC, int QT = TcCfg<DP>::QT, bool BATCH = false, bool LATER = false>
 void launch(tk_ctx* ctx, const uint16_t* xh, const uint16_t* xl, const uint16_t* xn, const float* nrm,
             int64_t rows, const float* scale, int64_t N, const ScreenWork& work, int grid, int32_t* cand_idx,
-            float* cand_val)
+            float* cand_val, ListSlice slice = ListSlice{})
 {
+    if (slice.ld == 0)
+        slice.ld = KC;
+    if (LATER != (slice.off > 0) || (LATER && !slice.lo))
+        throw Error(TK_ERR_INTERNAL, "tensor screen: list slice does not match the kernel");
     using C = TcCfg<DP, QT>;
     static_assert(C::SMEM <= 227 * 1024, "shared memory budget");
     CUtensorMap mh, ml, mn;
     make_map(&mh, xh, rows, DP, 64, CU_TENSOR_MAP_SWIZZLE_128B);
     make_map(&ml, xl, rows, DP, 64, CU_TENSOR_MAP_SWIZZLE_128B);
     make_map(&mn, xn, rows, 16, 16, CU_TENSOR_MAP_SWIZZLE_32B);
-    TK_CUDA(cudaFuncSetAttribute(k_screen_tc<DP, KC, QT, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TK_CUDA(cudaFuncSetAttribute(k_screen_tc<DP, KC, QT, BATCH, LATER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)C::SMEM));
-    k_screen_tc<DP, KC, QT, BATCH><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, mn, scale, N, rows, work, cand_idx,
-                                                                        cand_val, nrm, ctx->dev_err);
+    k_screen_tc<DP, KC, QT, BATCH, LATER><<<grid, TC_THREADS, C::SMEM, ctx->stream>>>(mh, ml, mn, scale, N, rows, work, cand_idx,
+                                                                        cand_val, nrm, slice, ctx->dev_err);
     TK_CHECK_LAUNCH();
 }
 
@@ -1480,6 +1520,31 @@ void launch_single(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* can
     launch<DP, KC>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single, grid, cand_idx, cand_val);
 }
 
+// Lists of kc = 128 or 256 entries: kc / 64 passes of the 64-entry screen, pass p
+// writing entries [64 p, 64 p + 64) of each row after the entries of passes < p.
+template <int DP>
+void launch_multipass(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
+{
+    const ScreenWork single{nullptr, 0, nullptr, nullptr};
+    const int grid = (int)(P.Npad / (TcCfg<DP>::QT * TC_M));
+    float* last[2] = {(float*)ctx->scratch.get("tc.last0", sizeof(float) * (size_t)P.Npad),
+                      (float*)ctx->scratch.get("tc.last1", sizeof(float) * (size_t)P.Npad)};
+    const int passes = kc / 64;
+    for (int p = 0; p < passes; ++p)
+    {
+        ListSlice sl;
+        sl.ld = kc;
+        sl.off = 64 * p;
+        sl.lo = (p > 0) ? last[(p - 1) & 1] : nullptr;
+        sl.last = (p + 1 < passes) ? last[p & 1] : nullptr;
+        if (p == 0)
+            launch<DP, 64>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single, grid, cand_idx, cand_val, sl);
+        else
+            launch<DP, 64, TcCfg<DP>::QT, false, true>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single,
+                                                       grid, cand_idx, cand_val, sl);
+    }
+}
+
 } // namespace
 
 namespace {
@@ -1523,19 +1588,25 @@ void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int k, int32_t* cand_idx, f
 {
     if (!P.xh || !P.xl || !P.xn)
         throw Error(TK_ERR_INTERNAL, "tensor screen needs the fp16 split layout");
+    if (kc != 32 && kc != 64 && kc != 128 && kc != 256)
+        throw Error(TK_ERR_INTERNAL, "tensor screen: unsupported candidate count " + std::to_string(kc));
     if (P.Dp == 64)
     {
         if (kc == 32)
             launch_wide(ctx, P, k, cand_idx, cand_val);
-        else
+        else if (kc == 64)
             launch_single<64, 64>(ctx, P, cand_idx, cand_val);
+        else
+            launch_multipass<64>(ctx, P, kc, cand_idx, cand_val);
     }
     else if (P.Dp == 128)
     {
         if (kc == 32)
             launch_single<128, 32>(ctx, P, cand_idx, cand_val);
-        else
+        else if (kc == 64)
             launch_single<128, 64>(ctx, P, cand_idx, cand_val);
+        else
+            launch_multipass<128>(ctx, P, kc, cand_idx, cand_val);
     }
     else
         throw Error(TK_ERR_UNSUPPORTED, "the tensor-core screen supports D <= 128 (padded to 64 or 128); use the "

@@ -47,7 +47,9 @@ def test_swiss_roll_2000_bit_exact(ctx, golden, screen):
 
 @pytest.mark.parametrize("screen", SCREENS)
 @pytest.mark.parametrize("n,d,k,dtype", [(3000, 64, 16, np.float32), (2500, 32, 20, np.float32),
-                                         (1800, 128, 24, np.float64), (1200, 16, 40, np.float32)])
+                                         (1800, 128, 24, np.float64), (1200, 16, 40, np.float32),
+                                         (3000, 64, 64, np.float32), (2000, 100, 100, np.float32),
+                                         (1500, 64, 130, np.float64)])
 def test_lifted_rolls_match_oracle(ctx, screen, n, d, k, dtype):
     X = datasets.lifted_swiss_roll(n, d, seed=n + d, dtype=dtype)
     idx = ctx.knn_brute(X, k, screen=screen)
@@ -92,6 +94,11 @@ def _copies4(dtype):
     return np.ascontiguousarray(np.repeat(base, 4, axis=0), dtype=dtype)
 
 
+def _copies(n_base, copies, dim, seed, dtype):
+    base = np.random.default_rng(seed).normal(size=(n_base, dim))
+    return np.ascontiguousarray(np.repeat(base, copies, axis=0), dtype=dtype)
+
+
 TIE_CASES = [
     # the nearest other point's 4 copies straddle ranks k - 1, k and k + 1: equal
     # FP32 distances past rank k must be refined with the others
@@ -104,6 +111,11 @@ TIE_CASES = [
     ("2-D integer grid 40x40, k=10", lambda dt: _lattice((40, 40), dt), 10),
     ("2-D integer grid 40x40, k=6", lambda dt: _lattice((40, 40), dt), 6),
     ("3-D integer grid 12^3, k=12", lambda dt: _lattice((12, 12, 12), dt), 12),
+    # lists longer than 64 are screened in passes of 64: equal screened values
+    # straddle the passes (2 passes at k=70, 4 at k=150)
+    ("100 copies of 3 points, k=70", lambda dt: _copies(3, 100, 6, 5, dt), 70),
+    ("150 copies of 3 points, k=150", lambda dt: _copies(3, 150, 6, 6, dt), 150),
+    ("3-D integer grid 12^3, k=80", lambda dt: _lattice((12, 12, 12), dt), 80),
 ]
 
 
