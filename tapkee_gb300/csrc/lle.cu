@@ -164,6 +164,97 @@ __device__ __forceinline__ float reg_chol_solve(const float (&L)[KP], const floa
     return y;
 }
 
+// The same for KP = 64 with two rows per lane: lane a holds rows a (A0) and
+// a + 32 (A1), entries c <= row; rows of column j travel by shuffles from the
+// lane j & 31. ivd receives 1 / L_jj (written by the lane that holds row j).
+__device__ __forceinline__ void reg_cholesky64(float (&A0)[64], float (&A1)[64], float* ivd, int lane)
+{
+#pragma unroll
+    for (int j = 0; j < 64; ++j)
+    {
+        const float djj = __shfl_sync(0xffffffffu, (j < 32) ? A0[j] : A1[j], j & 31);
+        const float inv = rsqrtf(fmaxf(djj, FLT_MIN));
+        if (lane == (j & 31))
+            ivd[j] = inv;
+        if (j < 32)
+        {
+            if (lane >= j)
+                A0[j] *= inv;
+            A1[j] *= inv;
+        }
+        else if (lane + 32 >= j)
+            A1[j] *= inv;
+#pragma unroll
+        for (int c = 0; c < 64; ++c)
+        {
+            if (c > j)
+            {
+                const float lcj = __shfl_sync(0xffffffffu, (c < 32) ? A0[j] : A1[j], c & 31);
+                if (c < 32)
+                {
+                    if (lane >= c)
+                        A0[c] = fmaf(-A0[j], lcj, A0[c]);
+                    A1[c] = fmaf(-A1[j], lcj, A1[c]);
+                }
+                else if (lane + 32 >= c)
+                    A1[c] = fmaf(-A1[j], lcj, A1[c]);
+            }
+        }
+    }
+}
+
+// Solves L L^T x = r for KP = 64 with the factor of reg_cholesky64 stored in Ls
+// (row-major, stride 65) and ivd = 1 / L_jj; lane a holds r_a, r_{a+32} in y0, y1
+// and gets x there. The factor's loads do not depend on the sweep, so they are
+// issued ahead of the shuffle chain.
+__device__ __forceinline__ void reg_chol_solve64(const float* Ls, const float* ivd, float& y0, float& y1, int lane)
+{
+#pragma unroll
+    for (int j = 0; j < 64; ++j)
+    {
+        const float yj = __shfl_sync(0xffffffffu, (j < 32) ? y0 : y1, j & 31) * ivd[j];
+        const float a0 = (lane > j) ? Ls[lane * 65 + j] : 0.f;
+        const float a1 = (lane + 32 > j) ? Ls[(lane + 32) * 65 + j] : 0.f;
+        if (j < 32)
+        {
+            if (lane == j)
+                y0 = yj;
+            else if (lane > j)
+                y0 = fmaf(-a0, yj, y0);
+            y1 = fmaf(-a1, yj, y1);
+        }
+        else
+        {
+            if (lane + 32 == j)
+                y1 = yj;
+            else if (lane + 32 > j)
+                y1 = fmaf(-a1, yj, y1);
+        }
+    }
+#pragma unroll
+    for (int j = 63; j >= 0; --j)
+    {
+        const float xj = __shfl_sync(0xffffffffu, (j < 32) ? y0 : y1, j & 31) * ivd[j];
+        const float l0 = (lane < j) ? Ls[j * 65 + lane] : 0.f;
+        const float l1 = (lane + 32 < j) ? Ls[j * 65 + lane + 32] : 0.f;
+        if (j < 32)
+        {
+            if (lane == j)
+                y0 = xj;
+            else if (lane < j)
+                y0 = fmaf(-l0, xj, y0);
+        }
+        else
+        {
+            if (lane + 32 == j)
+                y1 = xj;
+            else if (lane + 32 < j)
+                y1 = fmaf(-l1, xj, y1);
+            y0 = fmaf(-l0, xj, y0);
+        }
+    }
+}
+
 __device__ __forceinline__ float ld_f(const void* X, int dtype, int64_t off)
 {
     return dtype == TK_F64 ? (float)reinterpret_cast<const double*>(X)[off] : reinterpret_cast<const float*>(X)[off];
@@ -287,19 +378,20 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         for (int d0 = 0; d0 < D; d0 += 32)
         {
             const int d = d0 + lane;
-            if (KP <= 32 && dtype == TK_F32)
+            if (KP <= 64 && dtype == TK_F32)
             {
                 // every neighbour value of the chunk in flight at once
+                constexpr int KV = (KP <= 64) ? KP : 1;
                 const float xi = (d < D) ? ld_f(X, dtype, i * ldx + d) : 0.f;
-                float v[KP <= 32 ? KP : 1];
+                float v[KV];
 #pragma unroll
-                for (int a = 0; a < (KP <= 32 ? KP : 1); ++a)
+                for (int a = 0; a < KV; ++a)
                 {
-                    const int nba = __shfl_sync(0xffffffffu, nb[0], a & 31);
+                    const int nba = __shfl_sync(0xffffffffu, nb[(a >> 5) < NPL ? (a >> 5) : 0], a & 31);
                     v[a] = (a < k && d < D) ? ld_f(X, dtype, (int64_t)nba * ldx + d) : xi;
                 }
 #pragma unroll
-                for (int a = 0; a < (KP <= 32 ? KP : 1); ++a)
+                for (int a = 0; a < KV; ++a)
                     S.Zh[a][lane] = v[a] - xi;
             }
             else
@@ -417,7 +509,35 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         // ---- FP32 Cholesky (lower) ----
         float Lr[KP <= 32 ? KP : 1];
         float invd = 1.f;
-        if constexpr (KP <= 32)
+        constexpr int K64 = (KP == 64) ? 64 : 1;
+        if constexpr (KP == 64)
+        {
+            float A0[64], A1[64];
+#pragma unroll
+            for (int c = 0; c < 64; ++c)
+            {
+                A0[c] = (c <= lane) ? S.C[lane][c] : 0.f;
+                A1[c] = (c <= lane + 32) ? S.C[lane + 32][c] : 0.f;
+            }
+            reg_cholesky64(A0, A1, S.ivd, lane);
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < 64; ++c)
+            {
+                if (c <= lane)
+                    S.C[lane][c] = A0[c];
+                if (c <= lane + 32)
+                    S.C[lane + 32][c] = A1[c];
+            }
+            __syncwarp();
+            float y0 = S.r[lane], y1 = S.r[lane + 32];
+            reg_chol_solve64(&S.C[0][0], S.ivd, y0, y1, lane);
+            __syncwarp();
+            S.w[lane] = (lane < k) ? y0 : 0.f;
+            S.w[lane + 32] = (lane + 32 < k) ? y1 : 0.f;
+            __syncwarp();
+        }
+        else if constexpr (KP <= 32)
         {
 #pragma unroll
             for (int c = 0; c < KP; ++c)
@@ -564,20 +684,47 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
                 for (int d0 = 0; d0 < D; d0 += 32)
                 {
                     const int d = d0 + lane;
-                    for (int a = 0; a < KP; ++a)
+                    if (KP == 64 && dtype == TK_F32)
                     {
-                        const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
-                        ff z = ff_zero();
-                        if (a < k && d < D)
-                            z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
-                        S.Zh[a][lane] = z.hi;
-                        S.Zl[a][lane] = z.lo;
+                        // every neighbour value of the chunk in flight at once
+                        const float xi = (d < D) ? ld_f(X, dtype, i * ldx + d) : 0.f;
+                        float xv[K64];
+#pragma unroll
+                        for (int a = 0; a < K64; ++a)
+                        {
+                            const int nba = __shfl_sync(0xffffffffu, nb[(a >> 5) < NPL ? (a >> 5) : 0], a & 31);
+                            xv[a] = (a < k && d < D) ? ld_f(X, dtype, (int64_t)nba * ldx + d) : xi;
+                        }
+#pragma unroll
+                        for (int a = 0; a < K64; ++a)
+                        {
+                            const ff z = two_sum(xv[a], -xi);
+                            S.Zh[a][lane] = z.hi;
+                            S.Zl[a][lane] = z.lo;
+                        }
+                    }
+                    else
+                    {
+                        for (int a = 0; a < KP; ++a)
+                        {
+                            const int nba =
+                                __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
+                            ff z = ff_zero();
+                            if (a < k && d < D)
+                                z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
+                            S.Zh[a][lane] = z.hi;
+                            S.Zl[a][lane] = z.lo;
+                        }
                     }
                     __syncwarp();
-                    // v_d = sum_b w_b z_bd for d = d0 + lane
-                    ff v = ff_zero();
-                    for (int b = 0; b < k; ++b)
-                        v = ff_fma(v, S.w[b], 0.f, S.Zh[b][lane], S.Zl[b][lane]);
+                    // v_d = sum_b w_b z_bd for d = d0 + lane, in four independent chains
+                    ff vq[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
+                    for (int b = 0; b < k; b += 4)
+#pragma unroll
+                        for (int t = 0; t < 4; ++t)
+                            if (b + t < k)
+                                vq[t] = ff_fma(vq[t], S.w[b + t], 0.f, S.Zh[b + t][lane], S.Zl[b + t][lane]);
+                    const ff v = ff_add(ff_add(vq[0], vq[1]), ff_add(vq[2], vq[3]));
                     S.vh[lane] = v.hi;
                     S.vl[lane] = v.lo;
                     __syncwarp();
@@ -615,7 +762,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
                 }
                 __syncwarp();
             }
-            if constexpr (KP <= 32)
+            if constexpr (KP == 64)
+            {
+                float y0 = S.r[lane], y1 = S.r[lane + 32];
+                reg_chol_solve64(&S.C[0][0], S.ivd, y0, y1, lane);
+                __syncwarp();
+                if (lane < k)
+                    S.w[lane] += y0;
+                if (lane + 32 < k)
+                    S.w[lane + 32] += y1;
+            }
+            else if constexpr (KP <= 32)
             {
                 const float x = reg_chol_solve<KP>(Lr, &S.C[0][0], S.ivd, lane < KP ? S.r[lane] : 0.f, lane);
                 __syncwarp();
@@ -689,7 +846,7 @@ void dispatch(tk_ctx* ctx, const LleRows& RW, const int32_t* idx, int k, double 
     else if (k <= 32)
         launch<32, 8, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
     else if (k <= 64)
-        launch<64, 4, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
+        launch<64, 6, BATCH>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
     else if (!BATCH && k <= 128)
         launch<128, 1, false>(ctx, RW, idx, k, klle_shift, rhs, nm, W);
     else

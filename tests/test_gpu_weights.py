@@ -24,9 +24,13 @@ def test_lle_weights_k_greater_than_d(ctx, golden):
     assert np.allclose(W.sum(1), 1.0, atol=1e-12)
 
 
-@pytest.mark.parametrize("n,d,k", [(4000, 64, 16), (3000, 128, 24), (2000, 32, 20), (1500, 16, 32), (800, 8, 48)])
-def test_lle_weights_lifted(ctx, n, d, k):
-    X = datasets.lifted_swiss_roll(n, d, seed=n)
+@pytest.mark.parametrize("n,d,k,dtype", [(4000, 64, 16, np.float32), (3000, 128, 24, np.float32),
+                                         (2000, 32, 20, np.float32), (1500, 16, 32, np.float32),
+                                         (800, 8, 48, np.float32), (3000, 64, 64, np.float32),
+                                         (2000, 128, 40, np.float32), (1500, 16, 60, np.float32),
+                                         (1200, 32, 50, np.float64), (900, 100, 33, np.float32)])
+def test_lle_weights_lifted(ctx, n, d, k, dtype):
+    X = datasets.lifted_swiss_roll(n, d, seed=n, dtype=dtype)
     idx, _, _ = oracle.knn_brute(X, k)
     W = ctx.lle_weights(X, idx, 1e-3)
     ref = oracle.lle_weights(X, idx, 1e-3)
