@@ -38,6 +38,10 @@ namespace {
 constexpr int TC_N = 128;      // candidates per stage (MMA N)
 constexpr int TC_M = 128;      // queries per A tile (MMA M)
 constexpr int TC_THREADS = 320;
+// Entries per pass of the long-list screen: with 32 columns per TMEM load, a
+// 48-entry list (values and ids) fits the 168 registers a thread of a 10-warp CTA
+// gets; a 64-entry list spills in the epilogue's loop.
+constexpr int TC_PASS = 48;
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per single wait
 
 // QT query blocks of 128 rows share each candidate tile (QT = 2 only for DP = 64:
@@ -308,12 +312,55 @@ __device__ __forceinline__ Item fetch_item(const ScreenWork& W, int j, int64_t N
 // passes together hold the ld smallest screened values of the row and the last
 // pass's last value bounds every candidate outside them. `last` (when set)
 // receives each row's last screened value of this pass for the next one.
+// Lists may also start full of each row's bound B = 1.01 T_r + 2 eps instead of
+// empty (seed_tr = T_r, the row's k-th distance over the other rows of its
+// 128-row block; rmax[0] = R; c1, c2 the screen's error model), as in the wide
+// kernel: only candidates screened below B are inserted, and a list with fewer
+// real entries ends in entries (B, -1). A later pass whose rows all ended the
+// previous pass below their list length (last value B) has nothing to add: the
+// CTA writes (B, -1) lists without screening.
 struct ListSlice
 {
     int ld = 0, off = 0;          // row stride of the output lists and this pass's offset
+    // entries written, [off, off + nw): a pass followed by another writes its KC;
+    // the last pass writes to the row's end, the first min(KC, nw) of its list
+    // (a sorted list cut short still bounds everything outside it by its last
+    // kept value) and, past KC, entries (its last value, -1)
+    int nw = 0;
     const float* lo = nullptr;    // previous pass's last values (off > 0)
     float* last = nullptr;        // this pass's last values (a later pass follows)
+    const float* seed_tr = nullptr;
+    const float* rmax = nullptr;
+    float c1 = 0.f, c2 = 0.f;
+    // near and far tiles (k_classify over 128-row blocks; null: every tile near):
+    // far tiles get only the high-part product, and far_val (when set) receives
+    // each row's smallest screened value over far tiles
+    const uint32_t* near_bits = nullptr;
+    int nwords = 0;
+    float* far_val = nullptr;
 };
+
+__device__ __forceinline__ bool tile_is_near(const ListSlice& sl, int64_t blk, int tile)
+{
+    return !sl.near_bits || ((__ldg(sl.near_bits + blk * sl.nwords + (tile >> 5)) >> (tile & 31)) & 1u) != 0u;
+}
+
+// The row's starting list value in screened units t = |y|^2 - 2 x.y (FLT_MAX:
+// no bound). T_r is an FP32 direct-difference sum over centred coordinates: its
+// relative rounding (D + 2) 2^-24 is far inside the 1 %, and the centring error
+// of a squared distance, at most 2^-22 d R, inside one eps. A neighbour among the
+// k nearest screens at most e_k + eps < B, and so does the row itself.
+__device__ __forceinline__ float seed_bound(const ListSlice& sl, int64_t q, float nq)
+{
+    if (!sl.seed_tr)
+        return FLT_MAX;
+    const float tb = sl.seed_tr[q];
+    if (!(nq < FLT_MAX && tb < FLT_MAX))
+        return FLT_MAX;
+    const float R = sl.rmax[0];
+    const float eps = sl.c1 * (nq + R * R) + sl.c2 * sqrtf(nq) * R;
+    return fmaf(1.01f, tb, 2.f * eps) - nq;
+}
 
 // true when the row's entries [0, off) hold id: only for candidates whose
 // screened value equals the previous pass's last value (exact float ties)
@@ -385,11 +432,40 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     tc_fence_before();
-    __syncthreads();
+    // a later pass screens only when one of its rows filled the previous pass's
+    // list below the row's bound
+    int need = 1;
+    if constexpr (LATER)
+    {
+        need = 0;
+        if (warp < C::EPI_WARPS)
+        {
+            const int64_t q = (int64_t)j_first * QROWS + (warp >> 2) * TC_M + (warp & 3) * 32 + lane;
+            need = slice.lo[q] < seed_bound(slice, q, nrm[q]) ? 1 : 0;
+        }
+    }
+    const bool screen = __syncthreads_or(need) != 0;
     tc_fence_after();
     const uint32_t tmem = Bar.tmem_base;
 
-    if (warp == 8)
+    if (!screen)
+    {
+        if (warp < C::EPI_WARPS)
+        {
+            const int64_t q = (int64_t)j_first * QROWS + (warp >> 2) * TC_M + (warp & 3) * 32 + lane;
+            const float nq = nrm[q];
+            const float b = seed_bound(slice, q, nq);
+            const int64_t o = q * slice.ld + slice.off;
+            for (int s = 0; s < slice.nw; ++s)
+            {
+                cand_idx[o + s] = -1;
+                cand_val[o + s] = (b < FLT_MAX) ? b + nq : FLT_MAX;
+            }
+            if (slice.last)
+                slice.last[q] = b;
+        }
+    }
+    else if (warp == 8)
     {
         // ------------------------------------------------------------ producer
         if (lane == 0)
@@ -479,8 +555,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 ++na;
                 tc_fence_after();
+                ZigZag zz((int)(I.q0 / TC_N) - I.t0, I.ntiles);
                 for (int it = 0; it < I.ntiles; ++it)
                 {
+                    const int tile = zz.next();  // local to the problem
                     const int slot = gi % C::STAGES;
                     const uint32_t ph = (uint32_t)(gi / C::STAGES) & 1u;
                     const int buf = gi & 1;
@@ -505,9 +583,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS + qt * TC_N);
                         // norm step first: D = 2^13 (h + l) of -|2^s y|^2 / 2^14
                         umma_f16(d, axd, bx0 + soff, 0u);
+                        // far tiles: the high-part product only
+                        const int nprod = (BATCH || tile_is_near(slice, I.q0 / TC_M + qt, tile)) ? 3 : 1;
 #pragma unroll
                         for (int prod = 0; prod < 3; ++prod)
                         {
+                            if (prod >= nprod)
+                                break;
                             const int apart = (prod == 2) ? 1 : 0;  // l_x . h_y
                             const int bpart = (prod == 1) ? 1 : 0;  // h_x . l_y
 #pragma unroll
@@ -554,20 +636,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // |y|^2 - 2 x.y = m2 * acc, m2 = -2^(1-2s) (exact power of two)
             const float m2 = -exp2f(1.0f - 2.0f * I.s);
             const float inv_m2 = 1.0f / m2;
+            float cmp = BATCH ? FLT_MAX : seed_bound(slice, q, nq);
             float L[KC];
             int32_t Ix[KC];
 #pragma unroll
             for (int s = 0; s < KC; ++s)
             {
-                L[s] = FLT_MAX;
+                L[s] = cmp;
                 Ix[s] = -1;
             }
-            float cmp = FLT_MAX;
-            float thr = -__int_as_float(0x7f800000);  // accept everything until the list fills
+            // without a bound: accept everything until the list fills
+            float thr = (cmp < FLT_MAX) ? cmp * inv_m2 : -__int_as_float(0x7f800000);
+            float far_max = -__int_as_float(0x7f800000);  // largest accumulator over far tiles
+            const int64_t blk = I.q0 / TC_M + qt;
             ZigZag zz((int)(I.q0 / TC_N) - I.t0, I.ntiles);
             for (int it = 0; it < I.ntiles; ++it)
             {
                 const int tile = zz.next();  // local to the problem
+                const bool far_tile = !BATCH && !tile_is_near(slice, blk, tile);
                 const int buf = gi & 1;
                 const uint32_t bph = (uint32_t)(gi >> 1) & 1u;
                 ++gi;
@@ -602,6 +688,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         __syncwarp();
                         if (lane == 0)
                             mbar_arrive(smem_u32(&Bar.tempty[buf][qt]));
+                    }
+                    if (far_tile)
+                    {
+                        // padding columns must not enter far_max
+                        const int64_t cf = c0 + h * CPW;
+                        if (cf + CPW <= I.n)
+                            far_max = fmaxf(far_max, gall);
+                        else
+                        {
+#pragma unroll
+                            for (int e = 0; e < CPW; ++e)
+                                if (cf + e < I.n)
+                                    far_max = fmaxf(far_max, v[e]);
+                        }
                     }
                     constexpr int NG = CPW / 8;
                     if (gall > thr)
@@ -646,14 +746,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (!alive)
                 break;
             const int64_t o = BATCH ? q * KC : q * slice.ld + slice.off;
+            const int nw = BATCH ? KC : slice.nw;
 #pragma unroll
             for (int s = 0; s < KC; ++s)
+                if (s < nw)
+                {
+                    cand_idx[o + s] = Ix[s];
+                    cand_val[o + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+                }
+            for (int s = KC; s < nw; ++s)
             {
-                cand_idx[o + s] = Ix[s];
-                cand_val[o + s] = (L[s] < FLT_MAX) ? L[s] + nq : FLT_MAX;
+                cand_idx[o + s] = -1;
+                cand_val[o + s] = (L[KC - 1] < FLT_MAX) ? L[KC - 1] + nq : FLT_MAX;
             }
             if (!BATCH && slice.last)
                 slice.last[q] = L[KC - 1];
+            // smallest screened value over far tiles (high-part products only)
+            if (!BATCH && slice.far_val)
+                slice.far_val[q] = (far_max > -FLT_MAX) ? m2 * far_max + nq : FLT_MAX;
         }
     }
 
@@ -1271,7 +1381,7 @@ __global__ void k_merge_parts(int64_t row0, int64_t rows, int parts, const int32
 // the KB smallest distances stay sorted in registers (KB >= k), kept by a
 // min/max network.
 template <int DP, int KB>
-__global__ void __launch_bounds__(128, 4) k_blockmate(const float* __restrict__ xc, int64_t N, int k, float* Tb,
+__global__ void __launch_bounds__(128, (KB > 32) ? 2 : 4) k_blockmate(const float* __restrict__ xc, int64_t N, int k, float* Tb,
                                                       float* Tr)
 {
     __shared__ __align__(16) float xs[128][DP];
@@ -1428,6 +1538,10 @@ void launch(tk_ctx* ctx, const uint16_t* xh, const uint16_t* xl, const uint16_t*
 {
     if (slice.ld == 0)
         slice.ld = KC;
+    if (slice.nw == 0)
+        slice.nw = KC;
+    if (slice.off + slice.nw > slice.ld)
+        throw Error(TK_ERR_INTERNAL, "tensor screen: list slice past the row's end");
     if (LATER != (slice.off > 0) || (LATER && !slice.lo))
         throw Error(TK_ERR_INTERNAL, "tensor screen: list slice does not match the kernel");
     using C = TcCfg<DP, QT>;
@@ -1512,37 +1626,101 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     }
 }
 
+// The bound that seeds the 64-entry lists (padded dimension 64, k <= 64): each
+// row's k-th distance over its 128-row block (k_blockmate). Without it (other
+// dimensions, larger k) the lists start empty.
+// The same bound classifies the candidate tiles (128 rows, the same blocks as the
+// query blocks, so one set of spheres serves both) into near and far, as for the
+// wide kernel; far_val goes to P for the re-rank's certification.
+ListSlice seeded_slice(tk_ctx* ctx, Prepared& P, int k)
+{
+    ListSlice sl;
+    if (P.Dp != 64 || k > 64 || k < 1)
+        return sl;
+    cudaStream_t st = ctx->stream;
+    const int nq = (int)(P.Npad / TC_M);
+    const int nwords = (nq + 31) / 32;
+    float* Tb = (float*)ctx->scratch.get("tc.tb", sizeof(float) * (size_t)nq);
+    float* Trow = (float*)ctx->scratch.get("tc.trow", sizeof(float) * (size_t)P.Npad);
+    float* bc = (float*)ctx->scratch.get("tc.bc", sizeof(float) * (size_t)nq * P.Dp);
+    float* bcT = (float*)ctx->scratch.get("tc.bcT", sizeof(float) * (size_t)nq * P.Dp);
+    float* br = (float*)ctx->scratch.get("tc.br", sizeof(float) * (size_t)nq);
+    uint32_t* bits = (uint32_t*)ctx->scratch.get("tc.bits", sizeof(uint32_t) * (size_t)nq * nwords);
+    P.far_val = (float*)ctx->scratch.get("tc.far", sizeof(float) * (size_t)P.Npad);
+    float c2f;
+    screen_error_model(TK_SCREEN_TENSOR, P.Dp, &sl.c1, &sl.c2);
+    screen_error_model_far(P.Dp, &c2f);
+    P.c2_far = c2f;
+    k_blockmate<64, 64><<<nq, 128, 0, st>>>(P.xc, P.N, k, Tb, Trow);
+    TK_CHECK_LAUNCH();
+    k_spheres<TC_M><<<nq, 256, 0, st>>>(P.xc, P.N, P.Dp, bc, br, bcT);
+    TK_CHECK_LAUNCH();
+    k_classify<<<nq, 256, 0, st>>>(bc, br, bcT, br, Tb, nq, nwords, P.Dp, P.rmax, sl.c1, c2f, bits);
+    TK_CHECK_LAUNCH();
+    sl.seed_tr = Trow;
+    sl.rmax = P.rmax;
+    sl.near_bits = bits;
+    sl.nwords = nwords;
+    sl.far_val = P.far_val;
+    return sl;
+}
+
 template <int DP, int KC>
-void launch_single(tk_ctx* ctx, const Prepared& P, int32_t* cand_idx, float* cand_val)
+void launch_single(tk_ctx* ctx, Prepared& P, int32_t* cand_idx, float* cand_val)
 {
     const ScreenWork single{nullptr, 0, nullptr, nullptr};
     const int grid = (int)(P.Npad / (TcCfg<DP>::QT * TC_M));
     launch<DP, KC>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single, grid, cand_idx, cand_val);
 }
 
-// Lists of kc = 128 or 256 entries: kc / 64 passes of the 64-entry screen, pass p
-// writing entries [64 p, 64 p + 64) of each row after the entries of passes < p.
-template <int DP>
-void launch_multipass(tk_ctx* ctx, const Prepared& P, int kc, int32_t* cand_idx, float* cand_val)
+// Passes of PASS entries that fill rows of kc entries with at least k + 8.
+constexpr int pass_count(int k, int kc, int pass)
+{
+    return ((k + 8 + pass - 1) / pass) < ((kc + pass - 1) / pass) ? (k + 8 + pass - 1) / pass : (kc + pass - 1) / pass;
+}
+
+// Lists of kc = 64, 128 or 256 entries per row: passes of the PASS-entry screen
+// until the row holds k + 8 entries, pass p writing entries [PASS p, ...) after
+// the entries of passes < p; the last pass writes to the row's end.
+template <int DP, int PASS>
+void launch_passes(tk_ctx* ctx, Prepared& P, int k, int kc, const ListSlice& seed, int32_t* cand_idx,
+                   float* cand_val)
 {
     const ScreenWork single{nullptr, 0, nullptr, nullptr};
     const int grid = (int)(P.Npad / (TcCfg<DP>::QT * TC_M));
     float* last[2] = {(float*)ctx->scratch.get("tc.last0", sizeof(float) * (size_t)P.Npad),
                       (float*)ctx->scratch.get("tc.last1", sizeof(float) * (size_t)P.Npad)};
-    const int passes = kc / 64;
+    const int passes = pass_count(k, kc, PASS);
     for (int p = 0; p < passes; ++p)
     {
-        ListSlice sl;
+        ListSlice sl = seed;
         sl.ld = kc;
-        sl.off = 64 * p;
+        sl.off = PASS * p;
+        sl.nw = (p + 1 < passes) ? PASS : kc - sl.off;
         sl.lo = (p > 0) ? last[(p - 1) & 1] : nullptr;
         sl.last = (p + 1 < passes) ? last[p & 1] : nullptr;
+        if (p > 0)
+            sl.far_val = nullptr;  // every pass screens the same far values
         if (p == 0)
-            launch<DP, 64>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single, grid, cand_idx, cand_val, sl);
+            launch<DP, PASS>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single, grid, cand_idx, cand_val,
+                             sl);
         else
-            launch<DP, 64, TcCfg<DP>::QT, false, true>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N, single,
-                                                       grid, cand_idx, cand_val, sl);
+            launch<DP, PASS, TcCfg<DP>::QT, false, true>(ctx, P.xh, P.xl, P.xn, P.nrm, P.Npad, P.rmax + 1, P.N,
+                                                         single, grid, cand_idx, cand_val, sl);
     }
+}
+
+// 48-entry passes do not spill; a 64-entry pass spills some registers in the
+// epilogue and took about 1.3 times as long at N = 200000 (13 ms against 10 ms),
+// so 64-entry passes are taken where they need fewer than 3/4 as many passes.
+template <int DP>
+void launch_long(tk_ctx* ctx, Prepared& P, int k, int kc, int32_t* cand_idx, float* cand_val)
+{
+    const ListSlice seed = seeded_slice(ctx, P, k);
+    if (4 * pass_count(k, kc, 64) < 3 * pass_count(k, kc, TC_PASS))
+        launch_passes<DP, 64>(ctx, P, k, kc, seed, cand_idx, cand_val);
+    else
+        launch_passes<DP, TC_PASS>(ctx, P, k, kc, seed, cand_idx, cand_val);
 }
 
 } // namespace
@@ -1594,19 +1772,15 @@ void screen_tensor(tk_ctx* ctx, Prepared& P, int kc, int k, int32_t* cand_idx, f
     {
         if (kc == 32)
             launch_wide(ctx, P, k, cand_idx, cand_val);
-        else if (kc == 64)
-            launch_single<64, 64>(ctx, P, cand_idx, cand_val);
         else
-            launch_multipass<64>(ctx, P, kc, cand_idx, cand_val);
+            launch_long<64>(ctx, P, k, kc, cand_idx, cand_val);
     }
     else if (P.Dp == 128)
     {
         if (kc == 32)
             launch_single<128, 32>(ctx, P, cand_idx, cand_val);
-        else if (kc == 64)
-            launch_single<128, 64>(ctx, P, cand_idx, cand_val);
         else
-            launch_multipass<128>(ctx, P, kc, cand_idx, cand_val);
+            launch_long<128>(ctx, P, k, kc, cand_idx, cand_val);
     }
     else
         throw Error(TK_ERR_UNSUPPORTED, "the tensor-core screen supports D <= 128 (padded to 64 or 128); use the "
