@@ -43,10 +43,14 @@ constexpr int HC = 256;         // hash slots of the big kernel's first attempt
 constexpr int HC_BIG = 8192;    // hash slots for rows that overflow the fused pass
 constexpr int ROW_WARPS = 8;
 constexpr int STAGE = 256;      // staged (column, value) contributions per warp
-// fused pass: (hash slots, row scratch entries) -- rows of LLE with k <= 24
-// hold ~3.5 k distinct columns; LTSA and larger k take the wider table
+// fused pass: (hash slots, row scratch entries, staged contributions) -- rows of
+// LLE with k <= 24 hold ~3.5 k distinct columns; LTSA and larger k take the
+// wider table; k > 40 the widest (LLE at k = 64: 234 distinct columns per row
+// on average, many above 256, which the 256-entry scratch sent to the one-warp
+// large-table kernel)
 constexpr int HC_S = 256, RCAP_S = 128;
 constexpr int HC_L = 512, RCAP_L = 256;
+constexpr int HC_X = 512, RCAP_X = 512, STAGE_X = 512;
 
 __global__ void k_indeg(const int32_t* __restrict__ idx, int64_t nk, int64_t N, int k, int* cnt, unsigned* repeats,
                         unsigned* err)
@@ -464,20 +468,20 @@ __device__ void table_emit(RowTable<CAP>& T, int lane, int64_t base, int32_t* co
 // ---------------------------------------------------------------------------
 // Fused row pass: one warp per row, contributions staged per round of sources.
 
-template <int HCT>
+template <int HCT, int ST = STAGE>
 struct FusedSmem
 {
     int keys[HCT];
     double vals[HCT];
-    int scol[STAGE];
-    double sval[STAGE];  // reused for the 64-bit sort keys of the emission (at most STAGE)
+    int scol[ST];
+    double sval[ST];  // reused for the 64-bit sort keys of the emission (at most ST)
 };
 
 // Bitonic sort of 32 * NK 64-bit keys held NK per lane (element i = e * 32 + lane).
 template <int NK>
 __device__ __forceinline__ void warp_bitonic(unsigned long long (&key)[NK], int lane)
 {
-    constexpr int LOGP = 5 + (NK == 8 ? 3 : (NK == 4 ? 2 : (NK == 2 ? 1 : 0)));
+    constexpr int LOGP = 5 + (NK == 16 ? 4 : (NK == 8 ? 3 : (NK == 4 ? 2 : (NK == 2 ? 1 : 0))));
 #pragma unroll
     for (int ls = 1; ls <= LOGP; ++ls)
     {
@@ -548,8 +552,8 @@ __device__ __forceinline__ void emit_sorted(Smem& F, int lane, int n, int32_t* o
 // Row j in one pass: table of (column, sum) in the serial triplet order, then
 // sorted into the row scratch (scol_out/sval_out, RCAP entries per row). Rows
 // that do not fit are listed for the large-table kernel.
-template <int HCT, int RCAP>
-__global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
+template <int HCT, int RCAP, int ST = STAGE>
+__global__ void __launch_bounds__(ROW_WARPS * 32, (ST > STAGE ? 2 : (HCT == 256 ? 4 : 3)))
     k_rows_fused(int method, int64_t N, int k, int td, const int32_t* __restrict__ idx,
                  const double* __restrict__ wts, double shift, const int64_t* __restrict__ rptr,
                  const int32_t* __restrict__ rev, int* row_nnz, int32_t* scol_out, double* sval_out,
@@ -557,10 +561,10 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    FusedSmem<HCT>& F = reinterpret_cast<FusedSmem<HCT>*>(smem_raw)[wib];
-    static_assert(RCAP <= STAGE && HCT <= 1024, "sort keys live in sval; slot ids take 10 bits");
+    FusedSmem<HCT, ST>& F = reinterpret_cast<FusedSmem<HCT, ST>*>(smem_raw)[wib];
+    static_assert(RCAP <= ST && HCT <= 1024, "sort keys live in sval; slot ids take 10 bits");
     const int KS = k + 1;          // contributions per source
-    const int S = STAGE / KS;      // sources per round (0 when k >= STAGE: every row takes the large table)
+    const int S = ST / KS;         // sources per round (0 when k >= ST: every row takes the large table)
     const int64_t nw = (int64_t)gridDim.x * ROW_WARPS;
     const bool lle = method == TK_METHOD_KLLE;
     const bool hlle = method == TK_METHOD_HLLE;
@@ -737,8 +741,10 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, (HCT == 256 ? 4 : 3))
             emit_sorted<2>(F, lane, n, oc, ov);
         else if (RCAP <= 128 || n <= 128)
             emit_sorted<4>(F, lane, n, oc, ov);
-        else
+        else if (RCAP <= 256 || n <= 256)
             emit_sorted<8>(F, lane, n, oc, ov);
+        else
+            emit_sorted<(RCAP > 256 ? 16 : 8)>(F, lane, n, oc, ov);
         if (lane == 0)
             row_nnz[j] = n;
         __syncwarp();
@@ -818,8 +824,9 @@ struct AsmState
     int rcap;
 };
 
-// the wide fused-pass table for LTSA and for LLE with k > 24
+// the wide fused-pass table for LTSA and for LLE with k > 24; the widest for k > 40
 bool wide_rows(int method, int k) { return method != TK_METHOD_KLLE || k > 24; }
+bool widest_rows(int k) { return k > 40; }
 
 AsmState asm_state(tk_ctx* ctx, int method, int64_t N, int k)
 {
@@ -831,7 +838,7 @@ AsmState asm_state(tk_ctx* ctx, int method, int64_t N, int k)
     a.big = (int32_t*)ctx->scratch.get("asm.big", sizeof(int32_t) * (size_t)N);
     a.nbig = (unsigned*)ctx->scratch.get("asm.nbig", 16);
     a.row_big = (unsigned char*)ctx->scratch.get("asm.rowbig", (size_t)N);
-    a.rcap = wide_rows(method, k) ? RCAP_L : RCAP_S;
+    a.rcap = widest_rows(k) ? RCAP_X : (wide_rows(method, k) ? RCAP_L : RCAP_S);
     a.scol = (int32_t*)ctx->scratch.get("asm.scol", sizeof(int32_t) * (size_t)N * a.rcap);
     a.sval = (double*)ctx->scratch.get("asm.sval", sizeof(double) * (size_t)N * a.rcap);
     return a;
@@ -844,6 +851,8 @@ void set_smem_limits()
                                  (int)(sizeof(FusedSmem<HC_S>) * ROW_WARPS)));
     TK_CUDA(cudaFuncSetAttribute(k_rows_fused<HC_L, RCAP_L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(FusedSmem<HC_L>) * ROW_WARPS)));
+    TK_CUDA(cudaFuncSetAttribute(k_rows_fused<HC_X, RCAP_X, STAGE_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(FusedSmem<HC_X, STAGE_X>) * ROW_WARPS)));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
     TK_CUDA(cudaFuncSetAttribute(k_rows_big<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_big));
 }
@@ -881,7 +890,12 @@ void assemble_rows_device(tk_ctx* ctx, int method, int64_t N, int k, int td, con
     TK_CHECK_LAUNCH();
     mark(ctx, KM_ASM_REV);
     set_smem_limits();
-    if (wide_rows(method, k))
+    if (widest_rows(k))
+        k_rows_fused<HC_X, RCAP_X, STAGE_X><<<rows_grid(ctx, N), ROW_WARPS * 32,
+                                              sizeof(FusedSmem<HC_X, STAGE_X>) * ROW_WARPS, st>>>(
+            method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig,
+            a.row_big, repeats);
+    else if (wide_rows(method, k))
         k_rows_fused<HC_L, RCAP_L><<<rows_grid(ctx, N), ROW_WARPS * 32, sizeof(FusedSmem<HC_L>) * ROW_WARPS, st>>>(
             method, N, k, td, idx, weights, shift, a.rptr, a.rev, a.row_nnz, a.scol, a.sval, a.big, a.nbig,
             a.row_big, repeats);
