@@ -647,6 +647,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             // without a bound: accept everything until the list fills
             float thr = (cmp < FLT_MAX) ? cmp * inv_m2 : -__int_as_float(0x7f800000);
+            const float thr_lo = lo * inv_m2;
             float far_max = -__int_as_float(0x7f800000);  // largest accumulator over far tiles
             const int64_t blk = I.q0 / TC_M + qt;
             ZigZag zz((int)(I.q0 / TC_N) - I.t0, I.ntiles);
@@ -712,11 +713,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                             const float* w = v + g * 8;
                             if (fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7])) > thr)
                             {
-                                // columns of the group that pass, then one insertion each
+                                // columns of the group that pass, then one insertion each; a
+                                // later pass drops the previous passes' entries (t < lo, i.e.
+                                // x > lo / m2, exact as m2 is a power of two) here already
                                 unsigned msk = 0u;
 #pragma unroll
                                 for (int e = 0; e < 8; ++e)
-                                    msk |= (w[e] > thr) ? (1u << e) : 0u;
+                                    msk |= (w[e] > thr && (!LATER || w[e] <= thr_lo)) ? (1u << e) : 0u;
                                 const int64_t cb = c0 + h * CPW + g * 8;
 #pragma unroll 1
                                 while (msk)
