@@ -164,22 +164,24 @@ __device__ __forceinline__ float reg_chol_solve(const float (&L)[KP], const floa
     return y;
 }
 
-// The same for KP = 64 with two rows per lane: lane a holds rows a (A0) and
-// a + 32 (A1), entries c <= row; rows of column j travel by shuffles from the
-// lane j & 31. ivd receives 1 / L_jj (written by the lane that holds row j).
-__device__ __forceinline__ void reg_cholesky64(float (&A0)[64], float (&A1)[64], float* ivd, int lane)
+// The same for KP = 64 with two rows per lane: lane a holds rows a (A0, columns
+// 0..31: its entries past column a are zero) and a + 32 (A1), entries c <= row;
+// rows of column j travel by shuffles from the lane j & 31. ivd receives 1 / L_jj
+// (written by the lane that holds row j). Indices into A0 are taken mod 32 in
+// branches that run only for columns below 32.
+__device__ __forceinline__ void reg_cholesky64(float (&A0)[32], float (&A1)[64], float* ivd, int lane)
 {
 #pragma unroll
     for (int j = 0; j < 64; ++j)
     {
-        const float djj = __shfl_sync(0xffffffffu, (j < 32) ? A0[j] : A1[j], j & 31);
+        const float djj = __shfl_sync(0xffffffffu, (j < 32) ? A0[j & 31] : A1[j], j & 31);
         const float inv = rsqrtf(fmaxf(djj, FLT_MIN));
         if (lane == (j & 31))
             ivd[j] = inv;
         if (j < 32)
         {
             if (lane >= j)
-                A0[j] *= inv;
+                A0[j & 31] *= inv;
             A1[j] *= inv;
         }
         else if (lane + 32 >= j)
@@ -189,11 +191,11 @@ __device__ __forceinline__ void reg_cholesky64(float (&A0)[64], float (&A1)[64],
         {
             if (c > j)
             {
-                const float lcj = __shfl_sync(0xffffffffu, (c < 32) ? A0[j] : A1[j], c & 31);
+                const float lcj = __shfl_sync(0xffffffffu, (c < 32) ? A0[j & 31] : A1[j], c & 31);
                 if (c < 32)
                 {
                     if (lane >= c)
-                        A0[c] = fmaf(-A0[j], lcj, A0[c]);
+                        A0[c & 31] = fmaf(-A0[j & 31], lcj, A0[c & 31]);
                     A1[c] = fmaf(-A1[j], lcj, A1[c]);
                 }
                 else if (lane + 32 >= c)
@@ -512,11 +514,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         constexpr int K64 = (KP == 64) ? 64 : 1;
         if constexpr (KP == 64)
         {
-            float A0[64], A1[64];
+            float A0[32], A1[64];
 #pragma unroll
             for (int c = 0; c < 64; ++c)
             {
-                A0[c] = (c <= lane) ? S.C[lane][c] : 0.f;
+                if (c < 32)
+                    A0[c & 31] = (c <= lane) ? S.C[lane][c] : 0.f;
                 A1[c] = (c <= lane + 32) ? S.C[lane + 32][c] : 0.f;
             }
             reg_cholesky64(A0, A1, S.ivd, lane);
@@ -524,8 +527,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
 #pragma unroll
             for (int c = 0; c < 64; ++c)
             {
-                if (c <= lane)
-                    S.C[lane][c] = A0[c];
+                if (c < 32 && c <= lane)
+                    S.C[lane][c] = A0[c & 31];
                 if (c <= lane + 32)
                     S.C[lane + 32][c] = A1[c];
             }
@@ -819,6 +822,331 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
     }
 }
 
+// ---------------------------------------------------------------------------
+// 33 <= k <= 64, float32 input, one problem: the k_lle solve with 18 KB of shared
+// memory per warp instead of 34.5 KB. The factor is kept as a packed lower
+// triangle (row r starts at r (r + 1) / 2; the triangular numbers mod 32 are all
+// distinct, so the row-per-lane reads of the sweeps hit distinct banks), and one
+// 64 x 33 buffer holds the chunk's differences for the Gram, then its raw
+// neighbour values for the refinement, which forms the exact differences by
+// two-sum as it reads them. Registers then bound the occupancy: 8 warps per SM
+// at up to 255 registers (k_lle at k = 64 ran 6). With 12 warps (168 registers)
+// the kernel spilled about 0.9 KB per thread and ran no faster than k_lle.
+constexpr int L64_WARPS = 8;
+
+struct Lle64Smem
+{
+    float B[64][33];
+    float Lp[64 * 65 / 2];
+    float xs[32];
+    float vh[32], vl[32];
+    float r[64], w[64], ivd[64];
+};
+
+__device__ __forceinline__ int tri(int r) { return (r * (r + 1)) >> 1; }
+
+// reg_chol_solve64 on the packed factor
+__device__ __forceinline__ void packed_solve64(const float* Lp, const float* ivd, float& y0, float& y1, int lane)
+{
+    const int t0 = tri(lane), t1 = tri(lane + 32);
+#pragma unroll 4
+    for (int j = 0; j < 64; ++j)
+    {
+        const float yj = __shfl_sync(0xffffffffu, (j < 32) ? y0 : y1, j & 31) * ivd[j];
+        const float a0 = (lane > j) ? Lp[t0 + j] : 0.f;
+        const float a1 = (lane + 32 > j) ? Lp[t1 + j] : 0.f;
+        if (j < 32)
+        {
+            if (lane == j)
+                y0 = yj;
+            else if (lane > j)
+                y0 = fmaf(-a0, yj, y0);
+            y1 = fmaf(-a1, yj, y1);
+        }
+        else
+        {
+            if (lane + 32 == j)
+                y1 = yj;
+            else if (lane + 32 > j)
+                y1 = fmaf(-a1, yj, y1);
+        }
+    }
+#pragma unroll 4
+    for (int j = 63; j >= 0; --j)
+    {
+        const float xj = __shfl_sync(0xffffffffu, (j < 32) ? y0 : y1, j & 31) * ivd[j];
+        const float l0 = (lane < j) ? Lp[tri(j) + lane] : 0.f;
+        const float l1 = (lane + 32 < j) ? Lp[tri(j) + lane + 32] : 0.f;
+        if (j < 32)
+        {
+            if (lane == j)
+                y0 = xj;
+            else if (lane < j)
+                y0 = fmaf(-l0, xj, y0);
+        }
+        else
+        {
+            if (lane + 32 == j)
+                y1 = xj;
+            else if (lane + 32 < j)
+                y1 = fmaf(-l1, xj, y1);
+            y0 = fmaf(-l0, xj, y0);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(L64_WARPS * 32) k_lle64(const float* __restrict__ X, int64_t N, int D, int64_t ldx,
+                                                          const int32_t* __restrict__ idx, int k, double klle_shift,
+                                                          const double* __restrict__ rhs, int normalize,
+                                                          double* __restrict__ W, unsigned* err)
+{
+    constexpr int NB4 = 16, NBLK = NB4 * (NB4 + 1) / 2, PERL = (NBLK + 31) / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    Lle64Smem& S = reinterpret_cast<Lle64Smem*>(smem_raw)[wib];
+    const int64_t nwarps = (int64_t)gridDim.x * L64_WARPS;
+    // (I, J) 4 x 4 blocks of the upper triangle owned by this lane
+    int bI[PERL], bJ[PERL];
+#pragma unroll
+    for (int m = 0; m < PERL; ++m)
+    {
+        int b = (lane + 32 * m < NBLK) ? lane + 32 * m : 0, I = 0;
+        while (b >= NB4 - I)
+        {
+            b -= NB4 - I;
+            ++I;
+        }
+        bI[m] = I;
+        bJ[m] = I + b;
+    }
+    const int t0 = tri(lane), t1 = tri(lane + 32);
+    for (int64_t i = (int64_t)blockIdx.x * L64_WARPS + wib; i < N; i += nwarps)
+    {
+        int nb[2];
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2)
+        {
+            const int a = lane + 32 * s2;
+            nb[s2] = (a < k) ? idx[i * k + a] : 0;
+            if (a < k && (nb[s2] < 0 || nb[s2] >= N))
+            {
+                atomicOr(err, DEV_ERR_BOUNDS);
+                nb[s2] = 0;
+            }
+        }
+        // ---- FP32 Gram of the differences, 4 x 4 blocks in registers ----
+        float acc[PERL][16];
+#pragma unroll
+        for (int m = 0; m < PERL; ++m)
+#pragma unroll
+            for (int t = 0; t < 16; ++t)
+                acc[m][t] = 0.f;
+        for (int d0 = 0; d0 < D; d0 += 32)
+        {
+            const int d = d0 + lane;
+            const float xi = (d < D) ? X[i * ldx + d] : 0.f;
+            __syncwarp();
+            // 32 neighbour values in flight at a time
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+            {
+                float v[32];
+#pragma unroll
+                for (int a = 0; a < 32; ++a)
+                {
+                    const int nba = __shfl_sync(0xffffffffu, nb[h], a);
+                    v[a] = (32 * h + a < k && d < D) ? X[(int64_t)nba * ldx + d] : xi;
+                }
+#pragma unroll
+                for (int a = 0; a < 32; ++a)
+                    S.B[32 * h + a][lane] = v[a] - xi;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int m = 0; m < PERL; ++m)
+            {
+                if (lane + 32 * m < NBLK)
+                {
+                    const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
+#pragma unroll 2
+                    for (int dd = 0; dd < 32; ++dd)
+                    {
+                        float av[4], bv[4];
+#pragma unroll
+                        for (int t = 0; t < 4; ++t)
+                        {
+                            av[t] = S.B[I4 + t][dd];
+                            bv[t] = S.B[J4 + t][dd];
+                        }
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c)
+                                acc[m][r * 4 + c] = fmaf(av[r], bv[c], acc[m][r * 4 + c]);
+                    }
+                }
+            }
+        }
+        // lower triangle: entry (J4 + c, I4 + r) of the upper block (I4 + r, J4 + c)
+#pragma unroll
+        for (int m = 0; m < PERL; ++m)
+            if (lane + 32 * m < NBLK)
+            {
+                const int I4 = 4 * bI[m], J4 = 4 * bJ[m];
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c)
+                        if (I4 + r <= J4 + c)
+                            S.Lp[tri(J4 + c) + I4 + r] = acc[m][r * 4 + c];
+            }
+        __syncwarp();
+        float trace = ((lane < k) ? S.Lp[t0 + lane] : 0.f) + ((lane + 32 < k) ? S.Lp[t1 + lane + 32] : 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            trace += __shfl_xor_sync(0xffffffffu, trace, o);
+        const float shift = (float)klle_shift * trace;
+        // regularised diagonal; padding rows and columns (zero) get an identity block
+        S.Lp[t0 + lane] = (lane < k) ? S.Lp[t0 + lane] + shift : 1.f;
+        S.Lp[t1 + lane + 32] = (lane + 32 < k) ? S.Lp[t1 + lane + 32] + shift : 1.f;
+        __syncwarp();
+
+        // ---- FP32 Cholesky in registers, solve with the packed factor ----
+        {
+            float A0[32], A1[64];
+#pragma unroll
+            for (int c = 0; c < 64; ++c)
+            {
+                if (c < 32)
+                    A0[c & 31] = (c <= lane) ? S.Lp[t0 + c] : 0.f;
+                A1[c] = (c <= lane + 32) ? S.Lp[t1 + c] : 0.f;
+            }
+            reg_cholesky64(A0, A1, S.ivd, lane);
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < 64; ++c)
+            {
+                if (c < 32 && c <= lane)
+                    S.Lp[t0 + c] = A0[c & 31];
+                if (c <= lane + 32)
+                    S.Lp[t1 + c] = A1[c];
+            }
+        }
+        __syncwarp();
+        {
+            float y0 = (lane < k) ? (rhs ? (float)rhs[i * k + lane] : 1.f) : 0.f;
+            float y1 = (lane + 32 < k) ? (rhs ? (float)rhs[i * k + lane + 32] : 1.f) : 0.f;
+            packed_solve64(S.Lp, S.ivd, y0, y1, lane);
+            S.w[lane] = (lane < k) ? y0 : 0.f;
+            S.w[lane + 32] = (lane + 32 < k) ? y1 : 0.f;
+        }
+        __syncwarp();
+
+        // ---- float-float residual refinement ----
+        const int iters = (k > D) ? 2 : 1;
+        for (int itr = 0; itr < iters; ++itr)
+        {
+            ff sa[2] = {ff_zero(), ff_zero()}, ta[2] = {ff_zero(), ff_zero()};
+            for (int d0 = 0; d0 < D; d0 += 32)
+            {
+                const int d = d0 + lane;
+                const float xi = (d < D) ? X[i * ldx + d] : 0.f;
+                __syncwarp();
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                {
+                    float v[32];
+#pragma unroll
+                    for (int a = 0; a < 32; ++a)
+                    {
+                        const int nba = __shfl_sync(0xffffffffu, nb[h], a);
+                        v[a] = (32 * h + a < k && d < D) ? X[(int64_t)nba * ldx + d] : xi;
+                    }
+#pragma unroll
+                    for (int a = 0; a < 32; ++a)
+                        S.B[32 * h + a][lane] = v[a];
+                }
+                S.xs[lane] = xi;
+                __syncwarp();
+                // v_d = sum_b w_b z_bd for d = d0 + lane, z exact by two-sum; four chains
+                ff vq[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
+                for (int b = 0; b < k; b += 4)
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+                        if (b + t < k)
+                        {
+                            const ff z = two_sum(S.B[b + t][lane], -xi);
+                            vq[t] = ff_fma(vq[t], S.w[b + t], 0.f, z.hi, z.lo);
+                        }
+                const ff vv = ff_add(ff_add(vq[0], vq[1]), ff_add(vq[2], vq[3]));
+                S.vh[lane] = vv.hi;
+                S.vl[lane] = vv.lo;
+                __syncwarp();
+#pragma unroll
+                for (int s2 = 0; s2 < 2; ++s2)
+                {
+                    const int a = lane + 32 * s2;
+                    if (a < k)
+                        for (int dd = 0; dd < 32; ++dd)
+                        {
+                            const ff z = two_sum(S.B[a][dd], -S.xs[dd]);
+                            sa[s2] = ff_fma(sa[s2], z.hi, z.lo, S.vh[dd], S.vl[dd]);
+                            ta[s2] = ff_fma(ta[s2], z.hi, z.lo, z.hi, z.lo);
+                        }
+                }
+                __syncwarp();
+            }
+            // exact trace = sum_a |z_a|^2
+            ff tr = ff_add(ta[0], ta[1]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                tr = ff_add(tr, ff_shfl_xor(tr, o));
+            const double shift_true = klle_shift * ff_to_double(tr);
+            float y[2];
+#pragma unroll
+            for (int s2 = 0; s2 < 2; ++s2)
+            {
+                const int a = lane + 32 * s2;
+                y[s2] = (a < k) ? (float)((rhs ? rhs[i * k + a] : 1.0) - ff_to_double(sa[s2]) -
+                                          shift_true * (double)S.w[a])
+                                : 0.f;
+            }
+            packed_solve64(S.Lp, S.ivd, y[0], y[1], lane);
+            __syncwarp();
+            if (lane < k)
+                S.w[lane] += y[0];
+            if (lane + 32 < k)
+                S.w[lane + 32] += y[1];
+            __syncwarp();
+        }
+
+        // ---- normalise (weights) or store the raw solution (adjoint solve) ----
+        if (!normalize)
+        {
+            for (int a = lane; a < k; a += 32)
+                W[i * k + a] = (double)S.w[a];
+            __syncwarp();
+            continue;
+        }
+        ff sum = ff_zero();
+        for (int a = lane; a < k; a += 32)
+            sum = ff_add(sum, ff{S.w[a], 0.f});
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            sum = ff_add(sum, ff_shfl_xor(sum, o));
+        const float y0 = 1.f / sum.hi;
+        const ff sy = two_prod(sum.hi, y0);
+        const float resid = ((1.f - sy.hi) - sy.lo) - sum.lo * y0;  // 1 - sum * y0
+        const float y1 = y0 * resid;
+        for (int a = lane; a < k; a += 32)
+        {
+            const ff q = two_prod(S.w[a], y0);
+            W[i * k + a] = (double)q.hi + (double)fmaf(S.w[a], y1, q.lo);
+        }
+        __syncwarp();
+    }
+}
+
 template <int KP, int WARPS, bool BATCH>
 void launch(tk_ctx* ctx, const LleRows& RW, const int32_t* idx, int k, double klle_shift, const double* rhs,
             int normalize, double* W)
@@ -861,6 +1189,17 @@ void lle_solve(tk_ctx* ctx, const void* X, int dtype, int64_t N, int D, int64_t 
     if (lle_pair_supported(X, dtype, ldx, k))
     {
         lle_pair_solve(ctx, X, N, D, ldx, idx, k, klle_shift, rhs, normalize, W);
+        return;
+    }
+    if (dtype == TK_F32 && k > 32 && k <= 64)
+    {
+        const size_t smem = sizeof(Lle64Smem) * L64_WARPS;
+        TK_CUDA(cudaFuncSetAttribute(k_lle64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int64_t want = (N + L64_WARPS - 1) / L64_WARPS;
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms));
+        k_lle64<<<grid, L64_WARPS * 32, smem, ctx->stream>>>(reinterpret_cast<const float*>(X), N, D, ldx, idx, k,
+                                                             klle_shift, rhs, normalize ? 1 : 0, W, ctx->dev_err);
+        TK_CHECK_LAUNCH();
         return;
     }
     const LleRows RW{X, dtype, N, D, ldx, N, nullptr, nullptr, 0, nullptr};
