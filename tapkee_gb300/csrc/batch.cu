@@ -479,6 +479,7 @@ void upload(T* dst, const std::vector<T>& src, cudaStream_t st)
 struct ScreenGroup
 {
     int Dp = 0, kc = 0, qt = 1;
+    int kmax = 0;            // largest k of the group's problems
     std::vector<int> probs;  // batch (sorted) problem numbers
     int64_t rows = 0;
     __half *xh = nullptr, *xl = nullptr, *xn = nullptr;
@@ -617,6 +618,7 @@ void enqueue(tk_batch* B)
         SS.Dp = S.Dp;
         SS.kc = S.kc;
         SS.qt = S.qt;
+        SS.kmax = S.kmax;
         SS.rows = S.rows;
         SS.xh = reinterpret_cast<const uint16_t*>(S.xh);
         SS.xl = reinterpret_cast<const uint16_t*>(S.xl);
@@ -767,6 +769,7 @@ void plan(tk_batch* B, const tk_batch_problem* problems, int count)
         h.row0 = g.rows;
         g.rows += ((q.N + 255) / 256) * 256;
         g.probs.push_back(s);
+        g.kmax = std::max(g.kmax, q.k);
         // Morton buckets: about four points each
         int bits = 2;
         while (bits < 24 && ((int64_t)1 << (bits + 2)) < q.N)

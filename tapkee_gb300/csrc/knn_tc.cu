@@ -748,8 +748,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (!alive)
                 break;
-            const int64_t o = BATCH ? q * KC : q * slice.ld + slice.off;
-            const int nw = BATCH ? KC : slice.nw;
+            const int64_t o = q * slice.ld + slice.off;
+            const int nw = slice.nw;
 #pragma unroll
             for (int s = 0; s < KC; ++s)
                 if (s < nw)
@@ -1798,17 +1798,29 @@ void screen_tensor_batch(tk_ctx* ctx, const StackedScreen& S, int32_t* cand_idx,
     if (grid <= 0)
         return;
 #define TK_SCREEN_BATCH(DPV, KCV, QTV)                                                                            \
-    launch<DPV, KCV, QTV, true>(ctx, S.xh, S.xl, S.xn, S.nrm, S.rows, nullptr, 0, work, grid, cand_idx, cand_val)
+    launch<DPV, KCV, QTV, true>(ctx, S.xh, S.xl, S.xn, S.nrm, S.rows, nullptr, 0, work, grid, cand_idx, cand_val, rows)
+    // 64-candidate rows of a group whose k are all <= 40 come from the 48-entry
+    // list (no spills), padded to 64 with its last value and id -1
+    const bool short64 = S.kc == 64 && S.kmax >= 1 && S.kmax + 8 <= TC_PASS;
+    ListSlice rows;
+    rows.ld = S.kc;
+    rows.nw = S.kc;
     if (S.Dp == 64 && S.kc == 32 && S.qt == 2)
         TK_SCREEN_BATCH(64, 32, 2);
     else if (S.Dp == 64 && S.kc == 32 && S.qt == 1)
         TK_SCREEN_BATCH(64, 32, 1);
+    else if (S.Dp == 64 && short64 && S.qt == 2)
+        TK_SCREEN_BATCH(64, TC_PASS, 2);
+    else if (S.Dp == 64 && short64 && S.qt == 1)
+        TK_SCREEN_BATCH(64, TC_PASS, 1);
     else if (S.Dp == 64 && S.kc == 64 && S.qt == 2)
         TK_SCREEN_BATCH(64, 64, 2);
     else if (S.Dp == 64 && S.kc == 64 && S.qt == 1)
         TK_SCREEN_BATCH(64, 64, 1);
     else if (S.Dp == 128 && S.kc == 32)
         TK_SCREEN_BATCH(128, 32, 1);
+    else if (S.Dp == 128 && short64)
+        TK_SCREEN_BATCH(128, TC_PASS, 1);
     else if (S.Dp == 128 && S.kc == 64)
         TK_SCREEN_BATCH(128, 64, 1);
     else

@@ -80,9 +80,9 @@ struct Prepared
     int32_t* perm = nullptr;    // sorted position -> original index
     float* rmax = nullptr;      // device scalars: [0] R = max |xc|, [1] fp16 scale exponent s
     float scale_log2 = 0.f;     // xh/xl hold xc * 2^scale_log2
-    // set by the wide tensor screen: per sorted row, the smallest screened value
-    // over the candidate tiles screened with high parts only (FLT_MAX: none),
-    // and the relative error constant of those values
+    // set by the wide tensor screen and the seeded long-list passes: per sorted
+    // row, the smallest screened value over the candidate tiles screened with
+    // high parts only (FLT_MAX: none), and the relative error constant of those values
     float* far_val = nullptr;
     float c2_far = 0.f;
 };
@@ -172,6 +172,7 @@ struct BatchProb
 struct StackedScreen
 {
     int Dp = 0, kc = 0, qt = 1;
+    int kmax = 0;                     // largest k of the group's problems
     int64_t rows = 0;                 // stacked rows (multiple of 256)
     const uint16_t* xh = nullptr;     // rows x Dp fp16 hi / lo of 2^s (x - mean)
     const uint16_t* xl = nullptr;
