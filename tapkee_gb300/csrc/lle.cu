@@ -257,13 +257,45 @@ __device__ __forceinline__ void reg_chol_solve64(const float* Ls, const float* i
     }
 }
 
+// reg_chol_solve with the factor's rows read from Ls (row a = row a of L, stride
+// KP + 1) in both sweeps, so no factor registers stay live: the same values and
+// operations, so the same results.
+template <int KP>
+__device__ __forceinline__ float smem_chol_solve(const float* Ls, const float* ivd, float r, int lane)
+{
+    float y = r;
+#pragma unroll 4
+    for (int j = 0; j < KP; ++j)
+    {
+        const float yj = __shfl_sync(0xffffffffu, y, j) * ivd[j];
+        const float lij = (lane > j && lane < KP) ? Ls[lane * (KP + 1) + j] : 0.f;
+        if (lane == j)
+            y = yj;
+        else if (lane > j)
+            y = fmaf(-lij, yj, y);
+    }
+#pragma unroll 4
+    for (int j = KP - 1; j >= 0; --j)
+    {
+        const float lji = (lane < j) ? Ls[j * (KP + 1) + lane] : 0.f;
+        const float xj = __shfl_sync(0xffffffffu, y, j) * ivd[j];
+        if (lane == j)
+            y = xj;
+        else if (lane < j)
+            y = fmaf(-lji, xj, y);
+    }
+    return y;
+}
+
 __device__ __forceinline__ float ld_f(const void* X, int dtype, int64_t off)
 {
     return dtype == TK_F64 ? (float)reinterpret_cast<const double*>(X)[off] : reinterpret_cast<const float*>(X)[off];
 }
 
+// KP = 32 holds at most 128 registers (16 warps per SM): its refinement keeps no
+// per-lane arrays over the neighbours (see below)
 template <int KP, int WARPS, bool BATCH, bool BLOCKED = (KP <= 64)>
-__global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int32_t* __restrict__ idx, int k,
+__global__ void __launch_bounds__(WARPS * 32, (KP == 32) ? 256 / WARPS : 1) k_lle(const LleRows RW, const int32_t* __restrict__ idx, int k,
                                                     double klle_shift, const double* __restrict__ rhs,
                                                     int normalize, double* __restrict__ W, unsigned* err)
 {
@@ -592,7 +624,81 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
         const int iters = (k > D) ? 2 : 1;
         for (int itr = 0; itr < iters; ++itr)
         {
-            if (KP <= 32)
+            if (KP == 32)
+            {
+                // the chunk's exact differences z_a(d) staged in shared memory (lanes
+                // own dimensions for the loads); v(d) = sum_b w_b z_b(d) by the lane
+                // owning d; then lane a forms (C w)_a = sum_d z_a(d) v(d) itself. The
+                // shift uses the FP32 trace, as for k <= 16.
+                ff ca = ff_zero();
+                for (int d0 = 0; d0 < D; d0 += 32)
+                {
+                    const int d = d0 + lane;
+                    if (dtype == TK_F32)
+                    {
+                        const float xi = (d < D) ? ld_f(X, dtype, i * ldx + d) : 0.f;
+                        float v[32];
+#pragma unroll
+                        for (int a = 0; a < 32; ++a)
+                        {
+                            const int nba = __shfl_sync(0xffffffffu, nb[0], a);
+                            v[a] = (a < k && d < D) ? ld_f(X, dtype, (int64_t)nba * ldx + d) : xi;
+                        }
+#pragma unroll
+                        for (int a = 0; a < 32; ++a)
+                        {
+                            const ff z = two_sum(v[a], -xi);
+                            S.Zh[a][lane] = z.hi;
+                            S.Zl[a][lane] = z.lo;
+                        }
+                    }
+                    else
+                    {
+                        for (int a = 0; a < 32; ++a)
+                        {
+                            const int nba = __shfl_sync(0xffffffffu, nb[0], a);
+                            ff z = ff_zero();
+                            if (a < k && d < D)
+                                z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
+                            S.Zh[a][lane] = z.hi;
+                            S.Zl[a][lane] = z.lo;
+                        }
+                    }
+                    __syncwarp();
+                    ff vq[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
+                    for (int b = 0; b < k; b += 4)
+#pragma unroll
+                        for (int t = 0; t < 4; ++t)
+                            if (b + t < k)
+                                vq[t] = ff_fma(vq[t], S.w[b + t], 0.f, S.Zh[b + t][lane], S.Zl[b + t][lane]);
+                    const ff vv = ff_add(ff_add(vq[0], vq[1]), ff_add(vq[2], vq[3]));
+                    S.vh[lane] = vv.hi;
+                    S.vl[lane] = vv.lo;
+                    __syncwarp();
+                    if (lane < k)
+#pragma unroll 8
+                        for (int dd = 0; dd < 32; ++dd)
+                            ca = ff_fma(ca, S.Zh[lane][dd], S.Zl[lane][dd], S.vh[dd], S.vl[dd]);
+                    __syncwarp();
+                }
+                float ra = 0.f;
+                if (lane < k)
+                {
+                    const ff sw = ff_mul(ff_mul(ks, ff{trace, 0.f}), ff{S.w[lane], 0.f});
+                    ff b = ff{1.f, 0.f};
+                    if (rhs)
+                    {
+                        const double rb = rhs[g * k + lane];
+                        b.hi = (float)rb;
+                        b.lo = (float)(rb - (double)b.hi);
+                    }
+                    const ff rr = ff_add(ff_add(b, ff_neg(ca)), ff_neg(sw));
+                    ra = rr.hi + rr.lo;
+                }
+                S.r[lane] = ra;
+                __syncwarp();
+            }
+            else if (KP <= 32)
             {
                 // lanes own dimensions: z_a(d) = hi + lo exactly, v(d) = sum_b w_b z_b(d),
                 // and lane-local partials of (C w)_a = sum_d z_a(d) v(d); one
@@ -774,6 +880,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_lle(const LleRows RW, const int3
                     S.w[lane] += y0;
                 if (lane + 32 < k)
                     S.w[lane + 32] += y1;
+            }
+            else if constexpr (KP == 32)
+            {
+                const float x = smem_chol_solve<KP>(&S.C[0][0], S.ivd, S.r[lane], lane);
+                __syncwarp();
+                if (lane < k)
+                    S.w[lane] += x;
             }
             else if constexpr (KP <= 32)
             {
