@@ -292,10 +292,10 @@ __device__ __forceinline__ float ld_f(const void* X, int dtype, int64_t off)
     return dtype == TK_F64 ? (float)reinterpret_cast<const double*>(X)[off] : reinterpret_cast<const float*>(X)[off];
 }
 
-// KP = 32 holds at most 128 registers (16 warps per SM): its refinement keeps no
+// KP <= 32 holds at most 128 registers (16 warps per SM): its refinement keeps no
 // per-lane arrays over the neighbours (see below)
 template <int KP, int WARPS, bool BATCH, bool BLOCKED = (KP <= 64)>
-__global__ void __launch_bounds__(WARPS * 32, (KP == 32) ? 256 / WARPS : 1) k_lle(const LleRows RW, const int32_t* __restrict__ idx, int k,
+__global__ void __launch_bounds__(WARPS * 32, (KP <= 32) ? 16 / WARPS : 1) k_lle(const LleRows RW, const int32_t* __restrict__ idx, int k,
                                                     double klle_shift, const double* __restrict__ rhs,
                                                     int normalize, double* __restrict__ W, unsigned* err)
 {
@@ -624,12 +624,13 @@ __global__ void __launch_bounds__(WARPS * 32, (KP == 32) ? 256 / WARPS : 1) k_ll
         const int iters = (k > D) ? 2 : 1;
         for (int itr = 0; itr < iters; ++itr)
         {
-            if (KP == 32)
+            if (KP <= 32)
             {
                 // the chunk's exact differences z_a(d) staged in shared memory (lanes
                 // own dimensions for the loads); v(d) = sum_b w_b z_b(d) by the lane
                 // owning d; then lane a forms (C w)_a = sum_d z_a(d) v(d) itself. The
-                // shift uses the FP32 trace, as for k <= 16.
+                // shift uses the FP32 trace: its relative error (~D 2^-24) enters the
+                // residual scaled by klle_shift, far below the solve's own error.
                 ff ca = ff_zero();
                 for (int d0 = 0; d0 < D; d0 += 32)
                 {
@@ -637,15 +638,16 @@ __global__ void __launch_bounds__(WARPS * 32, (KP == 32) ? 256 / WARPS : 1) k_ll
                     if (dtype == TK_F32)
                     {
                         const float xi = (d < D) ? ld_f(X, dtype, i * ldx + d) : 0.f;
-                        float v[32];
+                        constexpr int KV = (KP <= 32) ? KP : 1;
+                        float v[KV];
 #pragma unroll
-                        for (int a = 0; a < 32; ++a)
+                        for (int a = 0; a < KV; ++a)
                         {
                             const int nba = __shfl_sync(0xffffffffu, nb[0], a);
                             v[a] = (a < k && d < D) ? ld_f(X, dtype, (int64_t)nba * ldx + d) : xi;
                         }
 #pragma unroll
-                        for (int a = 0; a < 32; ++a)
+                        for (int a = 0; a < KV; ++a)
                         {
                             const ff z = two_sum(v[a], -xi);
                             S.Zh[a][lane] = z.hi;
@@ -654,7 +656,7 @@ __global__ void __launch_bounds__(WARPS * 32, (KP == 32) ? 256 / WARPS : 1) k_ll
                     }
                     else
                     {
-                        for (int a = 0; a < 32; ++a)
+                        for (int a = 0; a < KP && a < 32; ++a)
                         {
                             const int nba = __shfl_sync(0xffffffffu, nb[0], a);
                             ff z = ff_zero();
@@ -695,90 +697,8 @@ __global__ void __launch_bounds__(WARPS * 32, (KP == 32) ? 256 / WARPS : 1) k_ll
                     const ff rr = ff_add(ff_add(b, ff_neg(ca)), ff_neg(sw));
                     ra = rr.hi + rr.lo;
                 }
-                S.r[lane] = ra;
-                __syncwarp();
-            }
-            else if (KP <= 32)
-            {
-                // lanes own dimensions: z_a(d) = hi + lo exactly, v(d) = sum_b w_b z_b(d),
-                // and lane-local partials of (C w)_a = sum_d z_a(d) v(d); one
-                // reduce-scatter gathers (C w)_a. The shift uses the FP32 trace:
-                // its relative error (~D 2^-24) enters the residual scaled by
-                // klle_shift, far below the solve's own error.
-                constexpr int KR = (KP <= 32) ? KP : 32;
-                ff part[KR];
-#pragma unroll
-                for (int a = 0; a < KR; ++a)
-                    part[a] = ff_zero();
-                for (int d0 = 0; d0 < D; d0 += 32)
-                {
-                    const int d = d0 + lane;
-                    float zh[KR], zl[KR];
-#pragma unroll
-                    for (int a = 0; a < KR; ++a)
-                    {
-                        const int nba = __shfl_sync(0xffffffffu, nb[0], a & 31);
-                        ff z = ff_zero();
-                        if (a < k && d < D)
-                            z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
-                        zh[a] = z.hi;
-                        zl[a] = z.lo;
-                    }
-                    // two independent chains for v
-                    ff v0 = ff_zero(), v1 = ff_zero();
-#pragma unroll
-                    for (int b = 0; b < KR; b += 2)
-                    {
-                        v0 = ff_fma(v0, S.w[b], 0.f, zh[b], zl[b]);
-                        if (b + 1 < KR)
-                            v1 = ff_fma(v1, S.w[b + 1], 0.f, zh[b + 1], zl[b + 1]);
-                    }
-                    const ff v = ff_add(v0, v1);
-#pragma unroll
-                    for (int a = 0; a < KR; ++a)
-                        part[a] = ff_fma(part[a], zh[a], zl[a], v.hi, v.lo);
-                }
-                // reduce-scatter of the KR partials (KR = 16 or 32 values)
-#pragma unroll
-                for (int lvl = 0; lvl < 5; ++lvl)
-                {
-                    const int o = 16 >> lvl;
-                    const int half = (KR >> (lvl + 1)) > 0 ? (KR >> (lvl + 1)) : 0;
-                    if (half > 0)
-                    {
-                        const bool upper = (lane & o) != 0;
-#pragma unroll
-                        for (int q = 0; q < half; ++q)
-                        {
-                            const ff send = upper ? part[q] : part[q + half];
-                            const ff keep = upper ? part[q + half] : part[q];
-                            part[q] = ff_add(keep, ff_shfl_xor(send, o));
-                        }
-                    }
-                    else
-                        part[0] = ff_add(part[0], ff_shfl_xor(part[0], o));  // pairs hold the same index
-                }
-                // part[0] of lane l is (C w)_a for a = KR == 32 ? l : (l >> 1);
-                // r_a = rhs_a - (C w)_a - klle_shift trace w_a in float-float
-                const int a_own = (KR == 32) ? lane : (lane >> 1);
-                if ((KR == 32 || (lane & 1) == 0) && a_own < KP)
-                {
-                    float ra = 0.f;
-                    if (a_own < k)
-                    {
-                        const ff sw = ff_mul(ff_mul(ks, ff{trace, 0.f}), ff{S.w[a_own], 0.f});
-                        ff b = ff{1.f, 0.f};
-                        if (rhs)
-                        {
-                            const double rb = rhs[g * k + a_own];
-                            b.hi = (float)rb;
-                            b.lo = (float)(rb - (double)b.hi);
-                        }
-                        const ff rr = ff_add(ff_add(b, ff_neg(part[0])), ff_neg(sw));
-                        ra = rr.hi + rr.lo;
-                    }
-                    S.r[a_own] = ra;
-                }
+                if (lane < KP)
+                    S.r[lane] = ra;
                 __syncwarp();
             }
             else
@@ -881,16 +801,9 @@ __global__ void __launch_bounds__(WARPS * 32, (KP == 32) ? 256 / WARPS : 1) k_ll
                 if (lane + 32 < k)
                     S.w[lane + 32] += y1;
             }
-            else if constexpr (KP == 32)
-            {
-                const float x = smem_chol_solve<KP>(&S.C[0][0], S.ivd, S.r[lane], lane);
-                __syncwarp();
-                if (lane < k)
-                    S.w[lane] += x;
-            }
             else if constexpr (KP <= 32)
             {
-                const float x = reg_chol_solve<KP>(Lr, &S.C[0][0], S.ivd, lane < KP ? S.r[lane] : 0.f, lane);
+                const float x = smem_chol_solve<KP>(&S.C[0][0], S.ivd, lane < KP ? S.r[lane] : 0.f, lane);
                 __syncwarp();
                 if (lane < k)
                     S.w[lane] += x;
