@@ -316,9 +316,9 @@ __device__ __forceinline__ Item fetch_item(const ScreenWork& W, int j, int64_t N
 // empty (seed_tr = T_r, the row's k-th distance over the other rows of its
 // 128-row block; rmax[0] = R; c1, c2 the screen's error model), as in the wide
 // kernel: only candidates screened below B are inserted, and a list with fewer
-// real entries ends in entries (B, -1). A later pass whose rows all ended the
-// previous pass below their list length (last value B) has nothing to add: the
-// CTA writes (B, -1) lists without screening.
+// real entries ends in entries (B, -1). (A later pass runs only where a row needs
+// more than one pass's entries, k + 8 > KC, so the k + 1 candidates below B have
+// filled the earlier passes' lists.)
 struct ListSlice
 {
     int ld = 0, off = 0;          // row stride of the output lists and this pass's offset
@@ -432,40 +432,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     tc_fence_before();
-    // a later pass screens only when one of its rows filled the previous pass's
-    // list below the row's bound
-    int need = 1;
-    if constexpr (LATER)
-    {
-        need = 0;
-        if (warp < C::EPI_WARPS)
-        {
-            const int64_t q = (int64_t)j_first * QROWS + (warp >> 2) * TC_M + (warp & 3) * 32 + lane;
-            need = slice.lo[q] < seed_bound(slice, q, nrm[q]) ? 1 : 0;
-        }
-    }
-    const bool screen = __syncthreads_or(need) != 0;
+    __syncthreads();
     tc_fence_after();
     const uint32_t tmem = Bar.tmem_base;
 
-    if (!screen)
-    {
-        if (warp < C::EPI_WARPS)
-        {
-            const int64_t q = (int64_t)j_first * QROWS + (warp >> 2) * TC_M + (warp & 3) * 32 + lane;
-            const float nq = nrm[q];
-            const float b = seed_bound(slice, q, nq);
-            const int64_t o = q * slice.ld + slice.off;
-            for (int s = 0; s < slice.nw; ++s)
-            {
-                cand_idx[o + s] = -1;
-                cand_val[o + s] = (b < FLT_MAX) ? b + nq : FLT_MAX;
-            }
-            if (slice.last)
-                slice.last[q] = b;
-        }
-    }
-    else if (warp == 8)
+    if (warp == 8)
     {
         // ------------------------------------------------------------ producer
         if (lane == 0)
