@@ -18,11 +18,6 @@
 namespace tk {
 namespace {
 
-__device__ __forceinline__ double ldx_elem(const void* X, int dtype, int64_t off)
-{
-    return dtype == TK_F64 ? reinterpret_cast<const double*>(X)[off] : (double)reinterpret_cast<const float*>(X)[off];
-}
-
 // x_a - x_b for element d as an unevaluated float sum hi + lo (exact for float32
 // input: two_sum of the two floats; float64 input: the FP64 difference split).
 __device__ __forceinline__ ff diff_ff(const void* X, int dtype, int64_t a_off, int64_t b_off)
@@ -287,6 +282,18 @@ __device__ __forceinline__ float smem_chol_solve(const float* Ls, const float* i
     return y;
 }
 
+// nb[s] holds neighbour lane + 32 s of the lane; a runtime group index picks the
+// register by selects (no indexed local-memory access)
+template <int NPL>
+__device__ __forceinline__ int nb_group(const int (&nb)[NPL], int s)
+{
+    int v = nb[0];
+#pragma unroll
+    for (int t = 1; t < NPL; ++t)
+        v = (s == t) ? nb[t] : v;
+    return v;
+}
+
 __device__ __forceinline__ float ld_f(const void* X, int dtype, int64_t off)
 {
     return dtype == TK_F64 ? (float)reinterpret_cast<const double*>(X)[off] : reinterpret_cast<const float*>(X)[off];
@@ -433,7 +440,7 @@ __global__ void __launch_bounds__(WARPS * 32, (KP <= 32) ? 16 / WARPS : 1) k_lle
 #pragma unroll 4
                 for (int a = 0; a < KP; ++a)
                 {
-                    const int nba = __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
+                    const int nba = __shfl_sync(0xffffffffu, nb_group<NPL>(nb, a >> 5), a & 31);
                     float v = 0.f;
                     if (a < k && d < D)
                         v = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d).hi;
@@ -441,7 +448,7 @@ __global__ void __launch_bounds__(WARPS * 32, (KP <= 32) ? 16 / WARPS : 1) k_lle
                 }
             }
             __syncwarp();
-            if (!BLOCKED)
+            if constexpr (!BLOCKED)
             {
                 // upper-triangle entries, one lane per entry (large k)
                 for (int e = lane; e < KP * KP; e += 32)
@@ -457,6 +464,7 @@ __global__ void __launch_bounds__(WARPS * 32, (KP <= 32) ? 16 / WARPS : 1) k_lle
                 __syncwarp();
                 continue;
             }
+            else
 #pragma unroll
             for (int m = 0; m < PERL; ++m)
             {
@@ -737,7 +745,7 @@ __global__ void __launch_bounds__(WARPS * 32, (KP <= 32) ? 16 / WARPS : 1) k_lle
                         for (int a = 0; a < KP; ++a)
                         {
                             const int nba =
-                                __shfl_sync(0xffffffffu, (NPL == 1 || a < 32) ? nb[0] : nb[NPL - 1], a & 31);
+                                __shfl_sync(0xffffffffu, nb_group<NPL>(nb, a >> 5), a & 31);
                             ff z = ff_zero();
                             if (a < k && d < D)
                                 z = diff_ff(X, dtype, (int64_t)nba * ldx + d, i * ldx + d);
