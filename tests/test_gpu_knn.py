@@ -149,6 +149,18 @@ def test_continuous_data_has_no_tie_rows(ctx):
     assert st["tie_rows"] == 0 and st["extra_rows"] == 0
 
 
+def test_wide_dimensions_take_the_fp32_screen(ctx):
+    """D = 300: the tensor-core screen (padded D <= 128) refuses it; the FP32
+    screen and the re-rank's dimension-parallel path (D > 256) match the oracle."""
+    import tapkee_gb300 as tk
+    X = datasets.lifted_swiss_roll(700, 300, seed=5)
+    with pytest.raises(tk.UnsupportedMethodError):
+        ctx.knn_brute(X, 12, screen="tensor")
+    idx = ctx.knn_brute(X, 12, screen="fp32")
+    ref, _, _ = oracle.knn_brute(X, 12)
+    assert np.array_equal(idx, _ordered(X, ref)[0])
+
+
 def test_invalid_arguments(ctx):
     import tapkee_gb300 as tk
     X = np.zeros((10, 3), np.float32)

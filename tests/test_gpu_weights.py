@@ -29,7 +29,8 @@ def test_lle_weights_k_greater_than_d(ctx, golden):
                                          (800, 8, 48, np.float32), (3000, 64, 64, np.float32),
                                          (2000, 128, 40, np.float32), (1500, 16, 60, np.float32),
                                          (1200, 32, 50, np.float64), (900, 100, 33, np.float32),
-                                         (1000, 16, 100, np.float32)])
+                                         (1000, 16, 100, np.float32), (700, 8, 90, np.float64),
+                                         (600, 300, 12, np.float32), (500, 300, 40, np.float32)])
 def test_lle_weights_lifted(ctx, n, d, k, dtype):
     X = datasets.lifted_swiss_roll(n, d, seed=n, dtype=dtype)
     idx, _, _ = oracle.knn_brute(X, k)
