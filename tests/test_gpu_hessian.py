@@ -44,7 +44,8 @@ def test_hessian_blocks_golden_s_curve(ctx, golden):
 
 
 @pytest.mark.parametrize("n,d,k,td,dtype", [(3000, 32, 20, 2, np.float32), (2000, 16, 12, 1, np.float32),
-                                            (1200, 8, 30, 2, np.float64), (1500, 64, 48, 2, np.float32)])
+                                            (1200, 8, 30, 2, np.float64), (1500, 64, 48, 2, np.float32),
+                                            (1500, 64, 64, 2, np.float32), (900, 16, 40, 1, np.float64)])
 def test_hessian_blocks_lifted(ctx, n, d, k, td, dtype):
     X = datasets.lifted_s_curve(n, d, seed=n + k, noise=0.02, dtype=dtype)
     idx, _, _ = oracle.knn_brute(X, k)
