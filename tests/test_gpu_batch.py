@@ -63,6 +63,28 @@ def test_batch_vs_oracle_and_mixed_dtypes(ctx):
     b.close()
 
 
+def test_batch_long_lists_vs_oracle(ctx):
+    """k from 33 to 56 in a batch: 64-candidate rows from the 48-entry list (a
+    group whose k are all <= 40) and from the 64-entry list (k up to 56), and the
+    weight solve at 64 padded neighbours; D = 3 to 128."""
+    import torch
+    from tapkee_gb300.batch import Batch
+    rng = np.random.default_rng(21)
+    dims = [3, 16, 64, 128, 16, 64]
+    ks = [36, 44, 56, 40, 52, 33]
+    data = [datasets.batch_problem_data(int(rng.integers(400, 1200)), d, 100 + i) for i, d in enumerate(dims)]
+    Xs = [torch.from_numpy(x).cuda() for x in data]
+    b = Batch(Xs, ks, context=ctx)
+    b.run()
+    for p, k in enumerate(ks):
+        got = b.result(p)
+        idx_ref, _, _ = oracle.knn_brute(data[p], k)
+        assert all(set(a) == set(c) for a, c in zip(got.idx.tolist(), idx_ref.tolist())), p
+        W_ref = oracle.lle_weights(data[p], got.idx, 1e-3)
+        assert np.abs(got.weights - W_ref).max() / np.abs(W_ref).max() < 1e-5, p
+    b.close()
+
+
 def test_batch_rejects_bad_problems(ctx):
     import torch
     from tapkee_gb300 import WrongParameterError, UnsupportedMethodError
