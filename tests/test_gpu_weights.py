@@ -43,10 +43,13 @@ def _P(V, k):
     return np.einsum("nat,nbt->nab", V, V) + 1.0 / k
 
 
-@pytest.mark.parametrize("n,d,k,td", [(1500, 8, 12, 2), (3000, 32, 20, 2), (2000, 16, 10, 3), (1000, 64, 30, 2),
-                                      (1500, 16, 40, 2), (1200, 8, 64, 3), (1500, 32, 22, 2)])
-def test_ltsa_basis(ctx, n, d, k, td):
-    X = datasets.lifted_s_curve(n, d, seed=n, noise=0.02)
+@pytest.mark.parametrize("n,d,k,td,dtype", [(1500, 8, 12, 2, np.float32), (3000, 32, 20, 2, np.float32),
+                                            (2000, 16, 10, 3, np.float32), (1000, 64, 30, 2, np.float32),
+                                            (1500, 16, 40, 2, np.float32), (1200, 8, 64, 3, np.float32),
+                                            (1500, 32, 22, 2, np.float32), (900, 16, 40, 2, np.float64),
+                                            (700, 32, 64, 4, np.float64)])
+def test_ltsa_basis(ctx, n, d, k, td, dtype):
+    X = datasets.lifted_s_curve(n, d, seed=n, noise=0.02, dtype=dtype)
     idx, _, _ = oracle.knn_brute(X, k)
     V = ctx.ltsa_basis(X, idx, td)
     ref = oracle.ltsa_basis(X, idx, td)
