@@ -275,6 +275,31 @@ __global__ void __launch_bounds__(RR_WARPS * 32)
                     exact[s] = false;
                 }
         }
+        else if (D < 32)
+        {
+            // few dimensions in rows that are not 16-byte aligned: lanes own
+            // candidates, scalar loads against the query row staged in shared
+            // memory (lanes owning dimensions would leave most lanes idle)
+            const float* Xf = reinterpret_cast<const float*>(X);
+            __syncwarp();
+            if (lane < D)
+                qs[lane] = __ldg(Xf + i * ldx + lane);
+            __syncwarp();
+#pragma unroll
+            for (int s = 0; s < PER; ++s)
+                if (j[s] < NONE)
+                {
+                    const float* yr = Xf + (int64_t)j[s] * ldx;
+                    float a = 0.f;
+                    for (int d = 0; d < D; ++d)
+                    {
+                        const float z = __ldg(yr + d) - qs[d];
+                        a = fmaf(z, z, a);
+                    }
+                    kh[s] = a;
+                    exact[s] = false;
+                }
+        }
         else
         {
             // FP32 screen of the candidates: lanes own dimensions, so every row
