@@ -301,17 +301,17 @@ __device__ __forceinline__ Item fetch_item(const ScreenWork& W, int j, int64_t N
     return it;
 }
 
-// Where a launch writes its KC entries per row, for candidate lists longer than the
-// register lists (KC = 64): pass p of a multi-pass screen writes entries
-// [off, off + KC) of rows of ld entries, and keeps only candidates that come after
-// the previous passes' lists in the order (screened value, id). `lo` holds each
-// row's last screened value of pass p - 1 (before the row norm is added); pass p
-// takes t > lo, and t == lo only for ids that entries [0, off) do not hold. Every
+// Where a launch writes its KC-entry register list per row, for candidate lists
+// longer than one such list: pass p of a multi-pass screen writes from entry off
+// of rows of ld entries, and keeps only candidates that come after the previous
+// passes' lists in the order (screened value, id). `lo` holds each row's last
+// screened value of pass p - 1 (before the row norm is added); pass p takes
+// t > lo, and t == lo only for ids that entries [0, off) do not hold. Every
 // candidate with t < lo is in those entries already (a list that ends at lo
 // rejected only values >= its last value at the time, which never rose), so the
-// passes together hold the ld smallest screened values of the row and the last
-// pass's last value bounds every candidate outside them. `last` (when set)
-// receives each row's last screened value of this pass for the next one.
+// passes together hold the row's smallest screened values in order, and the last
+// kept value bounds every candidate outside them. `last` (when set) receives each
+// row's last screened value of this pass for the next one.
 // Lists may also start full of each row's bound B = 1.01 T_r + 2 eps instead of
 // empty (seed_tr = T_r, the row's k-th distance over the other rows of its
 // 128-row block; rmax[0] = R; c1, c2 the screen's error model), as in the wide
@@ -1600,9 +1600,9 @@ void launch_wide(tk_ctx* ctx, Prepared& P, int k, int32_t* cand_idx, float* cand
     }
 }
 
-// The bound that seeds the 64-entry lists (padded dimension 64, k <= 64): each
-// row's k-th distance over its 128-row block (k_blockmate). Without it (other
-// dimensions, larger k) the lists start empty.
+// The bound that seeds the lists of the long-list passes (padded dimension 64,
+// k <= 64): each row's k-th distance over its 128-row block (k_blockmate).
+// Without it (other dimensions, larger k) the lists start empty.
 // The same bound classifies the candidate tiles (128 rows, the same blocks as the
 // query blocks, so one set of spheres serves both) into near and far, as for the
 // wide kernel; far_val goes to P for the re-rank's certification.
@@ -1684,9 +1684,9 @@ void launch_passes(tk_ctx* ctx, Prepared& P, int k, int kc, const ListSlice& see
     }
 }
 
-// 48-entry passes do not spill; a 64-entry pass spills some registers in the
-// epilogue and took about 1.3 times as long at N = 200000 (13 ms against 10 ms),
-// so 64-entry passes are taken where they need fewer than 3/4 as many passes.
+// 48-entry passes do not spill; a 64-entry pass spills registers in the epilogue
+// and took about 1.4 times as long (13.0 against 9.0 ms per pass at N = 200000),
+// so 64-entry passes are taken only where they need fewer than 3/4 as many.
 template <int DP>
 void launch_long(tk_ctx* ctx, Prepared& P, int k, int kc, int32_t* cand_idx, float* cand_val)
 {
